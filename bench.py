@@ -1,0 +1,353 @@
+"""Benchmark of the explicit phase-field step (one JSON line on stdout).
+
+Default workload: 3D Cahn-Hilliard, f=c^2(1-c)^2, 256^3 cells, dt=0.002,
+kappa=M=1, periodic, 1000 explicit steps per bench step, FP32 precision form
+(FP64 compensated reductions).  ``value`` is cell-updates/s with the state
+resident in HBM; ``e2e`` is the same metric through the C ABI call a user's
+update(grid&, steps) makes (mmsp_gpu_update: pinned host buffer in, device
+steps, host buffer out, all inside the timed region).  The FP64 plain form is
+measured on the same grid and reported under ``forms``.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``--impl reference`` times the reference's serial update() restated as the
+C oracle (the reference itself cannot be compiled on the GPU host: its
+source is not there) on all host cores, in FP64, on bounded samples of the
+same grid.  Under torchrun each rank runs an independent replica (the grid
+does not shard across devices in this build): ``scaling`` is "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s (3D Cahn-Hilliard 256^3, 1000 explicit steps)"
+SHAPE = (256, 256, 256)
+SOLVE_STEPS = 1000
+DT, KAPPA, MOB = 0.002, 1.0, 1.0
+MEAN, AMP, SEED = 0.4, 0.02, 2
+WORKLOAD = "ch3d_256_f32"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_tag: str):
+    """DRAM bytes per launch of the named kernel, from the ncu summary in profiles/."""
+    p = os.path.join(ROOT, "profiles", kernel_tag + ".txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap,utilization.gpu")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.p = None
+        self.path = None
+
+    def start(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            v = [x.strip() for x in line.split(",")]
+            if len(v) < 8:
+                continue
+            try:
+                util = float(v[7])
+                if util > 0:
+                    sm.append(float(v[0]))
+                smax = max(smax, float(v[1]))
+            except ValueError:
+                continue
+            for n, x in zip(names, v[3:7]):
+                if x.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples_under_load": len(sm)}
+
+
+def cpu_sample(threads: int, target_s: float = 10.0):
+    """The oracle (the reference's update() restated in C, FP64) on the full
+    grid for as many steps as fit in about target_s seconds."""
+    from mmsp_gb300 import inputs
+    from oracle import pf_oracle
+
+    c = inputs.noisy_composition(SHAPE, MEAN, AMP, SEED)
+    t0 = time.perf_counter()
+    pf_oracle.ch_baseline(c, 1, KAPPA, MOB, DT, threads=threads)
+    t1 = time.perf_counter() - t0
+    n = max(1, int(target_s / max(t1, 1e-3)))
+    t0 = time.perf_counter()
+    pf_oracle.ch_baseline(c, n, KAPPA, MOB, DT, threads=threads)
+    el = time.perf_counter() - t0
+    cells = int(np.prod(SHAPE))
+    return cells * n / el, n, el
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from mmsp_gb300 import inputs
+    from oracle import pf_oracle
+
+    c = inputs.noisy_composition(SHAPE, MEAN, AMP, SEED)
+    t0 = time.perf_counter()
+    pf_oracle.ch_baseline(c, 1, KAPPA, MOB, DT, threads=threads)
+    per = time.perf_counter() - t0
+    sample_steps = max(1, int(4.0 / max(per, 1e-3)))   # about 4 s per bench step
+    for _ in range(args.warmup):
+        pf_oracle.ch_baseline(c, sample_steps, KAPPA, MOB, DT, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pf_oracle.ch_baseline(c, sample_steps, KAPPA, MOB, DT, threads=threads)
+    el = time.perf_counter() - t0
+    cells = int(np.prod(SHAPE))
+    v = cells * sample_steps * args.steps / el
+    sample = "%d of the %d explicit steps of the 256^3 grid per bench step, FP64" % (sample_steps, SOLVE_STEPS)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ch3d_256_f64_cpu", "grid": list(SHAPE), "steps_per_solve": SOLVE_STEPS,
+                   "dt": DT, "kappa": KAPPA, "M": MOB, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    from mmsp_gb300 import inputs, native
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    native.load()
+    cells = int(np.prod(SHAPE))
+    c0 = inputs.noisy_composition(SHAPE, MEAN, AMP, SEED)
+    c0_32 = c0.astype(np.float32)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def make(dtype):
+        d = native.make_desc(SHAPE, 1, dtype, "ch", kappa=KAPPA, mobility=MOB, dt=DT)
+        s = native.Stepper(d)
+        s.set_stream(stream.cuda_stream)
+        return s
+
+    s32 = make(np.float32)
+    init32 = torch.from_numpy(c0_32).cuda()
+    nbytes32 = init32.numel() * 4
+
+    def timed_solve(s, init, nbytes):
+        """One bench step on `stream`: reset the state (untimed), flush L2
+        (untimed), then 1000 steps between CUDA events on the same stream."""
+        with torch.cuda.stream(stream):
+            s.upload_device(init.data_ptr(), nbytes, native.FIELD_MAJOR)
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.step(SOLVE_STEPS)
+            e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        timed_solve(s32, init32, nbytes32)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    evs = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        evs.append(timed_solve(s32, init32, nbytes32))
+    stream.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier()
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    ms_step = float(np.mean(ms))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_step], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = ws * cells * SOLVE_STEPS / (ms_step / 1e3)
+    # accuracy of the timed form: FP32 result vs the FP64 plain form, mass drift
+    st32 = s32.reduce()
+    out32 = s32.download().astype(np.float64)
+
+    # FP64 plain form on the same grid (reported beside the headline)
+    s64 = make(np.float64)
+    init64 = torch.from_numpy(c0).cuda()
+    timed_solve(s64, init64, init64.numel() * 8)
+    stream.synchronize()
+    a, b = timed_solve(s64, init64, init64.numel() * 8)
+    stream.synchronize()
+    ms64 = a.elapsed_time(b)
+    st64 = s64.reduce()
+    out64 = s64.download()
+    err = np.abs(out32 - out64)
+    m0 = float(np.sum(c0))
+    s64.close()
+
+    # end to end through the C ABI with pinned host buffers
+    d32 = native.make_desc(SHAPE, 1, np.float32, "ch", kappa=KAPPA, mobility=MOB, dt=DT)
+    host = torch.empty(cells, dtype=torch.float32, pin_memory=True)
+    hv = host.numpy()
+    L = native.load()
+    import ctypes
+    stats = native.Stats()
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        hv[:] = c0_32.ravel()
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        rc = L.mmsp_gpu_update(ctypes.byref(d32), host.data_ptr(), nbytes32, native.CELL_MAJOR, SOLVE_STEPS,
+                               ctypes.byref(stats))
+        t2 = time.perf_counter()
+        if rc != 0:
+            raise native.GpuError(rc, "mmsp_gpu_update")
+        if i >= args.warmup:
+            e2e_t.append(t2 - t1)
+    e2e_s = float(np.mean(e2e_t))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = ws * cells * SOLVE_STEPS / e2e_s
+
+    peak, peak_kind = peaks()
+    alg_bytes = cells * 2 * 4                     # one read + one write of the FP32 state per step
+    launch_s = ms_step / 1e3 / SOLVE_STEPS
+    achieved = alg_bytes / launch_s / 1e9
+    traffic = profile_traffic("ch_step_kernel_f32_3d_256")
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64, c=0.4+0.02*U(-1,1))",
+        "config": {"workload": WORKLOAD, "grid": list(SHAPE), "steps_per_solve": SOLVE_STEPS, "dt": DT,
+                   "kappa": KAPPA, "M": MOB, "bc": "periodic", "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "l2": "flushed (256 MiB write) before every timed solve; FP32 working set 134 MB"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "ch_step_kernel<float,3,CH>", "peak_source": peak_kind,
+                     "alg_bytes_per_launch": alg_bytes},
+        "e2e": {"value": e2e_val, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes32,
+                "d2h_bytes_per_step": nbytes32 + 16, "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": args.steps * SOLVE_STEPS,
+        "forms": {
+            "f32_precision": {"cell_updates_per_s": value, "ms_per_solve": ms_step,
+                              "max_err_vs_f64": float(err.max()), "l2_err_vs_f64": float(np.sqrt(np.mean(err ** 2))),
+                              "mass_drift": (st32.mass - m0) / m0},
+            "f64_plain": {"cell_updates_per_s": cells * SOLVE_STEPS / (ms64 / 1e3), "ms_per_solve": ms64,
+                          "mass_drift": (st64.mass - m0) / m0},
+        },
+        "clocks": clk,
+        "wall_s_timed_region": wall,
+    }
+    if rank == 0 and args.cpu_baseline:
+        v, n, el = cpu_sample(1)
+        line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                                "sample": "%d explicit FP64 steps of the 256^3 grid (%.1f s), serial C oracle" % (n, el)}
+    s32.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,176 @@
+/* MMSP.gpu.h -- C ABI of the GB300 explicit phase-field step (libmmsp_gpu.so).
+ *
+ * This is the drop-in boundary for MMSP's explicit-Euler update() of
+ * Cahn-Hilliard and multi-order-parameter Allen-Cahn grids.  Each entry point
+ * replaces a piece of the reference's serial path:
+ *
+ *   mmsp_gpu_update    the whole plugin call update(grid&, steps):
+ *                      examples/phase_transitions/cahn-hilliard/explicit/cahn-hilliard.cpp:47-81,
+ *                      examples/coarsening/grain_growth/isotropic/phase_field/graingrowth.cpp:73-111,
+ *                      examples/phase_transitions/allen-cahn/allen-cahn.cpp:47-75
+ *   mmsp_gpu_create    the scratch grids newGrid/temp of update() (copy-ctor,
+ *                      include/MMSP.grid.cpp:71-99) and the grid geometry
+ *                      (setup, include/MMSP.grid.cpp:141-327)
+ *   mmsp_gpu_upload / mmsp_gpu_download
+ *                      the host grid's storage, read as grid<dim,T>::to_buffer
+ *                      order (include/MMSP.grid.cpp:1146-1157) without the
+ *                      per-cell vector length
+ *   mmsp_gpu_step      the step loop of update(): laplacian
+ *                      (include/MMSP.grid.cpp:2049-2088), the model's pointwise
+ *                      update, swap (include/MMSP.grid.cpp:1913-1991) and the
+ *                      periodic halo of ghostswap (include/MMSP.grid.cpp:414-515)
+ *                      as serial check_boundary wraps it (include/MMSP.utility.cpp:42-57)
+ *   mmsp_gpu_reduce    mass and free energy of a snapshot, as reportEnergy()
+ *                      sums them (examples/phase_transitions/cahn-hilliard/
+ *                      convex_splitting/cahn-hilliard.cpp:179-213), in FP64
+ *                      with compensated accumulation
+ *
+ * All functions return MMSP_GPU_OK (0) or a negative MMSP_GPU_E* code; none
+ * throws, exits or prints.  The reference reports the same failures with
+ * exit()/MMSP::Abort() (include/MMSP.utility.cpp:30-36); the C++ wrapper
+ * MMSP.gpu.hpp maps a failure to std::cerr + MMSP::Abort(code).
+ *
+ * Threading: calls on one handle must not overlap; different handles are
+ * independent.  Device work of a handle is ordered on that handle's stream.
+ */
+#ifndef MMSP_GPU_H
+#define MMSP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMSP_GPU_ABI_VERSION 1
+
+/* Status codes. */
+#define MMSP_GPU_OK            0
+#define MMSP_GPU_EINVAL       -1  /* argument out of range, size mismatch, NULL pointer */
+#define MMSP_GPU_ENOMEM       -2  /* device allocation failed or memory budget exceeded */
+#define MMSP_GPU_ECUDA        -3  /* CUDA runtime error (message in mmsp_gpu_last_error) */
+#define MMSP_GPU_EUNSUPPORTED -4  /* valid MMSP input that the device path does not handle */
+#define MMSP_GPU_ETIMEDOUT    -5  /* a bounded wait ran out */
+#define MMSP_GPU_ENODEV       -6  /* no CUDA device, or not an sm_103 device */
+#define MMSP_GPU_ENOTFOUND    -7  /* unknown request id (server) */
+#define MMSP_GPU_ECANCELED    -8  /* request cancelled (server) */
+#define MMSP_GPU_ESTOPPED     -9  /* server stopped */
+
+/* Boundary-condition codes, identical to include/MMSP.utility.h:23-29. */
+#define MMSP_GPU_BC_MIRROR    0
+#define MMSP_GPU_BC_NEUMANN   1
+#define MMSP_GPU_BC_PERIODIC  2
+#define MMSP_GPU_BC_PARALLEL  3
+#define MMSP_GPU_BC_DIRICHLET 4
+
+/* Storage type of the state (and the arithmetic of the step). */
+#define MMSP_GPU_F64 0   /* plain form: reference operation order, no fused multiply-add */
+#define MMSP_GPU_F32 1   /* precision form: FP32 state and arithmetic, FP64 reductions */
+
+/* Models.  Parameters are read from mmsp_gpu_desc as noted. */
+#define MMSP_GPU_CH       0  /* Cahn-Hilliard, f=c^2(1-c)^2: mu = 2c(1-c)(1-2c) - kappa*lap c;
+                                c' = c + dt*mobility*lap mu                                   */
+#define MMSP_GPU_CH_POLY  1  /* Cahn-Hilliard as shipped (cahn-hilliard.cpp:71):
+                                mu = -r c + u c^3 - kappa*lap c                              */
+#define MMSP_GPU_AC       2  /* multi-order Allen-Cahn, f = sum(-e^2/2+e^4/4) + gamma*sum_{i<j} e_i^2 e_j^2:
+                                e' = e - dt*mobility*(-e + e^3 + 2 gamma e (sum e^2 - e^2) - kappa*lap e) */
+#define MMSP_GPU_GG       3  /* grain growth as shipped (graingrowth.cpp:105):
+                                e' = e - dt*(-e - e^3 + 2 (e sum e^2 - lap e))                */
+#define MMSP_GPU_AC_POLY  4  /* scalar Allen-Cahn as shipped (allen-cahn.cpp:70), fields=1:
+                                p' = p - dt*mobility*(-r p + u p^3 - kappa*lap p)             */
+
+/* Host/device layouts of vector-valued grids (fields > 1). */
+#define MMSP_GPU_CELL_MAJOR  0  /* value j of cell i at i*fields + j (grid<dim,vector<T>> order) */
+#define MMSP_GPU_FIELD_MAJOR 1  /* value j of cell i at j*cells + i (the device layout)          */
+
+typedef struct mmsp_gpu_desc {
+    int dim;          /* 1, 2 or 3 */
+    int n[3];         /* extents per axis (x1-x0), axis 0 slowest; unused axes ignored */
+    int fields;       /* values per cell: 1 for grid<dim,T>, N for grid<dim,vector<T>> */
+    int dtype;        /* MMSP_GPU_F64 or MMSP_GPU_F32 */
+    int model;        /* MMSP_GPU_CH ... MMSP_GPU_AC_POLY */
+    int bc[3][2];     /* lower/upper boundary per axis; the device path takes periodic only */
+    double dx[3];     /* cell spacing per axis */
+    double dt;        /* time step */
+    double kappa;     /* gradient coefficient (K of the shipped examples) */
+    double mobility;  /* M (Cahn-Hilliard) or L (Allen-Cahn) */
+    double gamma;     /* grain-boundary coupling (MMSP_GPU_AC) */
+    double r, u;      /* polynomial coefficients (MMSP_GPU_CH_POLY, MMSP_GPU_AC_POLY) */
+} mmsp_gpu_desc;
+
+typedef struct mmsp_gpu_stats {
+    double mass;      /* dV * sum of all values (all fields) */
+    double energy;    /* dV * sum of the model's free-energy density + kappa/2 |grad|^2 */
+    double gpu_ms;    /* device time of the last mmsp_gpu_step call, CUDA events on the handle's stream */
+    int64_t steps;    /* steps advanced since the last upload */
+} mmsp_gpu_stats;
+
+typedef struct mmsp_gpu_handle mmsp_gpu_handle;
+
+/* Library ABI version (MMSP_GPU_ABI_VERSION). */
+int mmsp_gpu_version(void);
+
+/* Text for a status code. */
+const char* mmsp_gpu_strerror(int code);
+
+/* Fill *desc with the defaults of a periodic grid of the given model: dx=1,
+ * dt/kappa/mobility/gamma of the shipped example for that model. */
+int mmsp_gpu_desc_init(mmsp_gpu_desc* desc, int dim, const int* n, int fields,
+                       int dtype, int model);
+
+/* Validate a descriptor without touching the device (0, EINVAL or EUNSUPPORTED). */
+int mmsp_gpu_validate(const mmsp_gpu_desc* desc);
+
+/* Device bytes a handle for this descriptor allocates. */
+int mmsp_gpu_footprint(const mmsp_gpu_desc* desc, size_t* bytes);
+
+/* Create a handle: validates the descriptor, allocates two state buffers
+ * (the grid and its newGrid) and the reduction scratch on the current device,
+ * and a private non-blocking stream. */
+int mmsp_gpu_create(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc);
+
+/* Free the handle's device memory and stream. NULL is accepted. */
+int mmsp_gpu_destroy(mmsp_gpu_handle* h);
+
+/* Order the handle's work on an external cudaStream_t (NULL: back to the
+ * private stream).  Stream-ordered with previously queued work on the old stream. */
+int mmsp_gpu_set_stream(mmsp_gpu_handle* h, void* cuda_stream);
+
+/* Copy a host grid in (pageable or pinned memory); bytes must equal
+ * cells*fields*sizeof(T).  Resets the step counter.  Synchronous. */
+int mmsp_gpu_upload(mmsp_gpu_handle* h, const void* host, size_t bytes, int layout);
+
+/* Copy the current state out to host memory.  Synchronous. */
+int mmsp_gpu_download(mmsp_gpu_handle* h, void* host, size_t bytes, int layout);
+
+/* Same as upload/download with a device pointer, stream-ordered (asynchronous). */
+int mmsp_gpu_upload_device(mmsp_gpu_handle* h, const void* dev, size_t bytes, int layout);
+int mmsp_gpu_download_device(mmsp_gpu_handle* h, void* dev, size_t bytes, int layout);
+
+/* Advance the state by `steps` explicit-Euler steps (asynchronous; CUDA
+ * graphs replay long runs).  steps == 0 is a no-op. */
+int mmsp_gpu_step(mmsp_gpu_handle* h, int steps);
+
+/* Wait for the handle's queued work. */
+int mmsp_gpu_synchronize(mmsp_gpu_handle* h);
+
+/* Mass and free energy of the current state (FP64, compensated), plus the
+ * device time of the last step call and the step counter.  Synchronous. */
+int mmsp_gpu_reduce(mmsp_gpu_handle* h, mmsp_gpu_stats* stats);
+
+/* Device pointer of the current state (field-major), valid until the next step. */
+int mmsp_gpu_state(mmsp_gpu_handle* h, void** dev_ptr);
+
+/* Message of the last failure on this handle ("" if none). */
+const char* mmsp_gpu_last_error(const mmsp_gpu_handle* h);
+
+/* One call per update(grid&, steps): create, upload `host`, advance `steps`,
+ * download into `host`, destroy.  `stats` may be NULL. */
+int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t bytes, int layout,
+                    int steps, mmsp_gpu_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MMSP_GPU_H */

@@ -1,0 +1,164 @@
+// MMSP.gpu.hpp -- drop-in GB300 update() for MMSP grids.
+//
+// Include after MMSP.hpp and link libmmsp_gpu.so.  A plugin keeps MMSP's
+// contract (include/MMSP.main.hpp:5-26): it defines generate() and
+//
+//     template <int dim, typename T> void update(MMSP::grid<dim,T>& g, int steps)
+//
+// and forwards the body to MMSP::gpu::update with the model it integrates,
+// e.g. for the explicit Cahn-Hilliard example
+// (examples/phase_transitions/cahn-hilliard/explicit/cahn-hilliard.cpp:47-81):
+//
+//     template <int dim, typename T> void update(MMSP::grid<dim,T>& g, int steps)
+//     { MMSP::gpu::update(g, steps, MMSP::gpu::cahn_hilliard(1.0, 1.0, 0.005)); }
+//
+// and for isotropic phase-field grain growth
+// (examples/coarsening/grain_growth/isotropic/phase_field/graingrowth.cpp:73-111):
+//
+//     template <int dim, typename T> void update(MMSP::grid<dim,MMSP::vector<T> >& g, int steps)
+//     { MMSP::gpu::update(g, steps, MMSP::gpu::grain_growth_shipped(0.01)); }
+//
+// The grid is read once, advanced `steps` explicit steps on the device and
+// written back, like the reference's update() which swaps its result into the
+// caller's grid (cahn-hilliard.cpp:78).  grid<dim,double> runs the FP64 plain
+// form (the reference's operation order, bit-identical results);
+// grid<dim,float> runs the FP32 precision form.  Output, file format and
+// main() stay the reference's own.
+//
+// Errors follow the reference: a message on std::cerr and MMSP::Abort(code)
+// (include/MMSP.utility.cpp:30-36).  gpu::try_update returns the code instead.
+//
+// The wrapper uses only MMSP's free grid functions (nodes, fields, g0, g1,
+// x0, x1, b0, b1, dx) and operator()(int), so any container with that
+// interface works.
+#ifndef MMSP_GPU_HPP
+#define MMSP_GPU_HPP
+
+#include <iostream>
+#include <vector>
+
+#include "MMSP.gpu.h"
+
+namespace MMSP {
+namespace gpu {
+
+struct Model {
+    int model;
+    double dt, kappa, mobility, gamma, r, u;
+};
+
+// f = c^2(1-c)^2: mu = 2c(1-c)(1-2c) - kappa*lap c; dc/dt = M lap mu
+inline Model cahn_hilliard(double kappa, double M, double dt)
+{
+    Model m = {MMSP_GPU_CH, dt, kappa, M, 0.0, 0.0, 0.0};
+    return m;
+}
+// cahn-hilliard.cpp:59-76 as shipped: mu = -r c + u c^3 - K lap c
+inline Model cahn_hilliard_shipped(double r, double u, double K, double M, double dt)
+{
+    Model m = {MMSP_GPU_CH_POLY, dt, K, M, 0.0, r, u};
+    return m;
+}
+// f = sum(-e^2/2 + e^4/4) + gamma sum_{i<j} e_i^2 e_j^2, de/dt = -L (df/de - kappa lap e)
+inline Model allen_cahn(double gamma, double kappa, double L, double dt)
+{
+    Model m = {MMSP_GPU_AC, dt, kappa, L, gamma, 0.0, 0.0};
+    return m;
+}
+// graingrowth.cpp:84-106 as shipped
+inline Model grain_growth_shipped(double dt)
+{
+    Model m = {MMSP_GPU_GG, dt, 2.0, 1.0, 1.0, 0.0, 0.0};
+    return m;
+}
+// allen-cahn.cpp:57-70 as shipped (scalar grid)
+inline Model allen_cahn_shipped(double r, double u, double K, double M, double dt)
+{
+    Model m = {MMSP_GPU_AC_POLY, dt, K, M, 0.0, r, u};
+    return m;
+}
+
+template <typename T> struct dtype_of;
+template <> struct dtype_of<double> { static const int value = MMSP_GPU_F64; };
+template <> struct dtype_of<float> { static const int value = MMSP_GPU_F32; };
+
+template <class G>
+int describe(const G& g, int dim, int fields, int dtype, const Model& m, mmsp_gpu_desc* d)
+{
+    int n[3] = {1, 1, 1};
+    for (int a = 0; a < dim; a++) {
+        // one serial domain covering the whole grid (no MPI decomposition)
+        if (x0(g, a) != g0(g, a) || x1(g, a) != g1(g, a)) return MMSP_GPU_EUNSUPPORTED;
+        n[a] = g1(g, a) - g0(g, a);
+    }
+    int rc = mmsp_gpu_desc_init(d, dim, n, fields, dtype, m.model);
+    if (rc == MMSP_GPU_EINVAL) return rc;
+    for (int a = 0; a < dim; a++) {
+        d->dx[a] = dx(g, a);
+        d->bc[a][0] = b0(g, a);
+        d->bc[a][1] = b1(g, a);
+    }
+    d->dt = m.dt;
+    d->kappa = m.kappa;
+    d->mobility = m.mobility;
+    d->gamma = m.gamma;
+    d->r = m.r;
+    d->u = m.u;
+    return mmsp_gpu_validate(d);
+}
+
+inline int report(int rc, const char* what)
+{
+    if (rc != MMSP_GPU_OK)
+        std::cerr << "MMSP::gpu::update: " << what << ": " << mmsp_gpu_strerror(rc) << " (" << rc << ")" << std::endl;
+    return rc;
+}
+
+// Scalar grids: grid<dim,double> (plain form) and grid<dim,float> (precision form).
+template <template <int, typename> class Grid, int dim, typename T>
+int try_update(Grid<dim, T>& g, int steps, const Model& m, mmsp_gpu_stats* stats = 0)
+{
+    mmsp_gpu_desc d;
+    int rc = describe(g, dim, 1, dtype_of<T>::value, m, &d);
+    if (rc) return report(rc, "descriptor");
+    const int n = nodes(g);
+    std::vector<T> buf((size_t)n);
+    for (int i = 0; i < n; i++) buf[i] = g(i);
+    rc = mmsp_gpu_update(&d, &buf[0], buf.size() * sizeof(T), MMSP_GPU_CELL_MAJOR, steps, stats);
+    if (rc) return report(rc, "device step");
+    for (int i = 0; i < n; i++) g(i) = buf[i];
+    return MMSP_GPU_OK;
+}
+
+// Vector grids: grid<dim,vector<double>> / grid<dim,vector<float>>.  Values
+// are gathered cell-major (to_buffer order without the per-cell length).
+template <template <int, typename> class Grid, template <typename> class Vec, int dim, typename T>
+int try_update(Grid<dim, Vec<T> >& g, int steps, const Model& m, mmsp_gpu_stats* stats = 0)
+{
+    const int N = fields(g);
+    mmsp_gpu_desc d;
+    int rc = describe(g, dim, N, dtype_of<T>::value, m, &d);
+    if (rc) return report(rc, "descriptor");
+    const int n = nodes(g);
+    std::vector<T> buf((size_t)n * N);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < N; j++) buf[(size_t)i * N + j] = g(i)[j];
+    rc = mmsp_gpu_update(&d, &buf[0], buf.size() * sizeof(T), MMSP_GPU_CELL_MAJOR, steps, stats);
+    if (rc) return report(rc, "device step");
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < N; j++) g(i)[j] = buf[(size_t)i * N + j];
+    return MMSP_GPU_OK;
+}
+
+// The plugin-facing call: aborts like the reference on failure.
+template <class G>
+void update(G& g, int steps, const Model& m)
+{
+    int rc = try_update(g, steps, m);
+    if (rc) MMSP::Abort(rc);
+}
+
+}  // namespace gpu
+}  // namespace MMSP
+
+#endif

@@ -1,0 +1,445 @@
+// mmsp_gpu.cu -- the C ABI of include/MMSP.gpu.h: handles, validation,
+// host/device transfers, CUDA-graph replay of step chunks, reductions.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "MMSP.gpu.h"
+#include "pf_internal.h"
+
+using pf::Coeffs;
+using pf::Geom;
+using pf::StepPlan;
+
+struct mmsp_gpu_handle {
+    mmsp_gpu_desc d;
+    Geom g;
+    Coeffs c;
+    StepPlan plan;
+    int device;
+    size_t esize, elems, bytes;
+    void* buf[2];
+    int cur;                 // buf[cur] holds the state
+    double* partials;        // reduction scratch
+    cudaStream_t own;        // private stream
+    cudaStream_t stream;     // stream in use
+    cudaEvent_t ev0, ev1;
+    bool timed;              // ev0/ev1 bracket the last step call
+    int64_t steps;
+    // CUDA graph of kGraphSteps steps starting from buf[0] (an even count ends in buf[0])
+    cudaGraphExec_t graph;
+    char err[512];
+};
+
+static const int kGraphSteps = 64;
+static const int kGraphMin = 2 * kGraphSteps;   // replay only for runs this long
+
+static int fail(mmsp_gpu_handle* h, int code, const char* fmt, const char* a = "", const char* b = "")
+{
+    if (h) snprintf(h->err, sizeof(h->err), fmt, a, b);
+    return code;
+}
+
+static int cuda_fail(mmsp_gpu_handle* h, cudaError_t e, const char* where)
+{
+    if (h) snprintf(h->err, sizeof(h->err), "%s: %s", where, cudaGetErrorString(e));
+    cudaGetLastError();   // clear a non-sticky error
+    return MMSP_GPU_ECUDA;
+}
+
+extern "C" int mmsp_gpu_version(void) { return MMSP_GPU_ABI_VERSION; }
+
+extern "C" const char* mmsp_gpu_strerror(int code)
+{
+    switch (code) {
+    case MMSP_GPU_OK: return "ok";
+    case MMSP_GPU_EINVAL: return "invalid argument";
+    case MMSP_GPU_ENOMEM: return "out of device memory";
+    case MMSP_GPU_ECUDA: return "CUDA error";
+    case MMSP_GPU_EUNSUPPORTED: return "unsupported configuration";
+    case MMSP_GPU_ETIMEDOUT: return "timed out";
+    case MMSP_GPU_ENODEV: return "no suitable CUDA device";
+    case MMSP_GPU_ENOTFOUND: return "unknown request";
+    case MMSP_GPU_ECANCELED: return "cancelled";
+    case MMSP_GPU_ESTOPPED: return "server stopped";
+    default: return "unknown status";
+    }
+}
+
+extern "C" int mmsp_gpu_desc_init(mmsp_gpu_desc* d, int dim, const int* n, int fields, int dtype, int model)
+{
+    if (!d || !n) return MMSP_GPU_EINVAL;
+    memset(d, 0, sizeof(*d));
+    d->dim = dim;
+    for (int a = 0; a < 3; a++) {
+        d->n[a] = (a < dim) ? n[a] : 1;
+        d->dx[a] = 1.0;
+        d->bc[a][0] = d->bc[a][1] = MMSP_GPU_BC_PERIODIC;
+    }
+    d->fields = fields;
+    d->dtype = dtype;
+    d->model = model;
+    d->mobility = 1.0;
+    d->kappa = 1.0;
+    d->r = 1.0;
+    d->u = 1.0;
+    d->gamma = 1.0;
+    switch (model) {
+    case MMSP_GPU_CH: d->dt = 0.005; break;                       // 2D configuration of the CH study
+    case MMSP_GPU_CH_POLY: d->dt = 0.01; break;                   // cahn-hilliard.cpp:59-63
+    case MMSP_GPU_AC: d->dt = 0.05; d->kappa = 2.0; d->gamma = 1.5; break;
+    case MMSP_GPU_GG: d->dt = 0.01; d->kappa = 2.0; break;        // graingrowth.cpp:84
+    case MMSP_GPU_AC_POLY: d->dt = 0.01; break;                   // allen-cahn.cpp:57-61
+    default: return MMSP_GPU_EINVAL;
+    }
+    return mmsp_gpu_validate(d);
+}
+
+static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
+{
+#define BAD(code, ...) do { if (why) snprintf(why, nwhy, __VA_ARGS__); return code; } while (0)
+    if (!d) BAD(MMSP_GPU_EINVAL, "NULL descriptor");
+    if (d->dim < 1 || d->dim > 3) BAD(MMSP_GPU_EINVAL, "dim %d outside 1..3", d->dim);
+    if (d->dtype != MMSP_GPU_F64 && d->dtype != MMSP_GPU_F32) BAD(MMSP_GPU_EINVAL, "dtype %d", d->dtype);
+    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_AC_POLY) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
+    long long cells = 1;
+    for (int a = 0; a < d->dim; a++) {
+        if (d->n[a] < 1) BAD(MMSP_GPU_EINVAL, "extent n[%d]=%d", a, d->n[a]);
+        if (!(d->dx[a] > 0.0) || !isfinite(d->dx[a])) BAD(MMSP_GPU_EINVAL, "dx[%d] not positive and finite", a);
+        for (int s = 0; s < 2; s++) {
+            int b = d->bc[a][s];
+            if (b < MMSP_GPU_BC_MIRROR || b > MMSP_GPU_BC_DIRICHLET) BAD(MMSP_GPU_EINVAL, "bc[%d][%d]=%d", a, s, b);
+            if (b != MMSP_GPU_BC_PERIODIC)
+                BAD(MMSP_GPU_EUNSUPPORTED, "bc[%d][%d]=%d: the device step takes periodic boundaries only", a, s, b);
+        }
+        cells *= d->n[a];
+        if (cells > (1LL << 40)) BAD(MMSP_GPU_EINVAL, "grid too large");
+    }
+    bool scalar_model = d->model == MMSP_GPU_CH || d->model == MMSP_GPU_CH_POLY || d->model == MMSP_GPU_AC_POLY;
+    if (scalar_model && d->fields != 1) BAD(MMSP_GPU_EINVAL, "model %d takes fields=1, got %d", d->model, d->fields);
+    if (d->fields < 1) BAD(MMSP_GPU_EINVAL, "fields=%d", d->fields);
+    if (d->fields > 32) BAD(MMSP_GPU_EUNSUPPORTED, "fields=%d above 32", d->fields);
+    long long yz = 1;
+    for (int a = (d->dim >= 2 ? d->dim - 2 : 0); a < d->dim; a++) yz *= d->n[a];
+    if (yz >= (1LL << 31)) BAD(MMSP_GPU_EUNSUPPORTED, "plane of %lld cells above 2^31", yz);
+    if ((long long)d->n[0] >= (1LL << 31)) BAD(MMSP_GPU_EINVAL, "extent too large");
+    if (!isfinite(d->dt) || !isfinite(d->kappa) || !isfinite(d->mobility) || !isfinite(d->gamma) ||
+        !isfinite(d->r) || !isfinite(d->u))
+        BAD(MMSP_GPU_EINVAL, "non-finite model parameter");
+    return MMSP_GPU_OK;
+#undef BAD
+}
+
+extern "C" int mmsp_gpu_validate(const mmsp_gpu_desc* d) { return validate(d, nullptr, 0); }
+
+static size_t esize_of(const mmsp_gpu_desc* d) { return d->dtype == MMSP_GPU_F64 ? sizeof(double) : sizeof(float); }
+
+static size_t state_bytes(const mmsp_gpu_desc* d)
+{
+    size_t n = (size_t)d->fields;
+    for (int a = 0; a < d->dim; a++) n *= (size_t)d->n[a];
+    return n * esize_of(d);
+}
+
+extern "C" int mmsp_gpu_footprint(const mmsp_gpu_desc* d, size_t* bytes)
+{
+    int rc = mmsp_gpu_validate(d);
+    if (rc) return rc;
+    if (!bytes) return MMSP_GPU_EINVAL;
+    *bytes = 2 * state_bytes(d) + pf::kPartialsBytes;
+    return MMSP_GPU_OK;
+}
+
+static void release(mmsp_gpu_handle* h)
+{
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->buf[0]) cudaFree(h->buf[0]);
+    if (h->buf[1]) cudaFree(h->buf[1]);
+    if (h->partials) cudaFree(h->partials);
+    if (h->own) cudaStreamDestroy(h->own);
+}
+
+static int make_plan(mmsp_gpu_handle* h)
+{
+    bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
+    cudaError_t e = ch ? pf::plan_ch(h->d, h->g, &h->plan) : pf::plan_ac(h->d, h->g, &h->plan);
+    if (e != cudaSuccess) {
+        if (!h->plan.ok && !ch) return fail(h, MMSP_GPU_EUNSUPPORTED, "%s", "too many fields for shared memory");
+        return cuda_fail(h, e, "plan");
+    }
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_create(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc)
+{
+    if (!out) return MMSP_GPU_EINVAL;
+    *out = nullptr;
+    int rc = validate(desc, nullptr, 0);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return MMSP_GPU_ENODEV;
+    }
+    mmsp_gpu_handle* h = new (std::nothrow) mmsp_gpu_handle();
+    if (!h) return MMSP_GPU_ENOMEM;
+    memset(h, 0, sizeof(*h));
+    h->d = *desc;
+    for (int a = desc->dim; a < 3; a++) h->d.n[a] = 1;
+    h->g = pf::make_geom(h->d);
+    h->c = pf::make_coeffs(h->d);
+    cudaGetDevice(&h->device);
+    h->esize = esize_of(&h->d);
+    h->bytes = state_bytes(&h->d);
+    h->elems = h->bytes / h->esize;
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking)) != cudaSuccess) goto cuda_err;
+    h->stream = h->own;
+    if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) goto cuda_err;
+    if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) goto cuda_err;
+    if (cudaMalloc(&h->buf[0], h->bytes) != cudaSuccess || cudaMalloc(&h->buf[1], h->bytes) != cudaSuccess ||
+        cudaMalloc((void**)&h->partials, pf::kPartialsBytes) != cudaSuccess) {
+        cudaGetLastError();
+        release(h);
+        delete h;
+        return MMSP_GPU_ENOMEM;
+    }
+    rc = make_plan(h);
+    if (rc) {
+        release(h);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return MMSP_GPU_OK;
+cuda_err:
+    release(h);
+    delete h;
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? MMSP_GPU_ENOMEM : MMSP_GPU_ECUDA;
+}
+
+extern "C" int mmsp_gpu_destroy(mmsp_gpu_handle* h)
+{
+    if (!h) return MMSP_GPU_OK;
+    cudaStreamSynchronize(h->stream);
+    release(h);
+    delete h;
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_set_stream(mmsp_gpu_handle* h, void* s)
+{
+    if (!h) return MMSP_GPU_EINVAL;
+    cudaStream_t ns = s ? (cudaStream_t)s : h->own;
+    if (ns != h->stream) {
+        // order the new stream after everything queued on the old one
+        cudaEvent_t ev;
+        cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(h, e, "set_stream");
+        cudaEventRecord(ev, h->stream);
+        cudaStreamWaitEvent(ns, ev, 0);
+        cudaEventDestroy(ev);
+        h->stream = ns;
+    }
+    return MMSP_GPU_OK;
+}
+
+static int check_io(mmsp_gpu_handle* h, const void* p, size_t bytes, int layout)
+{
+    if (!h || !p) return MMSP_GPU_EINVAL;
+    if (bytes != h->bytes) {
+        char a[64], b[64];
+        snprintf(a, sizeof a, "%zu", bytes);
+        snprintf(b, sizeof b, "%zu", h->bytes);
+        return fail(h, MMSP_GPU_EINVAL, "transfer of %s bytes, state is %s bytes", a, b);
+    }
+    if (layout != MMSP_GPU_CELL_MAJOR && layout != MMSP_GPU_FIELD_MAJOR) return fail(h, MMSP_GPU_EINVAL, "%s", "layout");
+    return MMSP_GPU_OK;
+}
+
+static int upload(mmsp_gpu_handle* h, const void* src, size_t bytes, int layout, cudaMemcpyKind kind, bool sync)
+{
+    int rc = check_io(h, src, bytes, layout);
+    if (rc) return rc;
+    bool transpose = layout == MMSP_GPU_CELL_MAJOR && h->d.fields > 1;
+    h->cur = 0;
+    void* dst = transpose ? h->buf[1] : h->buf[0];
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload");
+    if (transpose) {
+        e = pf::launch_transpose(h->d.dtype, h->buf[1], h->buf[0], h->g.cells, h->d.fields, true, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "upload transpose");
+    }
+    h->steps = 0;
+    h->timed = false;
+    if (sync && (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(h, e, "upload sync");
+    return MMSP_GPU_OK;
+}
+
+static int download(mmsp_gpu_handle* h, void* dst, size_t bytes, int layout, cudaMemcpyKind kind, bool sync)
+{
+    int rc = check_io(h, dst, bytes, layout);
+    if (rc) return rc;
+    bool transpose = layout == MMSP_GPU_CELL_MAJOR && h->d.fields > 1;
+    const void* src = h->buf[h->cur];
+    cudaError_t e;
+    if (transpose) {
+        // the other state buffer is free between steps
+        e = pf::launch_transpose(h->d.dtype, h->buf[h->cur], h->buf[h->cur ^ 1], h->g.cells, h->d.fields, false,
+                                 h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "download transpose");
+        src = h->buf[h->cur ^ 1];
+    }
+    e = cudaMemcpyAsync(dst, src, bytes, kind, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "download");
+    if (sync && (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(h, e, "download sync");
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_upload(mmsp_gpu_handle* h, const void* host, size_t bytes, int layout)
+{
+    return upload(h, host, bytes, layout, cudaMemcpyHostToDevice, true);
+}
+extern "C" int mmsp_gpu_download(mmsp_gpu_handle* h, void* host, size_t bytes, int layout)
+{
+    return download(h, host, bytes, layout, cudaMemcpyDeviceToHost, true);
+}
+extern "C" int mmsp_gpu_upload_device(mmsp_gpu_handle* h, const void* dev, size_t bytes, int layout)
+{
+    return upload(h, dev, bytes, layout, cudaMemcpyDeviceToDevice, false);
+}
+extern "C" int mmsp_gpu_download_device(mmsp_gpu_handle* h, void* dev, size_t bytes, int layout)
+{
+    return download(h, dev, bytes, layout, cudaMemcpyDeviceToDevice, false);
+}
+
+static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s)
+{
+    bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
+    const void* in = h->buf[h->cur];
+    void* out = h->buf[h->cur ^ 1];
+    cudaError_t e = ch ? pf::launch_ch(h->plan, h->d, h->g, h->c, in, out, s)
+                       : pf::launch_ac(h->plan, h->d, h->g, h->c, in, out, s);
+    h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913
+    return e;
+}
+
+static int build_graph(mmsp_gpu_handle* h)
+{
+    if (h->graph) return MMSP_GPU_OK;   // kernel nodes do not depend on the launch stream
+    // capture on a private stream so a caller's legacy/default stream works too
+    cudaStream_t cs;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(h, e, "graph stream");
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return cuda_fail(h, e, "begin capture");
+    }
+    int saved = h->cur;
+    h->cur = 0;
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < kGraphSteps && le == cudaSuccess; i++) le = one_step(h, cs);
+    h->cur = saved;
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(cs, &graph);
+    cudaStreamDestroy(cs);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(h, le != cudaSuccess ? le : e, "capture");
+    }
+    e = cudaGraphInstantiate(&h->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        h->graph = nullptr;
+        return cuda_fail(h, e, "instantiate");
+    }
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
+{
+    if (!h || steps < 0) return MMSP_GPU_EINVAL;
+    if (steps == 0) return MMSP_GPU_OK;
+    cudaError_t e = cudaEventRecord(h->ev0, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "event");
+    int left = steps;
+    if (steps >= kGraphMin) {
+        int rc = build_graph(h);
+        if (rc) return rc;
+        if (h->cur == 1) {
+            if ((e = one_step(h, h->stream)) != cudaSuccess) return cuda_fail(h, e, "step");
+            left--;
+        }
+        while (left >= kGraphSteps) {
+            if ((e = cudaGraphLaunch(h->graph, h->stream)) != cudaSuccess) return cuda_fail(h, e, "graph launch");
+            left -= kGraphSteps;   // even count: the state is back in buf[0]
+        }
+    }
+    while (left > 0) {
+        if ((e = one_step(h, h->stream)) != cudaSuccess) return cuda_fail(h, e, "step");
+        left--;
+    }
+    if ((e = cudaEventRecord(h->ev1, h->stream)) != cudaSuccess) return cuda_fail(h, e, "event");
+    h->timed = true;
+    h->steps += steps;
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_synchronize(mmsp_gpu_handle* h)
+{
+    if (!h) return MMSP_GPU_EINVAL;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_reduce(mmsp_gpu_handle* h, mmsp_gpu_stats* st)
+{
+    if (!h || !st) return MMSP_GPU_EINVAL;
+    cudaError_t e = pf::launch_reduce(h->d, h->g, h->c, h->buf[h->cur], h->partials, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "reduce");
+    double res[2];
+    e = cudaMemcpyAsync(res, h->partials + 4 * pf::kReduceBlocks, sizeof(res), cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "reduce copy");
+    if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(h, e, "reduce sync");
+    st->mass = res[0];
+    st->energy = res[1];
+    st->steps = h->steps;
+    st->gpu_ms = 0.0;
+    if (h->timed) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) == cudaSuccess) st->gpu_ms = ms;
+        else cudaGetLastError();
+    }
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_state(mmsp_gpu_handle* h, void** p)
+{
+    if (!h || !p) return MMSP_GPU_EINVAL;
+    *p = h->buf[h->cur];
+    return MMSP_GPU_OK;
+}
+
+extern "C" const char* mmsp_gpu_last_error(const mmsp_gpu_handle* h) { return h ? h->err : "NULL handle"; }
+
+extern "C" int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t bytes, int layout, int steps,
+                               mmsp_gpu_stats* stats)
+{
+    if (!host || steps < 0) return MMSP_GPU_EINVAL;
+    mmsp_gpu_handle* h = nullptr;
+    int rc = mmsp_gpu_create(&h, desc);
+    if (rc) return rc;
+    rc = mmsp_gpu_upload(h, host, bytes, layout);
+    if (!rc) rc = mmsp_gpu_step(h, steps);
+    if (!rc && stats) rc = mmsp_gpu_reduce(h, stats);
+    if (!rc) rc = mmsp_gpu_download(h, host, bytes, layout);
+    mmsp_gpu_destroy(h);
+    return rc;
+}

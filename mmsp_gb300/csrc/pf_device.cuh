@@ -1,0 +1,130 @@
+// pf_device.cuh -- device arithmetic shared by the step and reduction kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "MMSP.gpu.h"
+#include "pf_internal.h"
+
+namespace pf {
+
+// Arithmetic of the two forms.  The FP64 (plain) form rounds every operation
+// separately with the _rn intrinsics, so nothing is fused into a
+// multiply-add: that is how the reference's serial x86-64 build evaluates
+// the same expressions, and it keeps the device result bit-identical to it.
+// The FP32 (precision) form uses ordinary operators and lets the compiler
+// contract them.
+template <typename T> struct Ar;
+template <> struct Ar<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+};
+template <> struct Ar<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+};
+
+// x^3 for the shipped examples' pow(x,3).  The exact cube is
+// q + f + e*x with x*x = p + e and p*x = q + f split by the fused
+// multiply-add error-free product (Dekker 1971; Ogita, Rump and Oishi 2005);
+// rounding q + (f + e*x) once more gives the correctly rounded cube except
+// in rare ties, within the 1-ulp bound of the C library's pow.
+static __device__ __forceinline__ double cube(double x)
+{
+    double p = __dmul_rn(x, x);
+    double e = __fma_rn(x, x, -p);
+    double q = __dmul_rn(p, x);
+    double f = __fma_rn(p, x, -q);
+    return __dadd_rn(q, __fma_rn(e, x, f));
+}
+static __device__ __forceinline__ float cube(float x) { return x * x * x; }
+
+// Model constants in the state type.
+template <typename T> struct P {
+    T wx, wy, wz;      // Laplacian weights of padded axes X, Y, Z
+    T kappa, dtm, gamma2, neg_r, u;
+};
+
+// One axis of MMSP::laplacian (grid.cpp:2055-2064):
+//   acc + weight * (yh - 2.0*y + yl), with y2 = 2.0*y precomputed (exact).
+template <typename T, bool UNIT_W>
+static __device__ __forceinline__ T lap_axis(T acc, T yh, T y2, T yl, T w)
+{
+    using A = Ar<T>;
+    T t = A::add(A::sub(yh, y2), yl);
+    if (!UNIT_W) t = A::mul(w, t);
+    return A::add(acc, t);
+}
+
+// Chemical potential of the Cahn-Hilliard models.
+template <typename T, int MODEL>
+static __device__ __forceinline__ T ch_mu(T phi, T lap, const P<T>& p)
+{
+    using A = Ar<T>;
+    if (MODEL == MMSP_GPU_CH) {
+        // 2.0*phi*(1.0-phi)*(1.0-2.0*phi) - K*lap
+        T t2 = A::mul(T(2), phi);
+        T fp = A::mul(A::mul(t2, A::sub(T(1), phi)), A::sub(T(1), t2));
+        return A::sub(fp, A::mul(p.kappa, lap));
+    } else {
+        // -r*phi + u*pow(phi,3) - K*lap   (cahn-hilliard.cpp:71)
+        T a = A::add(A::mul(p.neg_r, phi), A::mul(p.u, cube(phi)));
+        return A::sub(a, A::mul(p.kappa, lap));
+    }
+}
+
+// New value of one order parameter of the Allen-Cahn models.
+template <typename T, int MODEL>
+static __device__ __forceinline__ T ac_new(T phi, T sum, T lap, const P<T>& p)
+{
+    using A = Ar<T>;
+    if (MODEL == MMSP_GPU_AC) {
+        // phi - dt*L*(-phi + phi*phi*phi + 2.0*gamma*phi*(sum - phi*phi) - kappa*lap)
+        T p2 = A::mul(phi, phi);
+        T p3 = A::mul(p2, phi);
+        T a = A::add(-phi, p3);
+        T g = A::mul(A::mul(p.gamma2, phi), A::sub(sum, p2));
+        T c = A::sub(A::add(a, g), A::mul(p.kappa, lap));
+        return A::sub(phi, A::mul(p.dtm, c));
+    } else if (MODEL == MMSP_GPU_GG) {
+        // phi - dt*(-phi - pow(phi,3) + 2.0*(phi*sum - lap))   (graingrowth.cpp:105)
+        T e = A::add(A::sub(-phi, cube(phi)), A::mul(T(2), A::sub(A::mul(phi, sum), lap)));
+        return A::sub(phi, A::mul(p.dtm, e));
+    } else {
+        // phi - dt*M*(-r*phi + u*pow(phi,3) - K*lap)   (allen-cahn.cpp:70)
+        T e = A::sub(A::add(A::mul(p.neg_r, phi), A::mul(p.u, cube(phi))), A::mul(p.kappa, lap));
+        return A::sub(phi, A::mul(p.dtm, e));
+    }
+}
+
+// Periodic index: any integer onto [0, n), as repeated application of
+// check_boundary's wrap (utility.cpp:47,51) would place it.
+static __device__ __forceinline__ int wrapi(int v, int n)
+{
+    int r = v % n;
+    return r < 0 ? r + n : r;
+}
+
+// Model constants narrowed to the state type; padded axes X, Y, Z take the
+// last `dim` real-axis weights.
+template <typename T>
+static inline P<T> narrow(const Coeffs& c, int dim)
+{
+    P<T> p;
+    double w[3] = {1.0, 1.0, 1.0};
+    for (int a = 0; a < dim; a++) w[3 - dim + a] = c.w[a];
+    p.wx = (T)w[0];
+    p.wy = (T)w[1];
+    p.wz = (T)w[2];
+    p.kappa = (T)c.kappa;
+    p.dtm = (T)c.dtm;
+    p.gamma2 = (T)c.gamma2;
+    p.neg_r = (T)c.neg_r;
+    p.u = (T)c.u;
+    return p;
+}
+
+}  // namespace pf

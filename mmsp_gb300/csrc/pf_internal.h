@@ -1,0 +1,72 @@
+// pf_internal.h -- interfaces between the translation units of libmmsp_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "MMSP.gpu.h"
+
+namespace pf {
+
+// Grid geometry as the kernels see it: three padded axes X (slowest), Y, Z
+// (fastest).  A grid of dim d occupies the last d axes; the leading ones
+// have extent 1.  Periodic wrap is applied to every index.
+struct Geom {
+    int X, Y, Z;       // padded extents
+    int dim;           // 1..3: number of real axes
+    long long YZ;      // Y*Z
+    long long cells;   // X*Y*Z
+};
+
+// Model constants in double; the launchers narrow them to the state type.
+struct Coeffs {
+    double w[3];       // 1/(dx*dx) per real axis, MMSP axis order (grid.cpp:2062)
+    double wg[3];      // 1/(2 dx) per real axis (grid.cpp:2163)
+    double kappa;      // gradient coefficient
+    double dtm;        // dt*M (CH, AC_POLY), dt*L (AC), dt (GG)
+    double gamma2;     // 2*gamma (AC)
+    double neg_r, u;   // -r, u (polynomial models)
+    double gamma;      // gamma (energy)
+    double dV;         // cell volume
+    bool unit_w;       // every w == 1.0 exactly
+};
+
+Geom make_geom(const mmsp_gpu_desc& d);
+int sm_count();                 // SMs of the current device
+Coeffs make_coeffs(const mmsp_gpu_desc& d);
+
+// A prepared launch of one explicit step.
+struct StepPlan {
+    const void* fn;    // kernel
+    dim3 grid, block;
+    size_t smem;
+    int planes;        // planes of axis X per block (3D streaming)
+    int fields;
+    bool ok;
+};
+
+// Plans; returns cudaSuccess or the error of cudaFuncSetAttribute.
+cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
+cudaError_t plan_ac(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
+
+// One step in -> out on `s`.
+cudaError_t launch_ch(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
+                      const void* in, void* out, cudaStream_t s);
+cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
+                      const void* in, void* out, cudaStream_t s);
+
+// Reductions: partial sums of (mass, energy) per block into `partials`
+// (4 doubles per block: mass sum, mass compensation, energy sum, energy
+// compensation), then a single-block pass into result[0..1] (mass, energy).
+// The block count is fixed (kReduceBlocks), so results do not depend on timing.
+constexpr int kReduceBlocks = 304;
+constexpr size_t kPartialsBytes = sizeof(double) * 4 * (kReduceBlocks + 1);
+cudaError_t launch_reduce(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
+                          const void* state, double* partials, cudaStream_t s);
+
+// Cell-major <-> field-major for vector grids.
+cudaError_t launch_transpose(int dtype, const void* in, void* out, long long cells, int fields,
+                             bool to_field_major, cudaStream_t s);
+
+}  // namespace pf

@@ -1,0 +1,87 @@
+"""Seeded synthetic initial conditions.
+
+The reference seeds ``rand()`` with the wall clock (include/MMSP.main.hpp:55),
+so its examples are not reproducible.  These generators replace it with a
+counter-based SplitMix64 stream (Steele, Lea and Flood, "Fast splittable
+pseudorandom number generators", OOPSLA 2014): value ``i`` of stream ``seed``
+depends only on ``(seed, i)``, so every run, machine and thread count sees
+the same bytes.  Doubles take the top 53 bits: ``u = (z >> 11) * 2**-53``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, n: int, start: int = 0) -> np.ndarray:
+    """Values ``start .. start+n-1`` of the SplitMix64 stream for ``seed``."""
+    with np.errstate(over="ignore"):
+        idx = np.arange(start + 1, start + n + 1, dtype=np.uint64)
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + idx * _GAMMA
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform(seed: int, n: int, start: int = 0) -> np.ndarray:
+    """Doubles in [0, 1)."""
+    z = splitmix64(seed, n, start)
+    return (z >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+
+
+def noisy_composition(shape, mean: float, amplitude: float, seed: int) -> np.ndarray:
+    """``c = mean + amplitude * U(-1, 1)`` i.i.d. per cell, node order."""
+    n = int(np.prod(shape))
+    u = uniform(seed, n)
+    return (mean + amplitude * (2.0 * u - 1.0)).reshape(shape)
+
+
+def voronoi_grains(shape, points: int, fields: int, seed: int) -> np.ndarray:
+    """Order parameters of a periodic Voronoi tessellation.
+
+    ``points`` seeds are drawn uniformly in the box (one stream value per
+    coordinate).  Each cell belongs to the seed nearest by the periodic
+    minimum-image distance (lowest seed index on a tie); ``eta_k = 1`` for
+    ``k = grain % fields`` and 0 otherwise.  Returns shape ``shape + (fields,)``.
+    """
+    shape = tuple(int(s) for s in shape)
+    dim = len(shape)
+    u = uniform(seed, points * dim).reshape(points, dim)
+    pts = u * np.asarray(shape, dtype=np.float64)
+    ncell = int(np.prod(shape))
+    grain = np.empty(ncell, dtype=np.int64)
+    grids = np.indices(shape).reshape(dim, -1).T.astype(np.float64)
+    L = np.asarray(shape, dtype=np.float64)
+    chunk = max(1, (1 << 22) // max(points, 1))
+    for s in range(0, ncell, chunk):
+        x = grids[s:s + chunk]
+        d2 = np.zeros((x.shape[0], points))
+        for a in range(dim):
+            d = np.abs(x[:, a:a + 1] - pts[None, :, a])
+            d = np.minimum(d, L[a] - d)
+            d2 += d * d
+        grain[s:s + chunk] = np.argmin(d2, axis=1)
+    eta = np.zeros((ncell, fields), dtype=np.float64)
+    eta[np.arange(ncell), grain % fields] = 1.0
+    return eta.reshape(shape + (fields,))
+
+
+def graingrowth_circles(shape, fields: int = 2) -> np.ndarray:
+    """The shipped grain-growth start state (graingrowth.cpp:34-51 in 2D/3D,
+    :18-30 in 1D): field 1 inside circles of radius 16 on a period-64
+    lattice of the first two axes, field 0 elsewhere."""
+    shape = tuple(int(s) for s in shape)
+    x = np.indices(shape)
+    if len(shape) == 1:
+        inside = (32 - x[0] % 64) < 16.0
+    else:
+        r = np.sqrt((32 - x[0] % 64) ** 2.0 + (32 - x[1] % 64) ** 2.0)
+        inside = r < 16.0
+    eta = np.zeros(shape + (fields,), dtype=np.float64)
+    eta[..., 0] = np.where(inside, 0.0, 1.0)
+    eta[..., 1] = np.where(inside, 1.0, 0.0)
+    return eta

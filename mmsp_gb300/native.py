@@ -1,0 +1,226 @@
+"""ctypes binding of libmmsp_gpu.so (the C ABI declared in include/MMSP.gpu.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, the calls raise.  The binding mirrors the header one to one; the
+Pythonic helpers (``Stepper``, ``update``) only marshal numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED, ESTOPPED = \
+    0, -1, -2, -3, -4, -5, -6, -7, -8, -9
+BC_MIRROR, BC_NEUMANN, BC_PERIODIC, BC_PARALLEL, BC_DIRICHLET = 0, 1, 2, 3, 4
+F64, F32 = 0, 1
+CH, CH_POLY, AC, GG, AC_POLY = 0, 1, 2, 3, 4
+CELL_MAJOR, FIELD_MAJOR = 0, 1
+
+MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY}
+DTYPES = {np.dtype(np.float64): F64, np.dtype(np.float32): F32}
+
+# Every symbol include/MMSP.gpu.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "mmsp_gpu_version", "mmsp_gpu_strerror", "mmsp_gpu_desc_init", "mmsp_gpu_validate",
+    "mmsp_gpu_footprint", "mmsp_gpu_create", "mmsp_gpu_destroy", "mmsp_gpu_set_stream",
+    "mmsp_gpu_upload", "mmsp_gpu_download", "mmsp_gpu_upload_device", "mmsp_gpu_download_device",
+    "mmsp_gpu_step", "mmsp_gpu_synchronize", "mmsp_gpu_reduce", "mmsp_gpu_state",
+    "mmsp_gpu_last_error", "mmsp_gpu_update",
+]
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("n", ctypes.c_int * 3), ("fields", ctypes.c_int),
+                ("dtype", ctypes.c_int), ("model", ctypes.c_int), ("bc", (ctypes.c_int * 2) * 3),
+                ("dx", ctypes.c_double * 3), ("dt", ctypes.c_double), ("kappa", ctypes.c_double),
+                ("mobility", ctypes.c_double), ("gamma", ctypes.c_double), ("r", ctypes.c_double),
+                ("u", ctypes.c_double)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("mass", ctypes.c_double), ("energy", ctypes.c_double), ("gpu_ms", ctypes.c_double),
+                ("steps", ctypes.c_int64)]
+
+
+class GpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%d)%s" % (strerror(code), code, (": " + msg) if msg else ""))
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libmmsp_gpu.so; raises if it is absent (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError("libmmsp_gpu.so is not built (%s); run __graft_entry__.build()" % path)
+        _build.build()
+    L = ctypes.CDLL(path)
+    vp, sz, i = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+    dp = ctypes.POINTER(Desc)
+    sig = {
+        "mmsp_gpu_version": (i, []),
+        "mmsp_gpu_strerror": (ctypes.c_char_p, [i]),
+        "mmsp_gpu_desc_init": (i, [dp, i, ctypes.POINTER(ctypes.c_int), i, i, i]),
+        "mmsp_gpu_validate": (i, [dp]),
+        "mmsp_gpu_footprint": (i, [dp, ctypes.POINTER(ctypes.c_size_t)]),
+        "mmsp_gpu_create": (i, [ctypes.POINTER(vp), dp]),
+        "mmsp_gpu_destroy": (i, [vp]),
+        "mmsp_gpu_set_stream": (i, [vp, vp]),
+        "mmsp_gpu_upload": (i, [vp, vp, sz, i]),
+        "mmsp_gpu_download": (i, [vp, vp, sz, i]),
+        "mmsp_gpu_upload_device": (i, [vp, vp, sz, i]),
+        "mmsp_gpu_download_device": (i, [vp, vp, sz, i]),
+        "mmsp_gpu_step": (i, [vp, i]),
+        "mmsp_gpu_synchronize": (i, [vp]),
+        "mmsp_gpu_reduce": (i, [vp, ctypes.POINTER(Stats)]),
+        "mmsp_gpu_state": (i, [vp, ctypes.POINTER(vp)]),
+        "mmsp_gpu_last_error": (ctypes.c_char_p, [vp]),
+        "mmsp_gpu_update": (i, [dp, vp, sz, i, i, ctypes.POINTER(Stats)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def strerror(code: int) -> str:
+    try:
+        return load().mmsp_gpu_strerror(code).decode()
+    except Exception:
+        return "status"
+
+
+def make_desc(shape, fields=1, dtype=np.float64, model="ch", dx=None, bc=None, dt=None, kappa=None,
+              mobility=None, gamma=None, r=None, u=None) -> Desc:
+    """A descriptor with the model's defaults (mmsp_gpu_desc_init), then overrides."""
+    L = load()
+    shape = tuple(int(s) for s in shape)
+    d = Desc()
+    n = (ctypes.c_int * 3)(*(list(shape) + [1] * (3 - len(shape))))
+    m = MODELS[model] if isinstance(model, str) else int(model)
+    # defaults only: mmsp_gpu_create validates the final descriptor
+    L.mmsp_gpu_desc_init(ctypes.byref(d), len(shape), n, int(fields), DTYPES[np.dtype(dtype)], m)
+    if dx is not None:
+        for a, v in enumerate(dx):
+            d.dx[a] = float(v)
+    if bc is not None:
+        for a, (lo, hi) in enumerate(bc):
+            d.bc[a][0] = int(lo)
+            d.bc[a][1] = int(hi)
+    for name, v in (("dt", dt), ("kappa", kappa), ("mobility", mobility), ("gamma", gamma), ("r", r), ("u", u)):
+        if v is not None:
+            setattr(d, name, float(v))
+    return d
+
+
+def _check(rc: int, h=None, what: str = ""):
+    if rc != OK:
+        msg = ""
+        if h is not None:
+            try:
+                msg = load().mmsp_gpu_last_error(h).decode()
+            except Exception:
+                msg = ""
+        raise GpuError(rc, (what + ": " + msg) if what else msg)
+
+
+class Stepper:
+    """A device-resident grid (one mmsp_gpu_handle)."""
+
+    def __init__(self, desc: Desc):
+        self.L = load()
+        self.desc = desc
+        h = ctypes.c_void_p()
+        _check(self.L.mmsp_gpu_create(ctypes.byref(h), ctypes.byref(desc)), None, "create")
+        self.h = h
+        self.dtype = np.float64 if desc.dtype == F64 else np.float32
+        self.shape = tuple(desc.n[a] for a in range(desc.dim))
+        self.fields = desc.fields
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mmsp_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _host_shape(self, layout):
+        if self.fields == 1:
+            return self.shape
+        return self.shape + (self.fields,) if layout == CELL_MAJOR else (self.fields,) + self.shape
+
+    def upload(self, arr: np.ndarray, layout: int = CELL_MAJOR):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        if a.shape != self._host_shape(layout):
+            raise ValueError("shape %s, expected %s" % (a.shape, self._host_shape(layout)))
+        _check(self.L.mmsp_gpu_upload(self.h, a.ctypes.data, a.nbytes, layout), self.h, "upload")
+
+    def download(self, layout: int = CELL_MAJOR, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self._host_shape(layout), dtype=self.dtype)
+        _check(self.L.mmsp_gpu_download(self.h, out.ctypes.data, out.nbytes, layout), self.h, "download")
+        return out
+
+    def step(self, steps: int):
+        _check(self.L.mmsp_gpu_step(self.h, int(steps)), self.h, "step")
+
+    def synchronize(self):
+        _check(self.L.mmsp_gpu_synchronize(self.h), self.h, "synchronize")
+
+    def reduce(self) -> Stats:
+        st = Stats()
+        _check(self.L.mmsp_gpu_reduce(self.h, ctypes.byref(st)), self.h, "reduce")
+        return st
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(self.L.mmsp_gpu_set_stream(self.h, ctypes.c_void_p(stream_ptr or 0)), self.h, "set_stream")
+
+    def state_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        _check(self.L.mmsp_gpu_state(self.h, ctypes.byref(p)), self.h, "state")
+        return p.value
+
+    def upload_device(self, ptr: int, nbytes: int, layout: int = FIELD_MAJOR):
+        _check(self.L.mmsp_gpu_upload_device(self.h, ctypes.c_void_p(ptr), nbytes, layout), self.h, "upload_device")
+
+    def download_device(self, ptr: int, nbytes: int, layout: int = FIELD_MAJOR):
+        _check(self.L.mmsp_gpu_download_device(self.h, ctypes.c_void_p(ptr), nbytes, layout), self.h,
+               "download_device")
+
+
+def update(arr: np.ndarray, steps: int, desc: Desc, layout: int = CELL_MAJOR):
+    """mmsp_gpu_update: one call per update(grid&, steps); returns (result, Stats)."""
+    L = load()
+    dt = np.float64 if desc.dtype == F64 else np.float32
+    a = np.array(arr, dtype=dt, order="C", copy=True)
+    st = Stats()
+    rc = L.mmsp_gpu_update(ctypes.byref(desc), a.ctypes.data, a.nbytes, layout, int(steps), ctypes.byref(st))
+    _check(rc, None, "update")
+    return a, st

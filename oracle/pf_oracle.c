@@ -1,0 +1,379 @@
+/* pf_oracle.c -- CPU oracle for the explicit phase-field step (TEST INFRASTRUCTURE).
+ *
+ * See pf_oracle.h for what each function restates and where in the
+ * reference it comes from.  Build with -ffp-contract=off (oracle/Makefile).
+ */
+#include "pf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* check_boundary (include/MMSP.utility.cpp:42-57, serial build) for a local
+ * domain [0, n).  Returns the mapped coordinate. */
+static int map_coord(int x, int n, int b0, int b1)
+{
+    if (x < 0) {
+        if (b0 == PFO_NEUMANN || b0 == PFO_DIRICHLET) x = 0;
+        else if (b0 == PFO_PERIODIC) x = n - (0 - x);
+        else if (b0 == PFO_MIRROR) x = 2 * 0 - x;
+    } else if (x >= n) {
+        if (b1 == PFO_NEUMANN || b1 == PFO_DIRICHLET) x = n - 1;
+        else if (b1 == PFO_PERIODIC) x = 0 + (x - n);
+        else if (b1 == PFO_MIRROR) x = 2 * (n - 1) - x;
+    }
+    return x;
+}
+
+/* The grid seen as three padded axes; the real axes are the last `dim`. */
+typedef struct {
+    int dim;
+    int n[3];          /* padded extents (leading 1s) */
+    long st[3];        /* strides, last axis fastest */
+    double w[3];       /* 1/(dx*dx) of each real axis, in real-axis order */
+    double wg[3];      /* 1/(2*dx), for gradient() */
+    int* lo[3];        /* mapped x-1 per padded axis */
+    int* hi[3];        /* mapped x+1 per padded axis */
+    long cells;
+} geo;
+
+static void geo_free(geo* q)
+{
+    for (int a = 0; a < 3; a++) {
+        free(q->lo[a]);
+        free(q->hi[a]);
+        q->lo[a] = q->hi[a] = NULL;
+    }
+}
+
+static int geo_init(geo* q, const pfo_grid* g)
+{
+    memset(q, 0, sizeof(*q));
+    if (!g || g->dim < 1 || g->dim > 3) return -1;
+    q->dim = g->dim;
+    int off = 3 - g->dim;
+    for (int a = 0; a < 3; a++) q->n[a] = 1;
+    for (int a = 0; a < g->dim; a++) {
+        if (g->n[a] < 1) return -1;
+        q->n[off + a] = g->n[a];
+        /* grid.cpp:2062 (scalar and vector overloads use dx*dx) */
+        q->w[a] = 1.0 / (g->dx[a] * g->dx[a]);
+        q->wg[a] = 1.0 / (2.0 * g->dx[a]);
+    }
+    q->st[2] = 1;
+    q->st[1] = q->n[2];
+    q->st[0] = (long)q->n[1] * q->n[2];
+    q->cells = (long)q->n[0] * q->st[0];
+    for (int a = 0; a < 3; a++) {
+        int n = q->n[a];
+        q->lo[a] = (int*)malloc(sizeof(int) * (size_t)n);
+        q->hi[a] = (int*)malloc(sizeof(int) * (size_t)n);
+        if (!q->lo[a] || !q->hi[a]) { geo_free(q); return -1; }
+        int ra = a - off; /* real axis index, <0 for padding */
+        for (int x = 0; x < n; x++) {
+            if (ra < 0) { q->lo[a][x] = q->hi[a][x] = x; continue; }
+            int l = map_coord(x - 1, n, g->bc[ra][0], g->bc[ra][1]);
+            int h = map_coord(x + 1, n, g->bc[ra][0], g->bc[ra][1]);
+            /* a mapping that leaves the domain (mirror on n=1, "parallel"
+             * in a serial grid) is undefined in the reference: refuse it. */
+            if (l < 0 || l >= n || h < 0 || h >= n) { geo_free(q); return -1; }
+            q->lo[a][x] = l;
+            q->hi[a][x] = h;
+        }
+    }
+    return 0;
+}
+
+long pfo_nodes(const pfo_grid* g)
+{
+    long c = 1;
+    for (int a = 0; a < g->dim; a++) c *= g->n[a];
+    return c;
+}
+
+/* Offsets of the low/high neighbour of cell (i0,i1,i2) along padded axis a. */
+#define NB_LO(q, a, x) (((long)(q)->lo[a][x] - (x)) * (q)->st[a])
+#define NB_HI(q, a, x) (((long)(q)->hi[a][x] - (x)) * (q)->st[a])
+
+/* MMSP::laplacian, scalar (grid.cpp:2049-2066): lap starts at 0.0 and adds
+ * weight*(yh - 2.0*y + yl) for axes 0..dim-1.  Field j of a cell-major
+ * vector grid with N values per cell when N > 1 (grid.cpp:2068-2088). */
+static inline double lap_at(const geo* q, const double* f, long idx, int N, int j,
+                            const int xc[3])
+{
+    double lap = 0.0;
+    const double y = f[idx * N + j];
+    int off = 3 - q->dim;
+    for (int ra = 0; ra < q->dim; ra++) {
+        int a = off + ra;
+        const double yh = f[(idx + NB_HI(q, a, xc[a])) * N + j];
+        const double yl = f[(idx + NB_LO(q, a, xc[a])) * N + j];
+        double weight = q->w[ra];
+        lap += weight * (yh - 2.0 * y + yl);
+    }
+    return lap;
+}
+
+static int nthreads(int t)
+{
+#ifdef _OPENMP
+    if (t <= 0) t = omp_get_max_threads();
+    return t;
+#else
+    (void)t;
+    return 1;
+#endif
+}
+
+int pfo_laplacian(const pfo_grid* g, const double* in, double* out)
+{
+    geo q;
+    if (geo_init(&q, g) || !in || !out) return -1;
+    for (int i0 = 0; i0 < q.n[0]; i0++)
+        for (int i1 = 0; i1 < q.n[1]; i1++)
+            for (int i2 = 0; i2 < q.n[2]; i2++) {
+                int xc[3] = {i0, i1, i2};
+                long idx = i0 * q.st[0] + i1 * q.st[1] + i2;
+                out[idx] = lap_at(&q, in, idx, 1, 0, xc);
+            }
+    geo_free(&q);
+    return 0;
+}
+
+/* Two-pass explicit Cahn-Hilliard in the structure of cahn-hilliard.cpp:65-80.
+ * form 0: BASELINE free energy, form 1: the shipped polynomial. */
+static int ch_run(const pfo_grid* g, double* c, int steps, int form,
+                  double r, double u, double K, double M, double dt, int threads)
+{
+    geo q;
+    if (geo_init(&q, g) || !c || steps < 0) return -1;
+    double* temp = (double*)malloc(sizeof(double) * (size_t)q.cells);
+    double* nw = (double*)malloc(sizeof(double) * (size_t)q.cells);
+    if (!temp || !nw) { free(temp); free(nw); geo_free(&q); return -1; }
+    double* old = c;
+    int nt = nthreads(threads);
+    (void)nt;
+    for (int step = 0; step < steps; step++) {
+        #pragma omp parallel for schedule(static) num_threads(nt)
+        for (int i0 = 0; i0 < q.n[0]; i0++)
+            for (int i1 = 0; i1 < q.n[1]; i1++)
+                for (int i2 = 0; i2 < q.n[2]; i2++) {
+                    int xc[3] = {i0, i1, i2};
+                    long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                    double phi = old[i];
+                    if (form == 0)
+                        temp[i] = 2.0 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) - K * lap_at(&q, old, i, 1, 0, xc);
+                    else
+                        temp[i] = -r * phi + u * pow(phi, 3) - K * lap_at(&q, old, i, 1, 0, xc);
+                }
+        #pragma omp parallel for schedule(static) num_threads(nt)
+        for (int i0 = 0; i0 < q.n[0]; i0++)
+            for (int i1 = 0; i1 < q.n[1]; i1++)
+                for (int i2 = 0; i2 < q.n[2]; i2++) {
+                    int xc[3] = {i0, i1, i2};
+                    long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                    nw[i] = old[i] + dt * M * lap_at(&q, temp, i, 1, 0, xc);
+                }
+        /* swap(oldGrid,newGrid), cahn-hilliard.cpp:78 */
+        double* t = old;
+        old = nw;
+        nw = t;
+    }
+    if (old != c) {
+        memcpy(c, old, sizeof(double) * (size_t)q.cells);
+        nw = old;
+    }
+    free(temp);
+    free(nw);
+    geo_free(&q);
+    return 0;
+}
+
+int pfo_ch_baseline(const pfo_grid* g, double* c, int steps,
+                    double kappa, double M, double dt, int threads)
+{
+    return ch_run(g, c, steps, 0, 0.0, 0.0, kappa, M, dt, threads);
+}
+
+int pfo_ch_shipped(const pfo_grid* g, double* c, int steps,
+                   double r, double u, double K, double M, double dt, int threads)
+{
+    return ch_run(g, c, steps, 1, r, u, K, M, dt, threads);
+}
+
+/* Single-pass multi-field Allen-Cahn in the structure of graingrowth.cpp:86-110.
+ * form 0: BASELINE free energy with gamma; form 1: graingrowth.cpp:105 as
+ * shipped; form 2: allen-cahn.cpp:70 as shipped (N must be 1). */
+static int ac_run(const pfo_grid* g, int N, double* eta, int steps, int form,
+                  double gamma, double kappa, double L, double r, double u,
+                  double dt, int threads)
+{
+    geo q;
+    if (N < 1 || N > 64 || geo_init(&q, g) || !eta || steps < 0) return -1;
+    if (form == 2 && N != 1) { geo_free(&q); return -1; }
+    double* nw = (double*)malloc(sizeof(double) * (size_t)q.cells * (size_t)N);
+    if (!nw) { geo_free(&q); return -1; }
+    double* old = eta;
+    int nt = nthreads(threads);
+    (void)nt;
+    for (int step = 0; step < steps; step++) {
+        #pragma omp parallel for schedule(static) num_threads(nt)
+        for (int i0 = 0; i0 < q.n[0]; i0++)
+            for (int i1 = 0; i1 < q.n[1]; i1++)
+                for (int i2 = 0; i2 < q.n[2]; i2++) {
+                    int xc[3] = {i0, i1, i2};
+                    long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                    const double* phi = old + i * N;
+                    double* out = nw + i * N;
+                    double lap[64];
+                    for (int j = 0; j < N; j++) lap[j] = lap_at(&q, old, i, N, j, xc);
+                    if (form == 2) {
+                        double p = phi[0];
+                        out[0] = p - dt * L * (-r * p + u * pow(p, 3) - kappa * lap[0]);
+                        continue;
+                    }
+                    /* sum of squares, graingrowth.cpp:97-101 */
+                    double sum = 0.0;
+                    for (int j = 0; j < N; j++) sum += phi[j] * phi[j];
+                    if (form == 0) {
+                        for (int j = 0; j < N; j++)
+                            out[j] = phi[j] - dt * L * (-phi[j] + phi[j] * phi[j] * phi[j]
+                                     + 2.0 * gamma * phi[j] * (sum - phi[j] * phi[j])
+                                     - kappa * lap[j]);
+                    } else {
+                        for (int j = 0; j < N; j++)
+                            out[j] = phi[j] - dt * (-phi[j] - pow(phi[j], 3) + 2.0 * (phi[j] * sum - lap[j]));
+                    }
+                }
+        double* t = old;
+        old = nw;
+        nw = t;
+    }
+    if (old != eta) {
+        memcpy(eta, old, sizeof(double) * (size_t)q.cells * (size_t)N);
+        nw = old;
+    }
+    free(nw);
+    geo_free(&q);
+    return 0;
+}
+
+int pfo_ac_baseline(const pfo_grid* g, int N, double* eta, int steps,
+                    double gamma, double kappa, double L, double dt, int threads)
+{
+    return ac_run(g, N, eta, steps, 0, gamma, kappa, L, 0.0, 0.0, dt, threads);
+}
+
+int pfo_ac_graingrowth(const pfo_grid* g, int N, double* eta, int steps,
+                       double dt, int threads)
+{
+    return ac_run(g, N, eta, steps, 1, 0.0, 0.0, 1.0, 0.0, 0.0, dt, threads);
+}
+
+int pfo_ac_scalar_shipped(const pfo_grid* g, double* phi, int steps,
+                          double r, double u, double K, double M, double dt,
+                          int threads)
+{
+    return ac_run(g, 1, phi, steps, 2, 0.0, K, M, r, u, dt, threads);
+}
+
+/* Neumaier's improvement of Kahan summation. */
+typedef struct { double s, c; } nsum;
+static inline void nadd(nsum* a, double x)
+{
+    double t = a->s + x;
+    if (fabs(a->s) >= fabs(x)) a->c += (a->s - t) + x;
+    else a->c += (x - t) + a->s;
+    a->s = t;
+}
+static inline double nval(const nsum* a) { return a->s + a->c; }
+
+/* |grad f_j|^2 at a cell with gradient() of grid.cpp:2154-2170:
+ * g_i = (1/(2 dx_i)) * (yh - yl), summed as g_i*g_i over axes. */
+static inline double gradsq_at(const geo* q, const double* f, long idx, int N, int j,
+                               const int xc[3])
+{
+    double s = 0.0;
+    int off = 3 - q->dim;
+    for (int ra = 0; ra < q->dim; ra++) {
+        int a = off + ra;
+        const double yh = f[(idx + NB_HI(q, a, xc[a])) * N + j];
+        const double yl = f[(idx + NB_LO(q, a, xc[a])) * N + j];
+        double gi = q->wg[ra] * (yh - yl);
+        s += gi * gi;
+    }
+    return s;
+}
+
+static double cell_volume(const pfo_grid* g)
+{
+    double dV = 1.0;
+    for (int a = 0; a < g->dim; a++) dV *= g->dx[a];
+    return dV;
+}
+
+int pfo_ch_mass_energy(const pfo_grid* g, const double* c, double kappa,
+                       double* mass, double* energy)
+{
+    geo q;
+    if (geo_init(&q, g) || !c) return -1;
+    nsum m = {0, 0}, e = {0, 0};
+    for (int i0 = 0; i0 < q.n[0]; i0++)
+        for (int i1 = 0; i1 < q.n[1]; i1++)
+            for (int i2 = 0; i2 < q.n[2]; i2++) {
+                int xc[3] = {i0, i1, i2};
+                long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                double C = c[i];
+                double omc = 1.0 - C;
+                double f = C * C * omc * omc;
+                nadd(&e, f + 0.5 * kappa * gradsq_at(&q, c, i, 1, 0, xc));
+                nadd(&m, C);
+            }
+    double dV = cell_volume(g);
+    if (mass) *mass = dV * nval(&m);
+    if (energy) *energy = dV * nval(&e);
+    geo_free(&q);
+    return 0;
+}
+
+int pfo_ac_mass_energy(const pfo_grid* g, int N, const double* eta,
+                       double gamma, double kappa, double* mass, double* energy)
+{
+    geo q;
+    if (N < 1 || N > 64 || geo_init(&q, g) || !eta) return -1;
+    nsum e = {0, 0};
+    nsum m[64];
+    for (int j = 0; j < N; j++) m[j].s = m[j].c = 0.0;
+    for (int i0 = 0; i0 < q.n[0]; i0++)
+        for (int i1 = 0; i1 < q.n[1]; i1++)
+            for (int i2 = 0; i2 < q.n[2]; i2++) {
+                int xc[3] = {i0, i1, i2};
+                long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                const double* p = eta + i * N;
+                double bulk = 0.0, pair = 0.0, grad = 0.0, sq = 0.0;
+                for (int j = 0; j < N; j++) {
+                    double p2 = p[j] * p[j];
+                    bulk += -0.5 * p2 + 0.25 * p2 * p2;
+                    pair += p2 * sq;          /* sum_{k<j} e_k^2 e_j^2 */
+                    sq += p2;
+                    grad += gradsq_at(&q, eta, i, N, j, xc);
+                    nadd(&m[j], p[j]);
+                }
+                nadd(&e, bulk + gamma * pair + 0.5 * kappa * grad);
+            }
+    double dV = cell_volume(g);
+    if (mass)
+        for (int j = 0; j < N; j++) mass[j] = dV * nval(&m[j]);
+    if (energy) *energy = dV * nval(&e);
+    geo_free(&q);
+    return 0;
+}
+
+void pfo_pow3(const double* x, double* y, long n)
+{
+    for (long i = 0; i < n; i++) y[i] = pow(x[i], 3);
+}

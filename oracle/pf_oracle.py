@@ -1,0 +1,159 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline legs
+import this module; the product never does.  It loads
+``oracle/_build/libpf_oracle.so`` (built by ``make -C oracle``) and exposes
+numpy-level wrappers of the functions declared in ``pf_oracle.h``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpf_oracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "ref_update")
+
+PERIODIC = 2
+
+
+class _Grid(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("n", ctypes.c_int * 3),
+                ("dx", ctypes.c_double * 3), ("bc", (ctypes.c_int * 2) * 3)]
+
+
+_lib = None
+
+
+def build() -> None:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        gp = ctypes.POINTER(_Grid)
+        for name, args in [
+            ("pfo_ch_baseline", [gp, dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]),
+            ("pfo_ch_shipped", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int]),
+            ("pfo_ac_baseline", [gp, ctypes.c_int, dp, ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int]),
+            ("pfo_ac_graingrowth", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+            ("pfo_ac_scalar_shipped", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int]),
+            ("pfo_laplacian", [gp, dp, dp]),
+            ("pfo_ch_mass_energy", [gp, dp, ctypes.c_double, dp, dp]),
+            ("pfo_ac_mass_energy", [gp, ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, dp, dp]),
+        ]:
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = ctypes.c_int
+        L.pfo_pow3.argtypes = [dp, dp, ctypes.c_long]
+        L.pfo_pow3.restype = None
+        _lib = L
+    return _lib
+
+
+def _grid(shape, dx=None, bc=None) -> _Grid:
+    g = _Grid()
+    g.dim = len(shape)
+    for a, s in enumerate(shape):
+        g.n[a] = int(s)
+        g.dx[a] = 1.0 if dx is None else float(dx[a])
+        lo, hi = (PERIODIC, PERIODIC) if bc is None else bc[a]
+        g.bc[a][0] = lo
+        g.bc[a][1] = hi
+    return g
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _check(rc, name):
+    if rc != 0:
+        raise ValueError("%s: oracle refused the arguments (%d)" % (name, rc))
+
+
+def ch_baseline(c, steps, kappa=1.0, M=1.0, dt=0.005, dx=None, bc=None, threads=0):
+    out = np.array(c, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape, dx, bc)
+    _check(lib().pfo_ch_baseline(ctypes.byref(g), _ptr(out), int(steps), kappa, M, dt, threads), "ch_baseline")
+    return out
+
+
+def ch_shipped(c, steps, r=1.0, u=1.0, K=1.0, M=1.0, dt=0.01, dx=None, bc=None, threads=0):
+    out = np.array(c, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape, dx, bc)
+    _check(lib().pfo_ch_shipped(ctypes.byref(g), _ptr(out), int(steps), r, u, K, M, dt, threads), "ch_shipped")
+    return out
+
+
+def ac_baseline(eta, steps, gamma=1.5, kappa=2.0, L=1.0, dt=0.05, dx=None, bc=None, threads=0):
+    """``eta`` has shape grid_shape + (N,) (cell-major)."""
+    out = np.array(eta, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape[:-1], dx, bc)
+    _check(lib().pfo_ac_baseline(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps),
+                                 gamma, kappa, L, dt, threads), "ac_baseline")
+    return out
+
+
+def ac_graingrowth(eta, steps, dt=0.01, dx=None, bc=None, threads=0):
+    out = np.array(eta, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape[:-1], dx, bc)
+    _check(lib().pfo_ac_graingrowth(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps), dt, threads),
+           "ac_graingrowth")
+    return out
+
+
+def ac_scalar_shipped(phi, steps, r=1.0, u=1.0, K=1.0, M=1.0, dt=0.01, dx=None, bc=None, threads=0):
+    out = np.array(phi, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape, dx, bc)
+    _check(lib().pfo_ac_scalar_shipped(ctypes.byref(g), _ptr(out), int(steps), r, u, K, M, dt, threads),
+           "ac_scalar_shipped")
+    return out
+
+
+def laplacian(f, dx=None, bc=None):
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    out = np.empty_like(f)
+    g = _grid(f.shape, dx, bc)
+    _check(lib().pfo_laplacian(ctypes.byref(g), _ptr(f), _ptr(out)), "laplacian")
+    return out
+
+
+def ch_mass_energy(c, kappa=1.0, dx=None, bc=None):
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    g = _grid(c.shape, dx, bc)
+    m = ctypes.c_double()
+    e = ctypes.c_double()
+    _check(lib().pfo_ch_mass_energy(ctypes.byref(g), _ptr(c), kappa, ctypes.byref(m), ctypes.byref(e)),
+           "ch_mass_energy")
+    return m.value, e.value
+
+
+def ac_mass_energy(eta, gamma=1.5, kappa=2.0, dx=None, bc=None):
+    eta = np.ascontiguousarray(eta, dtype=np.float64)
+    N = eta.shape[-1]
+    g = _grid(eta.shape[:-1], dx, bc)
+    m = np.zeros(N)
+    e = ctypes.c_double()
+    _check(lib().pfo_ac_mass_energy(ctypes.byref(g), N, _ptr(eta), gamma, kappa, _ptr(m), ctypes.byref(e)),
+           "ac_mass_energy")
+    return m, e.value
+
+
+def pow3(x):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    lib().pfo_pow3(_ptr(x), _ptr(y), x.size)
+    return y
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_BIN)

@@ -1,0 +1,178 @@
+// ref_update.cpp -- the reference's own explicit update() loops, driven from
+// the command line (TEST INFRASTRUCTURE: builds golden vectors and pins the C
+// oracle in pf_oracle.c; never part of the product).
+//
+// Compiled by oracle/Makefile against the reference's headers (MMSP.hpp:
+// grid, laplacian, swap, ghostswap, input/output), without copying them.
+// The bodies below keep the loop structure of
+//   examples/phase_transitions/cahn-hilliard/explicit/cahn-hilliard.cpp:47-81
+//   examples/coarsening/grain_growth/isotropic/phase_field/graingrowth.cpp:73-111
+//   examples/phase_transitions/allen-cahn/allen-cahn.cpp:47-75
+// The "shipped" models are those loops with the examples' own expressions;
+// the "baseline" models substitute f(c)=c^2(1-c)^2 for Cahn-Hilliard and
+// f = sum(-e^2/2+e^4/4) + gamma*sum_{i<j} e_i^2 e_j^2 for grain growth, with
+// the parameters taken from the command line instead of being hard-coded.
+//
+// usage: ref_update MODEL IN.dat OUT.dat STEPS [params...]
+//   ch_baseline      K M dt
+//   ch_shipped       r u K M dt
+//   ac_baseline      gamma kappa L dt
+//   graingrowth      dt
+//   ac_scalar        r u K M dt
+// Prints "update_seconds <t>" (std::chrono around update() only).
+#include "MMSP.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+namespace MMSP {
+
+template <int dim> void ch_update(grid<dim, double>& oldGrid, int steps, bool shipped,
+                                  const std::vector<double>& p)
+{
+	ghostswap(oldGrid);
+	grid<dim, double> newGrid(oldGrid);
+	grid<dim, double> temp(oldGrid);
+	double r = 0, u = 0, K, M, dt;
+	if (shipped) { r = p[0]; u = p[1]; K = p[2]; M = p[3]; dt = p[4]; }
+	else { K = p[0]; M = p[1]; dt = p[2]; }
+	for (int step = 0; step < steps; step++) {
+		for (int i = 0; i < nodes(oldGrid); i++) {
+			double phi = oldGrid(i);
+			if (shipped)
+				temp(i) = -r * phi + u * pow(phi, 3) - K * laplacian(oldGrid, i);
+			else
+				temp(i) = 2.0 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) - K * laplacian(oldGrid, i);
+		}
+		ghostswap(temp);
+		for (int i = 0; i < nodes(oldGrid); i++)
+			newGrid(i) = oldGrid(i) + dt * M * laplacian(temp, i);
+		swap(oldGrid, newGrid);
+		ghostswap(oldGrid);
+	}
+}
+
+template <int dim> void ac_scalar_update(grid<dim, double>& oldGrid, int steps,
+                                         const std::vector<double>& p)
+{
+	ghostswap(oldGrid);
+	grid<dim, double> newGrid(oldGrid);
+	double r = p[0], u = p[1], K = p[2], M = p[3], dt = p[4];
+	for (int step = 0; step < steps; step++) {
+		for (int i = 0; i < nodes(oldGrid); i++) {
+			double phi = oldGrid(i);
+			newGrid(i) = phi - dt * M * (-r * phi + u * pow(phi, 3) - K * laplacian(oldGrid, i));
+		}
+		swap(oldGrid, newGrid);
+		ghostswap(oldGrid);
+	}
+}
+
+template <int dim> void gg_update(grid<dim, vector<double> >& oldGrid, int steps, bool shipped,
+                                  const std::vector<double>& p)
+{
+	ghostswap(oldGrid);
+	grid<dim, vector<double> > newGrid(oldGrid);
+	double gamma = 0, kappa = 0, L = 0, dt;
+	if (shipped) dt = p[0];
+	else { gamma = p[0]; kappa = p[1]; L = p[2]; dt = p[3]; }
+	for (int step = 0; step < steps; step++) {
+		for (int i = 0; i < nodes(oldGrid); i++) {
+			const vector<double>& phi = oldGrid(i);
+			vector<double> lap = laplacian(oldGrid, i);
+			double sum = 0.0;
+			for (int j = 0; j < fields(oldGrid); j++)
+				sum += phi[j] * phi[j];
+			for (int j = 0; j < fields(oldGrid); j++) {
+				if (shipped)
+					newGrid(i)[j] = phi[j] - dt * (-phi[j] - pow(phi[j], 3) + 2.0 * (phi[j] * sum - lap[j]));
+				else
+					newGrid(i)[j] = phi[j] - dt * L * (-phi[j] + phi[j] * phi[j] * phi[j]
+					                + 2.0 * gamma * phi[j] * (sum - phi[j] * phi[j])
+					                - kappa * lap[j]);
+			}
+		}
+		swap(oldGrid, newGrid);
+		ghostswap(oldGrid);
+	}
+}
+
+} // namespace MMSP
+
+static double now_s()
+{
+	using namespace std::chrono;
+	return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+template <int dim> int run_scalar(const std::string& model, const char* in, const char* out,
+                                  int steps, const std::vector<double>& p)
+{
+	MMSP::grid<dim, double> g(in);
+	double t0 = now_s();
+	if (model == "ch_baseline") MMSP::ch_update(g, steps, false, p);
+	else if (model == "ch_shipped") MMSP::ch_update(g, steps, true, p);
+	else if (model == "ac_scalar") MMSP::ac_scalar_update(g, steps, p);
+	else return 2;
+	double t1 = now_s();
+	std::printf("update_seconds %.9f\n", t1 - t0);
+	MMSP::output(g, out);
+	return 0;
+}
+
+template <int dim> int run_vector(const std::string& model, const char* in, const char* out,
+                                  int steps, const std::vector<double>& p)
+{
+	MMSP::grid<dim, MMSP::vector<double> > g(in);
+	double t0 = now_s();
+	if (model == "ac_baseline") MMSP::gg_update(g, steps, false, p);
+	else if (model == "graingrowth") MMSP::gg_update(g, steps, true, p);
+	else return 2;
+	double t1 = now_s();
+	std::printf("update_seconds %.9f\n", t1 - t0);
+	MMSP::output(g, out);
+	return 0;
+}
+
+int main(int argc, char* argv[])
+{
+	if (argc < 5) {
+		std::cerr << "usage: ref_update MODEL IN OUT STEPS [params...]" << std::endl;
+		return 1;
+	}
+	std::string model = argv[1];
+	int steps = std::atoi(argv[4]);
+	std::vector<double> p;
+	for (int i = 5; i < argc; i++) p.push_back(std::atof(argv[i]));
+	size_t need = (model == "ch_baseline") ? 3 : (model == "ch_shipped" || model == "ac_scalar") ? 5
+	            : (model == "ac_baseline") ? 4 : (model == "graingrowth") ? 1 : 0;
+	if (need == 0 || p.size() != need) {
+		std::cerr << "bad model or parameter count" << std::endl;
+		return 1;
+	}
+	std::ifstream hdr(argv[2]);
+	std::string type;
+	int dim = 0;
+	std::getline(hdr, type);
+	hdr >> dim;
+	hdr.close();
+	bool vec = type.find("vector") != std::string::npos;
+	int rc = 2;
+	if (vec) {
+		if (dim == 1) rc = run_vector<1>(model, argv[2], argv[3], steps, p);
+		if (dim == 2) rc = run_vector<2>(model, argv[2], argv[3], steps, p);
+		if (dim == 3) rc = run_vector<3>(model, argv[2], argv[3], steps, p);
+	} else {
+		if (dim == 1) rc = run_scalar<1>(model, argv[2], argv[3], steps, p);
+		if (dim == 2) rc = run_scalar<2>(model, argv[2], argv[3], steps, p);
+		if (dim == 3) rc = run_scalar<3>(model, argv[2], argv[3], steps, p);
+	}
+	if (rc) std::cerr << "model/type mismatch: " << model << " on " << type << std::endl;
+	return rc;
+}

@@ -1,0 +1,171 @@
+"""Generate the golden vectors in tests/golden/ from the reference itself.
+
+Run in a container that holds the reference source (its headers are compiled
+by ``make -C oracle ref`` into ``oracle/_ref/ref_update``):
+
+    python tests/golden/make_golden.py            # small fixtures (*.npz)
+    python tests/golden/make_golden.py --full     # + full-size checksums
+
+Small fixtures: seeded start states are written as MMSP grid files with
+``mmsp_gb300.gridfile``, advanced by the reference's own ``grid``,
+``laplacian`` and ``swap`` (ref_update.cpp), and the reference's output file
+is read back.  Each ``.npz`` holds the start state, the reference's result,
+the model, its parameters and the step count.
+
+Full-size checksums (``full_size.json``): 2D CH 256x256 x 2000 steps is run
+through the reference itself; the 3D configurations (256^3 CH, 128^3 x 8 AC)
+would take hours through the reference's per-cell allocations, so they are
+run through the C oracle, which the small fixtures pin bit for bit to the
+reference.  Each entry stores the SHA-256 of the final float64 array (node
+order, little-endian), mass/energy and a strided sample.
+"""
+import argparse
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from mmsp_gb300 import gridfile, inputs  # noqa: E402
+from oracle import pf_oracle  # noqa: E402
+
+# (name, model, shape, fields, start, params, steps, extra)
+SMALL = [
+    ("ch2d_baseline", "ch_baseline", (40, 56), 0, ("noise", 0.5, 0.01, 11), (1.0, 1.0, 0.005), 200, {}),
+    ("ch3d_baseline", "ch_baseline", (12, 16, 20), 0, ("noise", 0.4, 0.02, 12), (1.0, 1.0, 0.002), 60, {}),
+    ("ch1d_baseline", "ch_baseline", (64,), 0, ("noise", 0.5, 0.05, 13), (1.0, 1.0, 0.005), 300, {}),
+    ("ch2d_baseline_dx", "ch_baseline", (24, 36), 0, ("noise", 0.5, 0.01, 14), (0.7, 1.3, 0.001), 100,
+     {"dx": [0.5, 2.0]}),
+    ("ch2d_baseline_neumann", "ch_baseline", (20, 28), 0, ("noise", 0.5, 0.02, 15), (1.0, 1.0, 0.005), 80,
+     {"bc": [[1, 1], [4, 0]]}),
+    ("ch2d_shipped", "ch_shipped", (32, 24), 0, ("noise", 0.0, 1.0, 16), (1.0, 1.0, 1.0, 1.0, 0.01), 50, {}),
+    ("ch3d_shipped", "ch_shipped", (10, 8, 12), 0, ("noise", 0.0, 1.0, 17), (1.0, 1.0, 1.0, 1.0, 0.01), 20, {}),
+    ("ac_scalar2d_shipped", "ac_scalar", (32, 32), 0, ("noise", 0.0, 1.0, 18), (1.0, 1.0, 1.0, 1.0, 0.01), 50, {}),
+    ("ac3d_baseline", "ac_baseline", (10, 12, 14), 8, ("voronoi", 20, 19), (1.5, 2.0, 1.0, 0.05), 30, {}),
+    ("ac2d_baseline", "ac_baseline", (24, 20), 4, ("voronoi", 12, 20), (1.5, 2.0, 1.0, 0.05), 40, {}),
+    ("ac3d_baseline_n3", "ac_baseline", (8, 9, 10), 3, ("voronoi", 9, 21), (1.2, 1.5, 0.8, 0.04), 25, {}),
+    ("gg2d_shipped", "graingrowth", (64, 64), 2, ("circles",), (0.01,), 100, {}),
+    ("gg3d_shipped", "graingrowth", (36, 36, 4), 2, ("circles",), (0.01,), 40, {}),
+]
+
+
+def start_state(shape, fields, spec):
+    kind = spec[0]
+    if kind == "noise":
+        _, mean, amp, seed = spec
+        return inputs.noisy_composition(shape, mean, amp, seed)
+    if kind == "voronoi":
+        _, pts, seed = spec
+        return inputs.voronoi_grains(shape, pts, fields, seed)
+    if kind == "circles":
+        return inputs.graingrowth_circles(shape, fields)
+    raise ValueError(kind)
+
+
+def run_ref(model, data, vector, fields, steps, params, dx=None, bc=None):
+    dim = data.ndim - (1 if vector else 0)
+    shape = data.shape[:dim]
+    g = gridfile.GridData(dim=dim, g0=[0] * dim, g1=list(shape),
+                          dx=list(dx) if dx else [1.0] * dim, data=data,
+                          vector=vector, fields=fields,
+                          b0=[b[0] for b in bc] if bc else [],
+                          b1=[b[1] for b in bc] if bc else [])
+    with tempfile.TemporaryDirectory() as td:
+        fin = os.path.join(td, "in.dat")
+        fout = os.path.join(td, "out.dat")
+        gridfile.write(fin, g)
+        res = subprocess.run([pf_oracle.REF_BIN, model, fin, fout, str(steps)] + [repr(float(p)) for p in params],
+                             check=True, capture_output=True, text=True)
+        secs = float(res.stdout.split()[-1])
+        out = gridfile.read(fout)
+    return out.data, secs
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def make_small():
+    for name, model, shape, fields, spec, params, steps, extra in SMALL:
+        x0 = start_state(shape, fields, spec)
+        vector = fields > 0
+        out, secs = run_ref(model, x0, vector, fields, steps, params, extra.get("dx"), extra.get("bc"))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), start=x0, result=out, model=model,
+                            params=np.asarray(params, dtype=np.float64), steps=steps,
+                            dx=np.asarray(extra.get("dx", [1.0] * len(shape))),
+                            bc=np.asarray(extra.get("bc", [[2, 2]] * len(shape))))
+        print("%-24s %s steps=%d ref %.3fs" % (name, shape, steps, secs))
+
+
+def make_full():
+    out = {}
+    # configuration 1: 2D CH 256^2 float64, 2000 steps, through the reference itself
+    c0 = inputs.noisy_composition((256, 256), 0.5, 0.01, 1)
+    t = time.time()
+    ref, secs = run_ref("ch_baseline", c0, False, 0, 2000, (1.0, 1.0, 0.005))
+    port = pf_oracle.ch_baseline(c0, 2000, 1.0, 1.0, 0.005)
+    assert np.array_equal(ref, port), "C oracle differs from the reference on 2D CH 256^2"
+    m, e = pf_oracle.ch_mass_energy(ref, 1.0)
+    m0, e0 = pf_oracle.ch_mass_energy(c0, 1.0)
+    out["ch2d_256_2000"] = dict(shape=[256, 256], seed=1, mean=0.5, amplitude=0.01, kappa=1.0, M=1.0,
+                                dt=0.005, steps=2000, source="reference", ref_update_seconds=secs,
+                                sha256=sha(ref), mass0=m0, energy0=e0, mass=m, energy=e,
+                                sample_stride=97, sample=ref.ravel()[::97][:64].tolist())
+    print("ch2d_256_2000 ref %.1fs (total %.1fs)" % (secs, time.time() - t))
+    # configuration 2: 3D CH 256^3 float64, 1000 steps, through the pinned C oracle
+    c0 = inputs.noisy_composition((256, 256, 256), 0.4, 0.02, 2)
+    t = time.time()
+    res = pf_oracle.ch_baseline(c0, 1000, 1.0, 1.0, 0.002)
+    dt_s = time.time() - t
+    m0, e0 = pf_oracle.ch_mass_energy(c0, 1.0)
+    m, e = pf_oracle.ch_mass_energy(res, 1.0)
+    out["ch3d_256_1000"] = dict(shape=[256, 256, 256], seed=2, mean=0.4, amplitude=0.02, kappa=1.0, M=1.0,
+                                dt=0.002, steps=1000, source="oracle", oracle_seconds=dt_s,
+                                sha256=sha(res), mass0=m0, energy0=e0, mass=m, energy=e,
+                                sample_stride=1000003, sample=res.ravel()[::1000003].tolist())
+    print("ch3d_256_1000 oracle %.1fs" % dt_s)
+    # configuration 3: 3D AC 128^3 x 8, Voronoi 200 seeds; dt=0.05 (stable) and dt=0.1 (as stated)
+    e0 = inputs.voronoi_grains((128, 128, 128), 200, 8, 3)
+    t = time.time()
+    res = pf_oracle.ac_baseline(e0, 500, 1.5, 2.0, 1.0, 0.05)
+    dt_s = time.time() - t
+    m, e = pf_oracle.ac_mass_energy(res, 1.5, 2.0)
+    out["ac3d_128_n8_dt0.05_500"] = dict(shape=[128, 128, 128], fields=8, points=200, seed=3, gamma=1.5,
+                                         kappa=2.0, L=1.0, dt=0.05, steps=500, source="oracle",
+                                         oracle_seconds=dt_s, sha256=sha(res), mass=m.tolist(), energy=e,
+                                         sample_stride=999983, sample=res.ravel()[::999983].tolist())
+    print("ac3d dt=0.05 oracle %.1fs" % dt_s)
+    x = e0.copy()
+    first_bad = None
+    maxabs = []
+    for s in range(1, 41):
+        x = pf_oracle.ac_baseline(x, 1, 1.5, 2.0, 1.0, 0.1)
+        mx = float(np.nanmax(np.abs(x))) if np.isfinite(x).any() else float("nan")
+        maxabs.append(mx)
+        if first_bad is None and not np.isfinite(x).all():
+            first_bad = s
+            break
+    out["ac3d_128_n8_dt0.1_divergence"] = dict(dt=0.1, first_nonfinite_step=first_bad, max_abs_per_step=maxabs,
+                                               source="oracle")
+    print("ac3d dt=0.1 first non-finite step", first_bad)
+    with open(os.path.join(HERE, "full_size.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--full", action="store_true")
+    args = ap.parse_args()
+    if not pf_oracle.ref_available():
+        sys.exit("build the reference program first: make -C oracle ref")
+    make_small()
+    if args.full:
+        make_full()

@@ -1,0 +1,96 @@
+"""The C ABI library on a machine without a GPU: it loads, exports every
+symbol include/MMSP.gpu.h declares, and its host-only entry points work."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "MMSP.gpu.h")).read()
+    return sorted(set(re.findall(r"\b(mmsp_gpu_[a-z_0-9]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mmsp_gb300 import build, native
+
+    if not os.path.exists(build.LIB):
+        build.build()
+    return native.load()
+
+
+def test_header_and_binding_agree():
+    from mmsp_gb300 import native
+
+    assert header_symbols() == sorted(native.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in header_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_version_and_strerror(lib):
+    assert lib.mmsp_gpu_version() == 1
+    assert lib.mmsp_gpu_strerror(0) == b"ok"
+    assert lib.mmsp_gpu_strerror(-4) == b"unsupported configuration"
+
+
+def test_desc_init_defaults(lib):
+    from mmsp_gb300 import native
+
+    d = native.Desc()
+    n = (ctypes.c_int * 3)(256, 256, 1)
+    assert lib.mmsp_gpu_desc_init(ctypes.byref(d), 2, n, 1, native.F64, native.CH) == 0
+    assert (d.dim, d.n[0], d.n[1], d.n[2], d.fields) == (2, 256, 256, 1, 1)
+    assert [d.bc[a][s] for a in range(3) for s in range(2)] == [native.BC_PERIODIC] * 6
+    assert d.dt == 0.005 and d.kappa == 1.0 and d.mobility == 1.0
+    assert lib.mmsp_gpu_desc_init(ctypes.byref(d), 3, n, 2, native.F32, native.GG) == 0
+    assert d.dt == 0.01 and d.kappa == 2.0
+
+
+def test_validation_without_device(lib):
+    from mmsp_gb300 import native
+
+    d = native.make_desc((8, 8), model="ch")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.OK
+    d.bc[0][0] = native.BC_NEUMANN
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EUNSUPPORTED
+    d = native.make_desc((8, 8), fields=2, model="ch")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL
+    d = native.make_desc((8, 8, 8), fields=40, model="ac")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EUNSUPPORTED
+    d = native.make_desc((8, 0), model="ch")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL
+    d = native.make_desc((8, 8), model="ch", dx=[0.0, 1.0])
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL
+    d = native.make_desc((8, 8), model="ch", dt=float("nan"))
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL
+    d.dim = 4
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL
+    assert lib.mmsp_gpu_validate(None) == native.EINVAL
+
+
+def test_footprint(lib):
+    from mmsp_gb300 import native
+
+    d = native.make_desc((256, 256, 256), model="ch", dtype=np.float32)
+    b = ctypes.c_size_t()
+    assert lib.mmsp_gpu_footprint(ctypes.byref(d), ctypes.byref(b)) == 0
+    assert b.value >= 2 * 256 ** 3 * 4
+    assert b.value < 2 * 256 ** 3 * 4 + (1 << 20)
+
+
+def test_null_arguments_are_rejected(lib):
+    from mmsp_gb300 import native
+
+    assert lib.mmsp_gpu_create(None, None) == native.EINVAL
+    assert lib.mmsp_gpu_destroy(None) == native.OK
+    assert lib.mmsp_gpu_step(None, 1) == native.EINVAL
+    assert lib.mmsp_gpu_reduce(None, None) == native.EINVAL
+    assert lib.mmsp_gpu_last_error(None) == b"NULL handle"

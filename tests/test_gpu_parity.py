@@ -1,0 +1,274 @@
+"""Parity of the device step with the reference, through the C ABI.
+
+FP64 (plain form): bit-identical to the reference's own update() on the
+golden fixtures, and to the CPU oracle on seeded random grids of ragged
+shapes.  The shipped examples' pow(x,3) is evaluated on the device by a
+compensated cube, so those forms are held to 1e-12 relative instead.
+FP32 (precision form): max error against the FP64 oracle within 1e-5.
+"""
+import glob
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+TOL_SHIPPED = 1e-12   # relative, forms with pow(x,3)
+TOL_F32 = 1e-5        # absolute, FP32 against FP64 after the stated steps
+
+
+def desc_for(native, model, params, shape, fields, dtype, dx=None, bc=None):
+    p = [float(v) for v in params]
+    kw = dict(dx=dx, bc=bc)
+    if model == "ch_baseline":
+        return native.make_desc(shape, 1, dtype, "ch", kappa=p[0], mobility=p[1], dt=p[2], **kw)
+    if model == "ch_shipped":
+        return native.make_desc(shape, 1, dtype, "ch_poly", r=p[0], u=p[1], kappa=p[2], mobility=p[3], dt=p[4], **kw)
+    if model == "ac_scalar":
+        return native.make_desc(shape, 1, dtype, "ac_poly", r=p[0], u=p[1], kappa=p[2], mobility=p[3], dt=p[4], **kw)
+    if model == "ac_baseline":
+        return native.make_desc(shape, fields, dtype, "ac", gamma=p[0], kappa=p[1], mobility=p[2], dt=p[3], **kw)
+    if model == "graingrowth":
+        return native.make_desc(shape, fields, dtype, "gg", dt=p[0], **kw)
+    raise ValueError(model)
+
+
+def run_gpu(native, desc, x, steps, layout=0):
+    with native.Stepper(desc) as s:
+        s.upload(x, layout)
+        s.step(steps)
+        return s.download(layout)
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, "<f8").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(f)[:-4] for f in FIXTURES])
+def test_fp64_matches_reference_fixture(gpu, path):
+    z = np.load(path)
+    model = str(z["model"])
+    x = z["start"]
+    vector = model in ("ac_baseline", "graingrowth")
+    shape = x.shape[:-1] if vector else x.shape
+    fields = x.shape[-1] if vector else 1
+    bc = z["bc"].tolist()
+    d = desc_for(gpu, model, z["params"], shape, fields, np.float64, dx=z["dx"].tolist(), bc=bc)
+    if any(b != [2, 2] for b in bc):
+        with pytest.raises(gpu.GpuError) as ei:
+            gpu.Stepper(d)
+        assert ei.value.code == gpu.EUNSUPPORTED
+        return
+    got = run_gpu(gpu, d, x, int(z["steps"]))
+    want = z["result"]
+    if model in ("ch_baseline", "ac_baseline"):
+        assert np.array_equal(got, want), "max |diff| %g" % np.abs(got - want).max()
+    else:
+        rel = np.abs(got - want).max() / np.abs(want).max()
+        assert rel <= TOL_SHIPPED, rel
+
+
+RAGGED = [(7,), (1, 9), (5, 7), (33, 45), (2, 3, 5), (1, 4, 6), (17, 33, 45), (40, 3, 70), (3, 50, 33)]
+
+
+@pytest.mark.parametrize("shape", RAGGED, ids=["x".join(map(str, s)) for s in RAGGED])
+def test_fp64_ch_ragged_shapes_bitwise(gpu, oracle, shape):
+    from mmsp_gb300 import inputs
+
+    c0 = inputs.noisy_composition(shape, 0.45, 0.03, 1000 + len(shape))
+    d = gpu.make_desc(shape, 1, np.float64, "ch", kappa=1.0, mobility=1.0, dt=0.002)
+    got = run_gpu(gpu, d, c0, 9)
+    want = oracle.ch_baseline(c0, 9, 1.0, 1.0, 0.002)
+    assert np.array_equal(got, want), "max |diff| %g" % np.abs(got - want).max()
+
+
+@pytest.mark.parametrize("shape,fields", [((6,), 2), ((9, 11), 3), ((5, 6, 7), 8), ((20, 9, 37), 5), ((2, 40, 3), 16)])
+def test_fp64_ac_ragged_shapes_bitwise(gpu, oracle, shape, fields):
+    from mmsp_gb300 import inputs
+
+    e0 = inputs.voronoi_grains(shape, 6, fields, 77)
+    d = gpu.make_desc(shape, fields, np.float64, "ac", gamma=1.5, kappa=2.0, mobility=1.0, dt=0.05)
+    got = run_gpu(gpu, d, e0, 7)
+    want = oracle.ac_baseline(e0, 7, 1.5, 2.0, 1.0, 0.05)
+    assert np.array_equal(got, want), "max |diff| %g" % np.abs(got - want).max()
+
+
+def test_fp64_nonunit_spacing_and_parameters(gpu, oracle):
+    from mmsp_gb300 import inputs
+
+    c0 = inputs.noisy_composition((12, 14, 16), 0.5, 0.02, 9)
+    d = gpu.make_desc(c0.shape, 1, np.float64, "ch", kappa=0.7, mobility=1.3, dt=0.0005, dx=[0.9, 1.1, 1.7])
+    got = run_gpu(gpu, d, c0, 11)
+    want = oracle.ch_baseline(c0, 11, 0.7, 1.3, 0.0005, dx=[0.9, 1.1, 1.7])
+    assert np.array_equal(got, want)
+
+
+def test_graph_replay_long_run_bitwise(gpu, oracle):
+    """Runs long enough for CUDA-graph replay (64-step graphs), started from
+    both ping-pong buffers, match a plain run."""
+    from mmsp_gb300 import inputs
+
+    c0 = inputs.noisy_composition((16, 20, 24), 0.4, 0.02, 12)
+    d = gpu.make_desc(c0.shape, 1, np.float64, "ch", dt=0.002)
+    with gpu.Stepper(d) as s:
+        s.upload(c0)
+        s.step(1)
+        s.step(300)    # odd buffer start: one plain step, graphs, remainder
+        s.step(129)
+        got = s.download()
+    want = oracle.ch_baseline(c0, 430, 1.0, 1.0, 0.002)
+    assert np.array_equal(got, want)
+
+
+def test_layouts_and_transfers(gpu, oracle):
+    from mmsp_gb300 import inputs
+
+    e0 = inputs.voronoi_grains((8, 9, 10), 5, 4, 3)
+    d = gpu.make_desc(e0.shape[:-1], 4, np.float64, "ac", gamma=1.5, kappa=2.0, dt=0.05)
+    a = run_gpu(gpu, d, e0, 3, layout=gpu.CELL_MAJOR)
+    b = run_gpu(gpu, d, np.moveaxis(e0, -1, 0).copy(), 3, layout=gpu.FIELD_MAJOR)
+    assert np.array_equal(a, np.moveaxis(b, 0, -1))
+    with gpu.Stepper(d) as s:
+        with pytest.raises(ValueError):
+            s.upload(e0[:-1])
+        import ctypes
+        buf = np.zeros(10)
+        rc = gpu.load().mmsp_gpu_upload(s.h, buf.ctypes.data, buf.nbytes, 0)
+        assert rc == gpu.EINVAL
+        assert b"bytes" in gpu.load().mmsp_gpu_last_error(s.h)
+
+
+def test_one_shot_update_matches_handle(gpu, oracle):
+    from mmsp_gb300 import inputs
+
+    c0 = inputs.noisy_composition((30, 31), 0.5, 0.01, 4)
+    d = gpu.make_desc(c0.shape, 1, np.float64, "ch", dt=0.005)
+    out, st = gpu.update(c0, 150, d)
+    want = oracle.ch_baseline(c0, 150, 1.0, 1.0, 0.005)
+    assert np.array_equal(out, want)
+    m, e = oracle.ch_mass_energy(want, 1.0)
+    assert st.mass == pytest.approx(m, rel=1e-12)
+    assert st.energy == pytest.approx(e, rel=1e-12)
+    assert st.steps == 150 and st.gpu_ms > 0
+
+
+@pytest.mark.parametrize("model", ["ch", "ac"])
+def test_reductions_match_oracle(gpu, oracle, model):
+    from mmsp_gb300 import inputs
+
+    if model == "ch":
+        x = inputs.noisy_composition((21, 34, 19), 0.4, 0.05, 21)
+        d = gpu.make_desc(x.shape, 1, np.float64, "ch", kappa=0.8, dx=[0.5, 1.0, 2.0])
+        m, e = oracle.ch_mass_energy(x, 0.8, dx=[0.5, 1.0, 2.0])
+    else:
+        x = inputs.voronoi_grains((14, 15, 16), 9, 5, 22) * 0.9 + 0.01
+        d = gpu.make_desc(x.shape[:-1], 5, np.float64, "ac", gamma=1.5, kappa=2.0)
+        ms, e = oracle.ac_mass_energy(x, 1.5, 2.0)
+        m = float(np.sum(ms))
+    with gpu.Stepper(d) as s:
+        s.upload(x)
+        st = s.reduce()
+    assert st.mass == pytest.approx(m, rel=1e-12)
+    assert st.energy == pytest.approx(e, rel=1e-12)
+
+
+def test_fp32_precision_form_small(gpu, oracle):
+    from mmsp_gb300 import inputs
+
+    c0 = inputs.noisy_composition((32, 40, 48), 0.4, 0.02, 31)
+    d = gpu.make_desc(c0.shape, 1, np.float32, "ch", dt=0.002)
+    got = run_gpu(gpu, d, c0.astype(np.float32), 200).astype(np.float64)
+    want = oracle.ch_baseline(c0, 200, 1.0, 1.0, 0.002)
+    assert np.abs(got - want).max() <= TOL_F32
+    e0 = inputs.voronoi_grains((20, 24, 28), 15, 8, 32)
+    d = gpu.make_desc(e0.shape[:-1], 8, np.float32, "ac", gamma=1.5, kappa=2.0, dt=0.05)
+    got = run_gpu(gpu, d, e0.astype(np.float32), 50).astype(np.float64)
+    want = oracle.ac_baseline(e0, 50, 1.5, 2.0, 1.0, 0.05)
+    assert np.abs(got - want).max() <= TOL_F32
+
+
+def test_errors_are_codes_not_crashes(gpu):
+    d = gpu.make_desc((8, 8), 1, np.float64, "ch", bc=[[1, 1], [2, 2]])
+    with pytest.raises(gpu.GpuError) as ei:
+        gpu.Stepper(d)
+    assert ei.value.code == gpu.EUNSUPPORTED
+    d = gpu.make_desc((8, 8), 2, np.float64, "ch")
+    with pytest.raises(gpu.GpuError) as ei:
+        gpu.Stepper(d)
+    assert ei.value.code == gpu.EINVAL
+    d = gpu.make_desc((8, 8), 1, np.float64, "ch")
+    with gpu.Stepper(d) as s:
+        assert gpu.load().mmsp_gpu_step(s.h, -1) == gpu.EINVAL
+        s.step(0)
+
+
+# ---------------------------------------------------------------- full size
+
+FULL = json.load(open(os.path.join(GOLDEN, "full_size.json")))
+
+
+def test_full_2d_256_fp64_matches_reference_checksum(gpu):
+    from mmsp_gb300 import inputs
+
+    m = FULL["ch2d_256_2000"]
+    c0 = inputs.noisy_composition(tuple(m["shape"]), m["mean"], m["amplitude"], m["seed"])
+    d = gpu.make_desc(c0.shape, 1, np.float64, "ch", kappa=m["kappa"], mobility=m["M"], dt=m["dt"])
+    out, st = gpu.update(c0, m["steps"], d)
+    assert sha(out) == m["sha256"]
+    assert st.mass == pytest.approx(m["mass"], rel=1e-12)
+    assert st.energy == pytest.approx(m["energy"], rel=1e-12)
+
+
+def test_full_3d_256_fp64_checksum_and_fp32_error(gpu):
+    """256^3 Cahn-Hilliard, 1000 steps: FP64 bit-identical to the oracle
+    (checksum); FP32 max error <= 1e-5 against that FP64 state; mass drift."""
+    from mmsp_gb300 import inputs
+
+    m = FULL["ch3d_256_1000"]
+    c0 = inputs.noisy_composition(tuple(m["shape"]), m["mean"], m["amplitude"], m["seed"])
+    d64 = gpu.make_desc(c0.shape, 1, np.float64, "ch", kappa=m["kappa"], mobility=m["M"], dt=m["dt"])
+    out64, st64 = gpu.update(c0, m["steps"], d64)
+    assert sha(out64) == m["sha256"]
+    assert st64.energy == pytest.approx(m["energy"], rel=1e-12)
+    d32 = gpu.make_desc(c0.shape, 1, np.float32, "ch", kappa=m["kappa"], mobility=m["M"], dt=m["dt"])
+    out32, st32 = gpu.update(c0.astype(np.float32), m["steps"], d32)
+    err = np.abs(out32.astype(np.float64) - out64)
+    assert err.max() <= TOL_F32, err.max()
+    assert abs(st32.mass - m["mass0"]) / m["mass0"] < 1e-6
+
+
+def test_full_3d_ac_128_n8(gpu):
+    """128^3 x 8 grain growth (Voronoi, 200 seeds): dt=0.05 FP64 bit-identical
+    to the oracle after 500 steps, FP32 within 1e-5; dt=0.1 diverges at the
+    same step as in the oracle."""
+    from mmsp_gb300 import inputs
+
+    m = FULL["ac3d_128_n8_dt0.05_500"]
+    e0 = inputs.voronoi_grains(tuple(m["shape"]), m["points"], m["fields"], m["seed"])
+    d64 = gpu.make_desc(e0.shape[:-1], 8, np.float64, "ac", gamma=m["gamma"], kappa=m["kappa"],
+                        mobility=m["L"], dt=m["dt"])
+    out64, st = gpu.update(e0, m["steps"], d64)
+    assert sha(out64) == m["sha256"]
+    d32 = gpu.make_desc(e0.shape[:-1], 8, np.float32, "ac", gamma=m["gamma"], kappa=m["kappa"],
+                        mobility=m["L"], dt=m["dt"])
+    out32, _ = gpu.update(e0.astype(np.float32), m["steps"], d32)
+    assert np.abs(out32.astype(np.float64) - out64).max() <= TOL_F32
+    div = FULL["ac3d_128_n8_dt0.1_divergence"]
+    d = gpu.make_desc(e0.shape[:-1], 8, np.float64, "ac", gamma=1.5, kappa=2.0, dt=0.1)
+    first_bad = None
+    with gpu.Stepper(d) as s:
+        s.upload(e0)
+        for k in range(1, 41):
+            s.step(1)
+            x = s.download()
+            if not np.isfinite(x).all():
+                first_bad = k
+                break
+            assert np.abs(x).max() == pytest.approx(div["max_abs_per_step"][k - 1], rel=1e-12)
+    assert first_bad == div["first_nonfinite_step"]
