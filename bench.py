@@ -334,6 +334,36 @@ def run_gpu(args):
     return 0
 
 
+CASES = {
+    # name: (shape, fields, dtype, model, params)
+    "ch3d_f32": (SHAPE, 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
+    "ch3d_f64": (SHAPE, 1, np.float64, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
+    "ch2d_f64": ((256, 256), 1, np.float64, "ch", dict(dt=0.005, kappa=1.0, mobility=1.0)),
+    "ac3d_f32": ((128, 128, 128), 8, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
+    "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
+}
+
+
+def run_case(name: str, steps: int):
+    """Run `steps` explicit steps of one workload once, untimed: the command
+    the ncu summaries under profiles/ are captured from."""
+    from mmsp_gb300 import inputs, native
+
+    shape, fields, dtype, model, params = CASES[name]
+    if fields == 1:
+        x = inputs.noisy_composition(shape, MEAN, AMP, SEED)
+    else:
+        x = inputs.voronoi_grains(shape, 200, fields, 3)
+    d = native.make_desc(shape, fields, dtype, model, **params)
+    with native.Stepper(d) as s:
+        s.upload(x.astype(dtype))
+        s.step(steps)
+        s.synchronize()
+        st = s.reduce()
+    print("case %s: %d steps, mass %.12g energy %.12g" % (name, steps, st.mass, st.energy))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -341,7 +371,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--case", choices=sorted(CASES), help="run one workload untimed (for ncu)")
+    ap.add_argument("--case-steps", type=int, default=5)
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case, args.case_steps)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -23,6 +23,7 @@ struct mmsp_gpu_handle {
     void* buf[2];
     int cur;                 // buf[cur] holds the state
     double* partials;        // reduction scratch
+    int* flags;              // device error word: a kernel's bounded wait ran out
     cudaStream_t own;        // private stream
     cudaStream_t stream;     // stream in use
     cudaEvent_t ev0, ev1;
@@ -48,6 +49,8 @@ static int cuda_fail(mmsp_gpu_handle* h, cudaError_t e, const char* where)
     cudaGetLastError();   // clear a non-sticky error
     return MMSP_GPU_ECUDA;
 }
+
+static int check_flags(mmsp_gpu_handle* h);
 
 extern "C" int mmsp_gpu_version(void) { return MMSP_GPU_ABI_VERSION; }
 
@@ -160,6 +163,7 @@ static void release(mmsp_gpu_handle* h)
     if (h->buf[0]) cudaFree(h->buf[0]);
     if (h->buf[1]) cudaFree(h->buf[1]);
     if (h->partials) cudaFree(h->partials);
+    if (h->flags) cudaFree(h->flags);
     if (h->own) cudaStreamDestroy(h->own);
 }
 
@@ -202,7 +206,8 @@ extern "C" int mmsp_gpu_create(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc)
     if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) goto cuda_err;
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) goto cuda_err;
     if (cudaMalloc(&h->buf[0], h->bytes) != cudaSuccess || cudaMalloc(&h->buf[1], h->bytes) != cudaSuccess ||
-        cudaMalloc((void**)&h->partials, pf::kPartialsBytes) != cudaSuccess) {
+        cudaMalloc((void**)&h->partials, pf::kPartialsBytes) != cudaSuccess ||
+        cudaMalloc((void**)&h->flags, 256) != cudaSuccess || cudaMemset(h->flags, 0, 256) != cudaSuccess) {
         cudaGetLastError();
         release(h);
         delete h;
@@ -298,7 +303,7 @@ static int download(mmsp_gpu_handle* h, void* dst, size_t bytes, int layout, cud
     e = cudaMemcpyAsync(dst, src, bytes, kind, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "download");
     if (sync && (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(h, e, "download sync");
-    return MMSP_GPU_OK;
+    return sync ? check_flags(h) : MMSP_GPU_OK;
 }
 
 extern "C" int mmsp_gpu_upload(mmsp_gpu_handle* h, const void* host, size_t bytes, int layout)
@@ -323,7 +328,7 @@ static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s)
     bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
     const void* in = h->buf[h->cur];
     void* out = h->buf[h->cur ^ 1];
-    cudaError_t e = ch ? pf::launch_ch(h->plan, h->d, h->g, h->c, in, out, s)
+    cudaError_t e = ch ? pf::launch_ch(h->plan, h->d, h->g, h->c, in, out, h->flags, s)
                        : pf::launch_ac(h->plan, h->d, h->g, h->c, in, out, s);
     h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913
     return e;
@@ -391,12 +396,25 @@ extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
     return MMSP_GPU_OK;
 }
 
+// After a synchronisation: report (and clear) a kernel's timed-out wait.
+static int check_flags(mmsp_gpu_handle* h)
+{
+    int f = 0;
+    cudaError_t e = cudaMemcpy(&f, h->flags, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(h, e, "flags");
+    if (f) {
+        cudaMemset(h->flags, 0, sizeof(int));
+        return fail(h, MMSP_GPU_ETIMEDOUT, "%s", "a step kernel's bounded wait ran out; the state is invalid");
+    }
+    return MMSP_GPU_OK;
+}
+
 extern "C" int mmsp_gpu_synchronize(mmsp_gpu_handle* h)
 {
     if (!h) return MMSP_GPU_EINVAL;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
-    return MMSP_GPU_OK;
+    return check_flags(h);
 }
 
 extern "C" int mmsp_gpu_reduce(mmsp_gpu_handle* h, mmsp_gpu_stats* st)
@@ -408,6 +426,8 @@ extern "C" int mmsp_gpu_reduce(mmsp_gpu_handle* h, mmsp_gpu_stats* st)
     e = cudaMemcpyAsync(res, h->partials + 4 * pf::kReduceBlocks, sizeof(res), cudaMemcpyDeviceToHost, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "reduce copy");
     if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(h, e, "reduce sync");
+    int rc = check_flags(h);
+    if (rc) return rc;
     st->mass = res[0];
     st->energy = res[1];
     st->steps = h->steps;

@@ -168,6 +168,7 @@ cudaError_t plan_ac(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     }
     p->grid = dim3(tz, tyn, segs);
     p->fields = d.fields;
+    p->kind = 0;
     p->ok = true;
     return cudaSuccess;
 }

@@ -1,0 +1,81 @@
+// pf_async.cuh -- mbarrier + bulk asynchronous copy (TMA engine) helpers, inline PTX.
+//
+// cp.async.bulk copies a contiguous global range into shared memory and
+// signals completion on an mbarrier with a transaction count.  Addresses must
+// be 16-byte aligned and sizes multiples of 16 bytes; callers guarantee it.
+// Every wait is bounded: mbar_wait returns false after kSpinLimit polls so a
+// kernel can raise its error flag and leave instead of hanging.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pf {
+
+constexpr uint32_t kSpinLimit = 1u << 14;     // polls of try_wait before giving up
+constexpr uint32_t kSuspendHintNs = 100000;  // each poll may sleep this long unless the phase completes
+
+static __device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+static __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// Make initialised barriers visible to the asynchronous proxy.
+static __device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Order this thread's earlier generic-proxy shared-memory accesses before
+// later asynchronous-proxy writes (a slot is refilled after it was read).
+static __device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+static __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// One poll; the thread sleeps until the phase completes or the hint elapses,
+// so waiting warps do not take issue slots from working ones.
+static __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendHintNs)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar` to complete.
+static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kSpinLimit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Global -> shared bulk copy of `bytes` (multiple of 16, both ends 16-byte
+// aligned), completing `bytes` transactions on `bar`.
+static __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+}  // namespace pf

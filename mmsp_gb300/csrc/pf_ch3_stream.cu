@@ -1,0 +1,362 @@
+// pf_ch3_stream.cu -- FP32 3D Cahn-Hilliard step, register streaming along X.
+//
+// The precision-form kernel for 3D grids whose rows (axis Z) hold 32, 64,
+// 128, 256 or 512 cells.  A block owns R consecutive rows (axis Y) of full
+// Z extent and a run of X planes; each thread owns V adjacent cells of a
+// row (V = 1 for 32-cell rows, else 2), so the block has Z/V threads.
+//
+// For every plane the block's R+4 rows (2 halo rows on each side, wrapped
+// periodically) arrive in shared memory through cp.async.bulk on an
+// mbarrier ring, several planes ahead of the one being computed.  Each
+// thread keeps its cells of c for planes x, x+1, x+2 and of mu for x-1, x,
+// x+1 in registers: Y neighbours are neighbouring registers, X neighbours
+// the neighbouring planes' registers, Z neighbours inside a thread are
+// registers, Z neighbours across threads come from shared memory (c) or
+// warp shuffles (mu), and the two cells at each warp's ends exchange mu
+// through a small shared array that wraps periodically across the row.
+// mu is recomputed only on the 2 halo rows of the strip; a block spans whole
+// rows, so there is no Z halo.
+//
+// FP32 arithmetic is reassociated for throughput (six-neighbour sums and
+// Horner's form of f'(c)); the result is checked against the FP64 oracle
+// with a tolerance, not bitwise.
+#include "pf_async.cuh"
+#include "pf_device.cuh"
+#include "pf_internal.h"
+
+namespace pf {
+
+#ifndef PF_CH3_RING
+#define PF_CH3_RING 4
+#endif
+#ifndef PF_CH3_MINB
+#define PF_CH3_MINB 1
+#endif
+#ifndef PF_CH3_R
+#define PF_CH3_R 8
+#endif
+constexpr int kRing = PF_CH3_RING;   // planes staged in shared memory (kRing-1 in flight)
+constexpr int kStreamR = PF_CH3_R;   // rows per block strip
+
+struct F32Coef {
+    float wx, wy, wz, w2;   // Laplacian weights, w2 = 2(wx+wy+wz)
+    float kappa, dtm, neg_r, u;
+};
+
+template <int MODEL>
+static __device__ __forceinline__ float mu_f32(float c, float lap, const F32Coef& q)
+{
+    float fp;
+    if (MODEL == MMSP_GPU_CH) {
+        // 2c(1-c)(1-2c) = c*(2 + c*(-6 + 4c))
+        fp = c * fmaf(fmaf(4.0f, c, -6.0f), c, 2.0f);
+    } else {
+        // -r c + u c^3 = c*(u c^2 - r)
+        fp = c * fmaf(q.u, c * c, q.neg_r);
+    }
+    return fmaf(-q.kappa, lap, fp);
+}
+
+// wx*sx + wy*sy + wz*sz - 2(wx+wy+wz)*c, with sx, sy, sz the sums of the two
+// neighbours along each axis.
+template <bool UNIT>
+static __device__ __forceinline__ float lap_f32(float sx, float sy, float sz, float c, const F32Coef& q)
+{
+    if (UNIT) return fmaf(-6.0f, c, (sx + sy) + sz);
+    return fmaf(q.wx, sx, fmaf(q.wy, sy, fmaf(q.wz, sz, -q.w2 * c)));
+}
+
+template <int V>
+static __device__ __forceinline__ void lds_vec(float (&dst)[V], const float* src)
+{
+    if constexpr (V == 1) {
+        dst[0] = src[0];
+    } else {
+        float2 t = *reinterpret_cast<const float2*>(src);
+        dst[0] = t.x;
+        dst[1] = t.y;
+    }
+}
+
+template <int V>
+static __device__ __forceinline__ void stg_vec(float* dst, const float (&v)[V])
+{
+    if constexpr (V == 1) {
+        dst[0] = v[0];
+    } else {
+        *reinterpret_cast<float2*>(dst) = make_float2(v[0], v[1]);
+    }
+}
+
+// Shared memory: kRing slots of (R+4) x Z floats, the warp-end mu buffers
+// [parity][warp][side][R], then kRing mbarriers.
+static size_t ch3_smem(int R, int Z, int V)
+{
+    int warps = Z / V / 32;
+    return sizeof(float) * (size_t)kRing * (R + 4) * Z + sizeof(float) * 2 * warps * 2 * R +
+           sizeof(uint64_t) * kRing;
+}
+
+template <int R, int Z, int V, int MODEL, bool UNIT>
+__global__ void __launch_bounds__(Z / V, PF_CH3_MINB)
+ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, F32Coef q, int planes,
+               int* __restrict__ err)
+{
+    constexpr int RR = R + 4;
+    constexpr int T = Z / V;             // threads per block
+    constexpr int W = T / 32;            // warps per block (one row)
+    static_assert(T % 32 == 0 && R % 4 == 0, "row split");
+    const int t = threadIdx.x;
+    const int lane = t & 31, warp = t >> 5;
+    const int z0 = t * V;                // first cell of this thread
+    extern __shared__ __align__(128) unsigned char sm[];
+    float* slots = reinterpret_cast<float*>(sm);
+    float* edges = slots + (size_t)kRing * RR * Z;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(edges + 2 * W * 2 * R);
+    __shared__ int s_err;
+
+    const int y0 = blockIdx.x * R;
+    const int xs = blockIdx.y * planes;
+    const int xe = min(xs + planes, g.X);
+    if (xs >= xe) return;
+    const int zl = z0 == 0 ? Z - 1 : z0 - 1;            // cell left of this thread's first
+    const int zh = z0 + V == Z ? 0 : z0 + V;            // cell right of this thread's last
+    const int wl = warp == 0 ? W - 1 : warp - 1;
+    const int wh = warp == W - 1 ? 0 : warp + 1;
+    const int x_first = xs - 2, x_last = xe + 1;        // planes read from global memory
+
+    // producer (thread 0): stage plane pl (wrapped) into its ring slot
+    auto fill = [&](int pl) {
+        const int k = pl - x_first, s = k % kRing;
+        uint64_t* bar = &bars[s];
+        float* dst = slots + (size_t)s * RR * Z;
+        const float* base = cin + (long long)wrapi(pl, g.X) * g.YZ;
+        constexpr uint32_t row = (uint32_t)Z * sizeof(float);
+        fence_proxy_async();
+        mbar_expect_tx(bar, RR * row);
+        const int a = y0 - 2, b = y0 + R + 2;
+        if (a >= 0 && b <= g.Y) {
+            bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
+        } else if (a < 0) {
+            const int n1 = -a;   // rows Y-n1 .. Y-1 first, then 0 ..
+            bulk_g2s(dst, base + (long long)(g.Y - n1) * Z, n1 * row, bar);
+            bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
+        } else {
+            const int n1 = g.Y - a;   // rows a .. Y-1, then 0 ..
+            bulk_g2s(dst, base + (long long)a * Z, n1 * row, bar);
+            bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
+        }
+    };
+    auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % kRing) * RR * Z; };
+    auto wait_plane = [&](int pl) {
+        const int k = pl - x_first;
+        if (!mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u)) {
+            s_err = 1;
+            atomicExch(err, 1);
+        }
+    };
+
+    if (t == 0) {
+        for (int s = 0; s < kRing; s++) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+        s_err = 0;
+    }
+    __syncthreads();
+    if (t == 0)
+        for (int pl = x_first; pl < x_first + kRing && pl <= x_last; pl++) fill(pl);
+
+    float cA[RR][V], cB[RR][V], cC[RR][V];
+    float mA[R + 2][V], mB[R + 2][V], mC[R + 2][V];
+    wait_plane(x_first);
+    wait_plane(x_first + 1);
+    {
+        const float* s0 = slot_of(x_first) + z0;
+        const float* s1 = slot_of(x_first + 1) + z0;
+#pragma unroll
+        for (int i = 0; i < RR; i++) {
+            lds_vec<V>(cA[i], s0 + i * Z);
+            lds_vec<V>(cB[i], s1 + i * Z);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < R + 2; i++)
+#pragma unroll
+        for (int j = 0; j < V; j++) mA[i][j] = mB[i][j] = 0.0f;
+    __syncthreads();
+    if (t == 0 && !s_err && x_first + kRing <= x_last) fill(x_first + kRing);   // slot of x_first is free
+
+    // One plane: a = c(x), b = c(x+1), c = c(x+2) (loaded here); ma = mu(x-1),
+    // mb = mu(x), mc = mu(x+1) (computed here); writes c'(x) when x >= xs.
+    auto iter = [&](int x, float (&a)[RR][V], float (&b)[RR][V], float (&c)[RR][V], float (&ma)[R + 2][V],
+                    float (&mb)[R + 2][V], float (&mc)[R + 2][V]) -> bool {
+        wait_plane(x + 2);
+        const float* s2 = slot_of(x + 2) + z0;
+#pragma unroll
+        for (int i = 0; i < RR; i++) lds_vec<V>(c[i], s2 + i * Z);
+        const float* s1 = slot_of(x + 1);
+#pragma unroll
+        for (int r = -1; r <= R; r++) {
+            const int i = r + 2;
+            const float left = s1[i * Z + zl];
+            const float right = s1[i * Z + zh];
+#pragma unroll
+            for (int j = 0; j < V; j++) {
+                const float cc = b[i][j];
+                const float sz = (j == 0 ? left : b[i][j - 1]) + (j == V - 1 ? right : b[i][j + 1]);
+                const float lap = lap_f32<UNIT>(a[i][j] + c[i][j], b[i - 1][j] + b[i + 1][j], sz, cc, q);
+                mc[r + 1][j] = mu_f32<MODEL>(cc, lap, q);
+            }
+        }
+        // warp ends publish mu(x+1) of rows 0..R-1 for the neighbouring warps
+        float* e1 = edges + (((x + 1) & 1) * W + warp) * 2 * R;
+        if (lane == 0 || lane == 31) {
+            // lane 0 publishes its first cell, lane 31 its last (selects keep mc in registers)
+            const bool first = lane == 0;
+            float* dst = e1 + (first ? 0 : R);
+#pragma unroll
+            for (int r = 0; r < R; r += 4)
+                *reinterpret_cast<float4*>(dst + r) = make_float4(
+                    first ? mc[r + 1][0] : mc[r + 1][V - 1], first ? mc[r + 2][0] : mc[r + 2][V - 1],
+                    first ? mc[r + 3][0] : mc[r + 3][V - 1], first ? mc[r + 4][0] : mc[r + 4][V - 1]);
+        }
+        if (x >= xs) {
+            // the neighbouring warps' end cells: every lane reads the same
+            // words (broadcast) and lanes 0 / 31 select them, without branches
+            const float4* eL = reinterpret_cast<const float4*>(edges + ((x & 1) * W + wl) * 2 * R + R);
+            const float4* eH = reinterpret_cast<const float4*>(edges + ((x & 1) * W + wh) * 2 * R);
+            float el[R], eh[R];
+#pragma unroll
+            for (int r = 0; r < R; r += 4) {
+                const float4 u = eL[r / 4], v = eH[r / 4];
+                el[r] = u.x, el[r + 1] = u.y, el[r + 2] = u.z, el[r + 3] = u.w;
+                eh[r] = v.x, eh[r + 1] = v.y, eh[r + 2] = v.z, eh[r + 3] = v.w;
+            }
+            float* dst = cout + (long long)x * g.YZ + (long long)y0 * Z + z0;
+            const int rows = min(R, g.Y - y0);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const float up = __shfl_up_sync(0xffffffffu, mb[r + 1][V - 1], 1);
+                const float down = __shfl_down_sync(0xffffffffu, mb[r + 1][0], 1);
+                const float left = lane == 0 ? el[r] : up;
+                const float right = lane == 31 ? eh[r] : down;
+                float o[V];
+#pragma unroll
+                for (int j = 0; j < V; j++) {
+                    const float m = mb[r + 1][j];
+                    const float sz = (j == 0 ? left : mb[r + 1][j - 1]) + (j == V - 1 ? right : mb[r + 1][j + 1]);
+                    const float lap = lap_f32<UNIT>(ma[r + 1][j] + mc[r + 1][j], mb[r][j] + mb[r + 2][j], sz, m, q);
+                    o[j] = fmaf(q.dtm, lap, a[r + 2][j]);
+                }
+                if (r < rows) stg_vec<V>(dst + (long long)r * Z, o);
+            }
+        }
+        __syncthreads();
+        if (s_err) return false;
+        if (t == 0 && x + 1 + kRing <= x_last) fill(x + 1 + kRing);   // slot of x+1 is free now
+        return true;
+    };
+
+    int x = x_first;
+    while (!s_err) {
+        if (x >= xe || !iter(x, cA, cB, cC, mA, mB, mC)) break;
+        x++;
+        if (x >= xe || !iter(x, cB, cC, cA, mB, mC, mA)) break;
+        x++;
+        if (x >= xe || !iter(x, cC, cA, cB, mC, mA, mB)) break;
+        x++;
+    }
+    if (s_err && t == 0) {
+        // leave no copy in flight: wait (bounded) for every issued fill
+        for (int pl = max(x, x_first); pl <= min(x + kRing, x_last); pl++) {
+            const int k = pl - x_first;
+            mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u);
+        }
+    }
+}
+
+static F32Coef f32coef(const Coeffs& c)
+{
+    F32Coef q;
+    q.wx = (float)c.w[0];
+    q.wy = (float)c.w[1];
+    q.wz = (float)c.w[2];
+    q.w2 = 2.0f * (q.wx + q.wy + q.wz);
+    q.kappa = (float)c.kappa;
+    q.dtm = (float)c.dtm;
+    q.neg_r = (float)c.neg_r;
+    q.u = (float)c.u;
+    return q;
+}
+
+static bool row_ok(int Z) { return Z == 32 || Z == 64 || Z == 128 || Z == 256 || Z == 512; }
+static int cells_per_thread(int Z) { return Z == 32 ? 1 : 2; }
+
+bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
+{
+    return d.dtype == MMSP_GPU_F32 && g.dim == 3 && row_ok(g.Z) && g.Y >= kStreamR + 4 &&
+           (d.model == MMSP_GPU_CH || d.model == MMSP_GPU_CH_POLY);
+}
+
+template <int Z, int V, bool UNIT>
+static const void* pick_model(bool ch)
+{
+    return ch ? reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH, UNIT>)
+              : reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH_POLY, UNIT>);
+}
+
+template <int Z, int V>
+static const void* pick_unit(bool ch, bool unit)
+{
+    return unit ? pick_model<Z, V, true>(ch) : pick_model<Z, V, false>(ch);
+}
+
+static const void* pick_stream(int Z, bool ch, bool unit)
+{
+    switch (Z) {
+    case 32: return pick_unit<32, 1>(ch, unit);
+    case 64: return pick_unit<64, 2>(ch, unit);
+    case 128: return pick_unit<128, 2>(ch, unit);
+    case 256: return pick_unit<256, 2>(ch, unit);
+    default: return pick_unit<512, 2>(ch, unit);
+    }
+}
+
+cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
+{
+    const Coeffs c = make_coeffs(d);
+    const int V = cells_per_thread(g.Z);
+    const int threads = g.Z / V;
+    p->fn = pick_stream(g.Z, d.model == MMSP_GPU_CH, c.unit_w);
+    p->smem = ch3_smem(kStreamR, g.Z, V);
+    p->block = dim3(threads, 1, 1);
+    cudaError_t e = cudaFuncSetAttribute(p->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, threads, p->smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int strips = (g.Y + kStreamR - 1) / kStreamR;
+    // one wave: strips * segments <= resident blocks, segments >= 1
+    long long slots = (long long)sm_count() * per_sm;
+    int segs = (int)(slots / strips);
+    if (segs < 1) segs = 1;
+    if (segs > g.X) segs = g.X;
+    p->planes = (g.X + segs - 1) / segs;
+    segs = (g.X + p->planes - 1) / p->planes;
+    p->grid = dim3(strips, segs, 1);
+    p->fields = 1;
+    p->kind = 1;
+    p->ok = true;
+    return cudaSuccess;
+}
+
+cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c, const void* in, void* out,
+                              int* err, cudaStream_t s)
+{
+    F32Coef q = f32coef(c);
+    int planes = p.planes;
+    void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes, (void*)&err};
+    return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);
+}
+
+}  // namespace pf

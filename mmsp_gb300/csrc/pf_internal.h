@@ -43,6 +43,7 @@ struct StepPlan {
     size_t smem;
     int planes;        // planes of axis X per block (3D streaming)
     int fields;
+    int kind;          // 0: generic tile kernel, 1: FP32 3D register-streaming kernel
     bool ok;
 };
 
@@ -50,9 +51,16 @@ struct StepPlan {
 cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t plan_ac(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 
-// One step in -> out on `s`.
+// FP32 3D Cahn-Hilliard on whole rows (pf_ch3_stream.cu).
+bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g);
+cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
+cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c, const void* in, void* out,
+                              int* err, cudaStream_t s);
+
+// One step in -> out on `s`.  `err` is a device word a kernel sets when a
+// bounded wait runs out.
 cudaError_t launch_ch(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
-                      const void* in, void* out, cudaStream_t s);
+                      const void* in, void* out, int* err, cudaStream_t s);
 cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
                       const void* in, void* out, cudaStream_t s);
 
