@@ -170,6 +170,34 @@ const char* mmsp_gpu_last_error(const mmsp_gpu_handle* h);
 int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t bytes, int layout,
                     int steps, mmsp_gpu_stats* stats);
 
+/* Largest state (bytes) mmsp_gpu_step_noalloc can advance by more than one
+ * step or in place: the size of the library's fixed device scratch array. */
+#define MMSP_GPU_NOALLOC_MAX_BYTES (16u << 20)
+
+/* Advance a device-resident grid without allocating any memory.
+ *
+ * No counterpart in the reference: MMSP's update() allocates its scratch
+ * grids on every call (cahn-hilliard.cpp:56-57).  This entry point is for
+ * callers that must not call cudaMalloc: code whose device memory belongs to
+ * another allocator or a fixed budget (a framework's memory pool, a serving
+ * loop that has committed its HBM), and hot loops that cannot afford
+ * cudaMalloc/cudaFree, which may synchronise the whole device.
+ *
+ * `in` and `out` are device pointers to field-major state of
+ * desc->fields * cells values of the descriptor's type; `out` may equal
+ * `in`.  The intermediate steps live in one file-scope device array of
+ * MMSP_GPU_NOALLOC_MAX_BYTES shared by every call in the process; a state
+ * larger than that returns MMSP_GPU_ENOMEM when steps > 1 or out == in
+ * (one step from in to a distinct out needs no scratch).  Work is queued on
+ * `cuda_stream` (NULL: the legacy default stream) and the call returns once
+ * it has finished, with MMSP_GPU_ETIMEDOUT if a kernel's bounded wait ran
+ * out.  The first call on a device looks up the array's device address
+ * with that device current; make that first call before any stream capture.
+ * Calls that overlap on the GPU (from several threads or streams) share the
+ * scratch array and race: serialise them. */
+int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, void* out, int steps,
+                          void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,8 +29,9 @@ EXPORTS = [
     "mmsp_gpu_footprint", "mmsp_gpu_create", "mmsp_gpu_destroy", "mmsp_gpu_set_stream",
     "mmsp_gpu_upload", "mmsp_gpu_download", "mmsp_gpu_upload_device", "mmsp_gpu_download_device",
     "mmsp_gpu_step", "mmsp_gpu_synchronize", "mmsp_gpu_reduce", "mmsp_gpu_state",
-    "mmsp_gpu_last_error", "mmsp_gpu_update",
+    "mmsp_gpu_last_error", "mmsp_gpu_update", "mmsp_gpu_step_noalloc",
 ]
+NOALLOC_MAX_BYTES = 16 << 20   # MMSP_GPU_NOALLOC_MAX_BYTES
 
 
 class Desc(ctypes.Structure):
@@ -91,6 +92,7 @@ def load(build_if_missing: bool = False):
         "mmsp_gpu_state": (i, [vp, ctypes.POINTER(vp)]),
         "mmsp_gpu_last_error": (ctypes.c_char_p, [vp]),
         "mmsp_gpu_update": (i, [dp, vp, sz, i, i, ctypes.POINTER(Stats)]),
+        "mmsp_gpu_step_noalloc": (i, [dp, vp, vp, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
