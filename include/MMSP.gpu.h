@@ -170,6 +170,51 @@ const char* mmsp_gpu_last_error(const mmsp_gpu_handle* h);
 int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t bytes, int layout,
                     int steps, mmsp_gpu_stats* stats);
 
+/* ---------------------------------------------------------------------------
+ * Batched form: many independent grids of uneven sizes and parameters
+ * advanced together.  The reference has no batched path (one update() per
+ * grid, cahn-hilliard.cpp:47-81); this replaces a loop of those calls.
+ *
+ * 2D Cahn-Hilliard grids (MMSP_GPU_CH / MMSP_GPU_CH_POLY, fields=1) whose
+ * rows hold a multiple of 32 cells up to 512 share one persistent kernel per
+ * step: a work list of (grid, run of rows) items is drained by all warps of
+ * the GPU.  Other grids in the batch are advanced by their own kernels in
+ * the same step.  All grids share one dtype.  Step chunks replay a CUDA
+ * graph.  The run of rows per work item and the block size are chosen by an
+ * autotuner on the first step (or mmsp_gpu_batch_tune) and cached per batch
+ * shape, in memory and, when the environment variable MMSP_GPU_TUNE_CACHE
+ * names a file, in that JSON file. */
+typedef struct mmsp_gpu_batch mmsp_gpu_batch;
+
+typedef struct mmsp_gpu_batch_info {
+    int instances;          /* grids in the batch */
+    int persistent;         /* grids advanced by the persistent kernel */
+    int fallback;           /* grids advanced by their own kernels */
+    int rows_per_item;      /* autotuned rows per work item (0 before tuning) */
+    int threads_per_block;  /* autotuned block size of the persistent kernel */
+    int blocks;             /* persistent grid size */
+    int items;              /* work items per step */
+    int tuned_from_cache;   /* 1 when the tuning came from the cache */
+    double tune_ms;         /* wall time spent autotuning */
+    size_t device_bytes;    /* device memory the batch holds */
+} mmsp_gpu_batch_info;
+
+int mmsp_gpu_batch_create(mmsp_gpu_batch** out, int count, const mmsp_gpu_desc* descs);
+int mmsp_gpu_batch_destroy(mmsp_gpu_batch* b);
+int mmsp_gpu_batch_set_stream(mmsp_gpu_batch* b, void* cuda_stream);
+/* Copy grid `index` in/out (synchronous), as mmsp_gpu_upload/download. */
+int mmsp_gpu_batch_upload(mmsp_gpu_batch* b, int index, const void* host, size_t bytes, int layout);
+int mmsp_gpu_batch_download(mmsp_gpu_batch* b, int index, void* host, size_t bytes, int layout);
+/* Advance every grid by `steps` steps (asynchronous). */
+int mmsp_gpu_batch_step(mmsp_gpu_batch* b, int steps);
+int mmsp_gpu_batch_synchronize(mmsp_gpu_batch* b);
+/* Mass and free energy of grid `index` (synchronous). */
+int mmsp_gpu_batch_reduce(mmsp_gpu_batch* b, int index, mmsp_gpu_stats* stats);
+/* Run the autotuner now; force != 0 ignores the cache. */
+int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force);
+int mmsp_gpu_batch_get_info(const mmsp_gpu_batch* b, mmsp_gpu_batch_info* info);
+const char* mmsp_gpu_batch_last_error(const mmsp_gpu_batch* b);
+
 /* Largest state (bytes) mmsp_gpu_step_noalloc can advance by more than one
  * step or in place: the size of the library's fixed device scratch array. */
 #define MMSP_GPU_NOALLOC_MAX_BYTES (16u << 20)

@@ -1,0 +1,203 @@
+// pf_batch.cu -- one persistent kernel advancing many 2D Cahn-Hilliard grids.
+//
+// The batched form: instances of uneven sizes and parameters live in one
+// pool (per-instance offsets), and a single launch advances all of them by
+// one explicit step.  The work list holds (instance, run of rows) items,
+// largest first; warps take items from a global counter until none is left,
+// so uneven instances balance across the whole GPU.
+//
+// A warp owns whole rows: lane l holds cells l*V .. l*V+V-1 of a row of
+// n1 = 32*V cells, so the periodic Z neighbours of its first and last cell
+// are one shuffle away (lane 0 wraps to lane 31) and no shared memory or
+// block barrier is needed.  The warp streams down its run of rows (axis 0)
+// keeping c for rows x, x+1, x+2 and mu for x-1, x, x+1 in registers, with
+// the next row's load issued one row ahead.
+//
+// FP64 instances use the reference's operation order (bit-identical to the
+// single-grid kernels and the oracle); FP32 instances use ordinary operators.
+#include "pf_batch.h"
+#include "pf_device.cuh"
+
+namespace pf {
+
+template <typename T, int N>
+static __device__ __forceinline__ void ld_row(T (&dst)[N], const T* __restrict__ src)
+{
+    if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < N; i += 4) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(src) + i / 4);
+            dst[i] = v.x, dst[i + 1] = v.y, dst[i + 2] = v.z, dst[i + 3] = v.w;
+        }
+    } else if constexpr (N % 2 == 0) {
+        using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+#pragma unroll
+        for (int i = 0; i < N; i += 2) {
+            const V2 v = __ldg(reinterpret_cast<const V2*>(src) + i / 2);
+            dst[i] = v.x, dst[i + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) dst[i] = __ldg(src + i);
+    }
+}
+
+template <typename T, int N>
+static __device__ __forceinline__ void st_row(T* __restrict__ dst, const T (&v)[N])
+{
+    if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < N; i += 4)
+            reinterpret_cast<float4*>(dst)[i / 4] = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    } else if constexpr (N % 2 == 0) {
+        using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+#pragma unroll
+        for (int i = 0; i < N; i += 2) {
+            V2 t;
+            t.x = v[i];
+            t.y = v[i + 1];
+            reinterpret_cast<V2*>(dst)[i / 2] = t;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) dst[i] = v[i];
+    }
+}
+
+// 2D Laplacian at cell j of a lane's row segment, reference order: axis 0
+// (rows) then axis 1 (cells of a row).
+template <typename T, int V, bool UNIT>
+static __device__ __forceinline__ T lap2(const T (&lo)[V], const T (&ce)[V], const T (&hi)[V], T left, T right,
+                                         int j, T w0, T w1)
+{
+    using A = Ar<T>;
+    const T y = ce[j];
+    const T y2 = A::mul(T(2), y);
+    T lap = lap_axis<T, UNIT>(T(0), hi[j], y2, lo[j], w0);
+    const T zl = j == 0 ? left : ce[j - 1];
+    const T zh = j == V - 1 ? right : ce[j + 1];
+    return lap_axis<T, UNIT>(lap, zh, y2, zl, w1);
+}
+
+template <typename T, int V, int MODEL, bool UNIT>
+static __device__ void run_rows(const BatchInst& bi, int xs, int xe, const T* __restrict__ in, T* __restrict__ out,
+                                int lane)
+{
+    using A = Ar<T>;
+    const int n0 = bi.n0, n1 = bi.n1;
+    const T* base_in = in + bi.off + lane * V;
+    T* base_out = out + bi.off + lane * V;
+    P<T> p;
+    p.kappa = (T)bi.kappa;
+    p.dtm = (T)bi.dtm;
+    p.neg_r = (T)bi.neg_r;
+    p.u = (T)bi.u;
+    p.gamma2 = T(0);
+    const T w0 = (T)bi.w0, w1 = (T)bi.w1;
+    const unsigned FULL = 0xffffffffu;
+    const int lm = (lane + 31) & 31, lp = (lane + 1) & 31;
+
+    T ca[V], cb[V], cc[V], nx[V];
+    T ma[V], mb[V], mc[V];
+    ld_row<T, V>(ca, base_in + (long long)wrapi(xs - 2, n0) * n1);
+    ld_row<T, V>(cb, base_in + (long long)wrapi(xs - 1, n0) * n1);
+    ld_row<T, V>(nx, base_in + (long long)wrapi(xs, n0) * n1);
+#pragma unroll
+    for (int j = 0; j < V; j++) ma[j] = mb[j] = T(0);
+
+    // a = c(x), b = c(x+1), c = c(x+2); ma = mu(x-1), mb = mu(x), mc = mu(x+1)
+    auto iter = [&](int x, T (&a)[V], T (&b)[V], T (&c)[V], T (&xa)[V], T (&xb)[V], T (&xc)[V]) {
+#pragma unroll
+        for (int j = 0; j < V; j++) c[j] = nx[j];
+        if (x + 3 <= xe + 1) ld_row<T, V>(nx, base_in + (long long)wrapi(x + 3, n0) * n1);
+        const T bl = __shfl_sync(FULL, b[V - 1], lm);
+        const T br = __shfl_sync(FULL, b[0], lp);
+#pragma unroll
+        for (int j = 0; j < V; j++) xc[j] = ch_mu<T, MODEL>(b[j], lap2<T, V, UNIT>(a, b, c, bl, br, j, w0, w1), p);
+        if (x >= xs) {
+            const T ml = __shfl_sync(FULL, xb[V - 1], lm);
+            const T mr = __shfl_sync(FULL, xb[0], lp);
+            T o[V];
+#pragma unroll
+            for (int j = 0; j < V; j++) o[j] = A::add(a[j], A::mul(p.dtm, lap2<T, V, UNIT>(xa, xb, xc, ml, mr, j, w0, w1)));
+            st_row<T, V>(base_out + (long long)x * n1, o);
+        }
+    };
+    int x = xs - 2;
+    while (true) {
+        if (x >= xe) break;
+        iter(x, ca, cb, cc, ma, mb, mc);
+        x++;
+        if (x >= xe) break;
+        iter(x, cb, cc, ca, mb, mc, ma);
+        x++;
+        if (x >= xe) break;
+        iter(x, cc, ca, cb, mc, ma, mb);
+        x++;
+    }
+}
+
+template <typename T, int MODEL, bool UNIT>
+__global__ void __launch_bounds__(128)
+ch2_batch_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items, int nitems,
+                 const T* __restrict__ in, T* __restrict__ out, int* __restrict__ counters, int parity)
+{
+    const int lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters[parity ^ 1] = 0;   // for the next launch
+    while (true) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(&counters[parity], 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= nitems) break;
+        const BatchItem it = items[k];
+        const BatchInst bi = insts[it.inst];
+        switch (bi.n1 >> 5) {
+#define PF_BATCH_CASE(v) \
+    case v: run_rows<T, v, MODEL, UNIT>(bi, it.xs, it.xe, in, out, lane); break;
+            PF_BATCH_CASE(1)
+            PF_BATCH_CASE(2)
+            PF_BATCH_CASE(3)
+            PF_BATCH_CASE(4)
+            PF_BATCH_CASE(5)
+            PF_BATCH_CASE(6)
+            PF_BATCH_CASE(7)
+            PF_BATCH_CASE(8)
+            PF_BATCH_CASE(9)
+            PF_BATCH_CASE(10)
+            PF_BATCH_CASE(11)
+            PF_BATCH_CASE(12)
+            PF_BATCH_CASE(13)
+            PF_BATCH_CASE(14)
+            PF_BATCH_CASE(15)
+            PF_BATCH_CASE(16)
+#undef PF_BATCH_CASE
+        default: break;
+        }
+    }
+}
+
+const void* batch_kernel(int dtype, int model, bool unit)
+{
+    if (dtype == MMSP_GPU_F64) {
+        if (model == MMSP_GPU_CH)
+            return unit ? (const void*)&ch2_batch_kernel<double, MMSP_GPU_CH, true>
+                        : (const void*)&ch2_batch_kernel<double, MMSP_GPU_CH, false>;
+        return unit ? (const void*)&ch2_batch_kernel<double, MMSP_GPU_CH_POLY, true>
+                    : (const void*)&ch2_batch_kernel<double, MMSP_GPU_CH_POLY, false>;
+    }
+    if (model == MMSP_GPU_CH)
+        return unit ? (const void*)&ch2_batch_kernel<float, MMSP_GPU_CH, true>
+                    : (const void*)&ch2_batch_kernel<float, MMSP_GPU_CH, false>;
+    return unit ? (const void*)&ch2_batch_kernel<float, MMSP_GPU_CH_POLY, true>
+                : (const void*)&ch2_batch_kernel<float, MMSP_GPU_CH_POLY, false>;
+}
+
+cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchInst* insts, const BatchItem* items,
+                         int nitems, const void* in, void* out, int* counters, int parity, cudaStream_t s)
+{
+    void* args[] = {(void*)&insts, (void*)&items, (void*)&nitems, (void*)&in, (void*)&out, (void*)&counters,
+                    (void*)&parity};
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
+}
+
+}  // namespace pf

@@ -1,0 +1,38 @@
+// pf_batch.h -- batched 2D Cahn-Hilliard: work-list types and kernel launcher.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pf_internal.h"
+
+namespace pf {
+
+// One instance in the pool.  Parameters are per instance (the batched
+// configuration draws kappa and the mean composition per grid).
+struct BatchInst {
+    long long off;          // element offset of the instance in the pool
+    int n0, n1;             // rows (axis 0) and cells per row (axis 1, a multiple of 32, <= 512)
+    double w0, w1;          // 1/(dx*dx) per axis
+    double kappa, dtm, neg_r, u;
+};
+
+// A run of output rows [xs, xe) of one instance.
+struct BatchItem {
+    int inst, xs, xe;
+};
+
+constexpr int kBatchMaxRow = 512;
+
+// True if a descriptor can join the persistent batched kernel.
+inline bool batch_eligible(const mmsp_gpu_desc& d)
+{
+    if (d.dim != 2 || d.fields != 1) return false;
+    if (d.model != MMSP_GPU_CH && d.model != MMSP_GPU_CH_POLY) return false;
+    return d.n[1] % 32 == 0 && d.n[1] >= 32 && d.n[1] <= kBatchMaxRow && d.n[0] >= 1;
+}
+
+const void* batch_kernel(int dtype, int model, bool unit);
+cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchInst* insts, const BatchItem* items,
+                         int nitems, const void* in, void* out, int* counters, int parity, cudaStream_t s);
+
+}  // namespace pf

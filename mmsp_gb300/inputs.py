@@ -70,6 +70,26 @@ def voronoi_grains(shape, points: int, fields: int, seed: int) -> np.ndarray:
     return eta.reshape(shape + (fields,))
 
 
+def batched_cahn_hilliard(count: int = 256, seed: int = 4, sides=tuple(range(64, 513, 32)),
+                          amplitude: float = 0.01):
+    """The batched 2D Cahn-Hilliard workload: `count` square grids with sides
+    drawn uniformly from `sides`, each with its own kappa ~ U(0.5, 2) and mean
+    composition ~ U(0.3, 0.7), c = mean + amplitude*U(-1, 1) per cell.
+
+    Returns a list of (c0, kappa) pairs.  Stream `seed` gives the per-grid
+    draws (3 values per grid); grid i's cells use stream seed*1000003 + i.
+    """
+    u = uniform(seed, 3 * count).reshape(count, 3)
+    out = []
+    for i in range(count):
+        side = int(sides[min(int(u[i, 0] * len(sides)), len(sides) - 1)])
+        kappa = 0.5 + 1.5 * u[i, 1]
+        mean = 0.3 + 0.4 * u[i, 2]
+        c0 = noisy_composition((side, side), mean, amplitude, seed * 1000003 + i)
+        out.append((c0, float(kappa)))
+    return out
+
+
 def graingrowth_circles(shape, fields: int = 2) -> np.ndarray:
     """The shipped grain-growth start state (graingrowth.cpp:34-51 in 2D/3D,
     :18-30 in 1D): field 1 inside circles of radius 16 on a period-64

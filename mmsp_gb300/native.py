@@ -30,6 +30,9 @@ EXPORTS = [
     "mmsp_gpu_upload", "mmsp_gpu_download", "mmsp_gpu_upload_device", "mmsp_gpu_download_device",
     "mmsp_gpu_step", "mmsp_gpu_synchronize", "mmsp_gpu_reduce", "mmsp_gpu_state",
     "mmsp_gpu_last_error", "mmsp_gpu_update", "mmsp_gpu_step_noalloc",
+    "mmsp_gpu_batch_create", "mmsp_gpu_batch_destroy", "mmsp_gpu_batch_set_stream", "mmsp_gpu_batch_upload",
+    "mmsp_gpu_batch_download", "mmsp_gpu_batch_step", "mmsp_gpu_batch_synchronize", "mmsp_gpu_batch_reduce",
+    "mmsp_gpu_batch_tune", "mmsp_gpu_batch_get_info", "mmsp_gpu_batch_last_error",
 ]
 NOALLOC_MAX_BYTES = 16 << 20   # MMSP_GPU_NOALLOC_MAX_BYTES
 
@@ -45,6 +48,13 @@ class Desc(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("mass", ctypes.c_double), ("energy", ctypes.c_double), ("gpu_ms", ctypes.c_double),
                 ("steps", ctypes.c_int64)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("instances", ctypes.c_int), ("persistent", ctypes.c_int), ("fallback", ctypes.c_int),
+                ("rows_per_item", ctypes.c_int), ("threads_per_block", ctypes.c_int), ("blocks", ctypes.c_int),
+                ("items", ctypes.c_int), ("tuned_from_cache", ctypes.c_int), ("tune_ms", ctypes.c_double),
+                ("device_bytes", ctypes.c_size_t)]
 
 
 class GpuError(RuntimeError):
@@ -93,6 +103,17 @@ def load(build_if_missing: bool = False):
         "mmsp_gpu_last_error": (ctypes.c_char_p, [vp]),
         "mmsp_gpu_update": (i, [dp, vp, sz, i, i, ctypes.POINTER(Stats)]),
         "mmsp_gpu_step_noalloc": (i, [dp, vp, vp, i, vp]),
+        "mmsp_gpu_batch_create": (i, [ctypes.POINTER(vp), i, dp]),
+        "mmsp_gpu_batch_destroy": (i, [vp]),
+        "mmsp_gpu_batch_set_stream": (i, [vp, vp]),
+        "mmsp_gpu_batch_upload": (i, [vp, i, vp, sz, i]),
+        "mmsp_gpu_batch_download": (i, [vp, i, vp, sz, i]),
+        "mmsp_gpu_batch_step": (i, [vp, i]),
+        "mmsp_gpu_batch_synchronize": (i, [vp]),
+        "mmsp_gpu_batch_reduce": (i, [vp, i, ctypes.POINTER(Stats)]),
+        "mmsp_gpu_batch_tune": (i, [vp, i]),
+        "mmsp_gpu_batch_get_info": (i, [vp, ctypes.POINTER(BatchInfo)]),
+        "mmsp_gpu_batch_last_error": (ctypes.c_char_p, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -226,3 +247,83 @@ def update(arr: np.ndarray, steps: int, desc: Desc, layout: int = CELL_MAJOR):
     rc = L.mmsp_gpu_update(ctypes.byref(desc), a.ctypes.data, a.nbytes, layout, int(steps), ctypes.byref(st))
     _check(rc, None, "update")
     return a, st
+
+
+def _bcheck(rc: int, b=None, what: str = ""):
+    if rc != OK:
+        msg = ""
+        if b is not None:
+            try:
+                msg = load().mmsp_gpu_batch_last_error(b).decode()
+            except Exception:
+                msg = ""
+        raise GpuError(rc, (what + ": " + msg) if what else msg)
+
+
+class Batch:
+    """Many grids advanced together (mmsp_gpu_batch_*)."""
+
+    def __init__(self, descs):
+        self.L = load()
+        arr = (Desc * len(descs))(*descs)
+        b = ctypes.c_void_p()
+        _bcheck(self.L.mmsp_gpu_batch_create(ctypes.byref(b), len(descs), arr), None, "batch_create")
+        self.b = b
+        self.descs = list(descs)
+        self.dtype = np.float64 if descs[0].dtype == F64 else np.float32
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.L.mmsp_gpu_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _shape(self, i):
+        d = self.descs[i]
+        s = tuple(d.n[a] for a in range(d.dim))
+        return s if d.fields == 1 else s + (d.fields,)
+
+    def upload(self, i: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        if a.shape != self._shape(i):
+            raise ValueError("shape %s, expected %s" % (a.shape, self._shape(i)))
+        _bcheck(self.L.mmsp_gpu_batch_upload(self.b, i, a.ctypes.data, a.nbytes, CELL_MAJOR), self.b, "upload")
+
+    def download(self, i: int) -> np.ndarray:
+        out = np.empty(self._shape(i), dtype=self.dtype)
+        _bcheck(self.L.mmsp_gpu_batch_download(self.b, i, out.ctypes.data, out.nbytes, CELL_MAJOR), self.b,
+                "download")
+        return out
+
+    def step(self, steps: int):
+        _bcheck(self.L.mmsp_gpu_batch_step(self.b, int(steps)), self.b, "step")
+
+    def synchronize(self):
+        _bcheck(self.L.mmsp_gpu_batch_synchronize(self.b), self.b, "synchronize")
+
+    def reduce(self, i: int) -> Stats:
+        st = Stats()
+        _bcheck(self.L.mmsp_gpu_batch_reduce(self.b, i, ctypes.byref(st)), self.b, "reduce")
+        return st
+
+    def tune(self, force: bool = False):
+        _bcheck(self.L.mmsp_gpu_batch_tune(self.b, 1 if force else 0), self.b, "tune")
+
+    def set_stream(self, stream_ptr):
+        _bcheck(self.L.mmsp_gpu_batch_set_stream(self.b, ctypes.c_void_p(stream_ptr or 0)), self.b, "set_stream")
+
+    def info(self) -> BatchInfo:
+        inf = BatchInfo()
+        _bcheck(self.L.mmsp_gpu_batch_get_info(self.b, ctypes.byref(inf)), self.b, "info")
+        return inf
