@@ -424,6 +424,120 @@ def run_batch(args):
     return 0
 
 
+def serve_requests(n, seed):
+    """The serving mix: 50% 2D CH (sides 64-1024), 30% 3D CH (sides 32-256),
+    20% 3D AC (4-16 order parameters, sides 32-128); steps log-uniform in
+    [100, 10000]; FP32.  dt: 0.005 (2D CH), 0.002 (3D CH), 0.05 (AC)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        kind = rng.random()
+        steps = int(round(10 ** rng.uniform(2.0, 4.0)))
+        if kind < 0.5:
+            s = int(rng.integers(64, 1025))
+            shape, fields, model, p = (s, s), 1, "ch", dict(dt=0.005, kappa=1.0, mobility=1.0)
+        elif kind < 0.8:
+            s = int(rng.integers(32, 257))
+            shape, fields, model, p = (s, s, s), 1, "ch", dict(dt=0.002, kappa=1.0, mobility=1.0)
+        else:
+            s = int(rng.integers(32, 129))
+            fields = int(rng.integers(4, 17))
+            shape, model, p = (s, s, s), "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)
+        out.append((shape, fields, model, p, steps, int(rng.integers(0, 2**31))))
+    return out
+
+
+def make_state(shape, fields, seed):
+    rng = np.random.default_rng(seed)
+    if fields == 1:
+        return (0.4 + 0.02 * (2 * rng.random(shape, dtype=np.float32) - 1)).astype(np.float32)
+    # grains: each cell one random order parameter at 1
+    g = rng.integers(0, fields, size=shape)
+    e = np.zeros(shape + (fields,), np.float32)
+    np.put_along_axis(e, g[..., None], 1.0, axis=-1)
+    return e
+
+
+def run_serve(args):
+    """Poisson arrivals of mixed solves into the request loop; p50/p99 latency
+    and solves/s, at the offered rate and at a sustainable one; one-at-a-time
+    FP64 plain solves/s estimated from per-kind FP64 rates measured here."""
+    import threading
+
+    from mmsp_gb300 import native
+
+    native.load()
+
+    def one_run(rate, n, seed):
+        reqs = serve_requests(n, seed)
+        rng = np.random.default_rng(seed + 1)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+        states = [make_state(sh, f, s) for sh, f, _, _, _, s in reqs]
+        descs = [native.make_desc(sh, f, np.float32, m, **p) for sh, f, m, p, _, _ in reqs]
+        srv = native.Server()
+        ids = [None] * n
+
+        def feeder():
+            t0 = time.perf_counter()
+            for i in range(n):
+                dt = arrivals[i] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                ids[i] = srv.submit(descs[i], states[i], reqs[i][4])
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        lat, fin, sub = [], [], []
+        for i in range(n):
+            st = srv.wait(ids[i], 3600.0)
+            assert st.state == native.REQ_DONE, (st.state, st.message, reqs[i])
+            lat.append(st.finish_s - st.submit_s)
+            fin.append(st.finish_s)
+            sub.append(st.submit_s)
+        stats = srv.stats()
+        srv.stop()
+        span = max(fin) - min(sub)
+        work = sum(int(np.prod(sh)) * f * st for sh, f, _, _, st, _ in reqs)
+        return {"rate_offered": rate, "requests": n, "solves_per_s": n / span, "p50_s": float(np.percentile(lat, 50)),
+                "p99_s": float(np.percentile(lat, 99)), "span_s": span, "value_updates_per_s": work / span,
+                "rounds": int(stats.rounds), "arrival_window_s": float(arrivals[-1])}, reqs
+
+    offered, reqs = one_run(200.0, args.serve_requests, 5)
+    sustained, _ = one_run(max(1.0, 0.7 * offered["solves_per_s"]), max(50, args.serve_requests // 2), 6)
+    # one-at-a-time FP64 plain: per-kind FP64 value-update rates, measured on representative grids
+    kinds = {"ch2": ((512, 512), 1, "ch", dict(dt=0.005)), "ch3": ((144, 144, 144), 1, "ch", dict(dt=0.002)),
+             "ac": ((80, 80, 80), 10, "ac", dict(dt=0.05, kappa=2.0, gamma=1.5))}
+    rate64 = {}
+    for k, (sh, f, m, p) in kinds.items():
+        d = native.make_desc(sh, f, np.float64, m, **p)
+        with native.Stepper(d) as s:
+            s.upload(make_state(sh, f, 1).astype(np.float64))
+            s.step(10)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.step(50)
+            s.synchronize()
+            rate64[k] = int(np.prod(sh)) * f * 50 / (time.perf_counter() - t0)
+    t64 = 0.0
+    for sh, f, m, p, st, _ in reqs:
+        k = "ac" if m == "ac" else ("ch3" if len(sh) == 3 else "ch2")
+        t64 += int(np.prod(sh)) * f * st / rate64[k]
+    seq64 = len(reqs) / t64
+    line = {
+        "metric": "served solves/s and p50/p99 latency (mixed CH/AC requests, Poisson arrivals)",
+        "value": offered["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": offered["span_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded request mix and states)",
+        "config": {"workload": "serve_mix_f32", "offered_rate": 200.0, "requests": args.serve_requests},
+        "offered": offered, "sustainable": sustained,
+        "sequential_f64_estimate": {"solves_per_s": seq64, "value_updates_per_s_by_kind": rate64},
+        "speedup_vs_sequential_f64": offered["solves_per_s"] / seq64,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 CASES = {
     # name: (shape, fields, dtype, model, params)
     "ch3d_f32": (SHAPE, 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
@@ -463,7 +577,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--case", choices=sorted(CASES), help="run one workload untimed (for ncu)")
     ap.add_argument("--case-steps", type=int, default=5)
-    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "batch"])
+    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "batch", "serve"])
+    ap.add_argument("--serve-requests", type=int, default=300)
     args = ap.parse_args()
     if args.case:
         return run_case(args.case, args.case_steps)
@@ -471,6 +586,8 @@ def main():
         if args.warmup < 3:
             args.warmup = 3
         return run_batch(args)
+    if args.workload == "serve" and args.impl != "reference":
+        return run_serve(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -215,6 +215,68 @@ int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force);
 int mmsp_gpu_batch_get_info(const mmsp_gpu_batch* b, mmsp_gpu_batch_info* info);
 const char* mmsp_gpu_batch_last_error(const mmsp_gpu_batch* b);
 
+/* ---------------------------------------------------------------------------
+ * Serving form: a request loop for mixed solves.  The reference has no
+ * counterpart (its driver runs one grid per process, MMSP.main.hpp:273-350).
+ *
+ * Clients submit (descriptor, initial state, steps) from any thread.  A
+ * scheduler thread admits queued requests in arrival order while their
+ * device footprint (mmsp_gpu_footprint) fits the HBM budget, keeps admitted
+ * state on the device, and advances every admitted request by up to
+ * chunk_steps steps per round on its own stream, so requests overlap on the
+ * GPU.  New requests join at round boundaries; finished ones are reduced
+ * (mass, energy), copied to the host and their device memory freed at once.
+ * Each request runs the same kernels with the same step sequence as a lone
+ * mmsp_gpu_update, so its result does not depend on what else is running. */
+typedef struct mmsp_gpu_server mmsp_gpu_server;
+
+typedef struct mmsp_gpu_server_config {
+    size_t hbm_budget_bytes;   /* device bytes for request state (0: 80% of free memory) */
+    int chunk_steps;           /* steps per round (0: 200) */
+    int max_active;            /* requests resident at once (0: no limit but the budget) */
+} mmsp_gpu_server_config;
+
+/* Request states. */
+#define MMSP_GPU_REQ_QUEUED  0
+#define MMSP_GPU_REQ_RUNNING 1
+#define MMSP_GPU_REQ_DONE    2   /* negative values: the request failed with that status */
+
+typedef struct mmsp_gpu_request_status {
+    int state;                 /* MMSP_GPU_REQ_* or a negative MMSP_GPU_E* code */
+    int steps_total;
+    int64_t steps_done;
+    double submit_s, admit_s, finish_s;   /* seconds since the server started */
+    double mass, energy;       /* of the result (state DONE) */
+    char message[160];         /* what failed, for a negative state */
+} mmsp_gpu_request_status;
+
+typedef struct mmsp_gpu_server_stats {
+    int64_t submitted, admitted, completed, failed, cancelled;
+    int queued, active;
+    size_t device_bytes_in_use, device_bytes_budget;
+    int64_t rounds;
+} mmsp_gpu_server_stats;
+
+int mmsp_gpu_server_start(mmsp_gpu_server** out, const mmsp_gpu_server_config* cfg);
+/* Queue a request; `host` is copied before the call returns.  A request whose
+ * footprint exceeds the whole budget is refused with MMSP_GPU_ENOMEM. */
+int mmsp_gpu_server_submit(mmsp_gpu_server* s, const mmsp_gpu_desc* desc, const void* host, size_t bytes,
+                           int layout, int steps, uint64_t* request_id);
+/* Status without blocking; MMSP_GPU_ENOTFOUND for an unknown or fetched id. */
+int mmsp_gpu_server_poll(mmsp_gpu_server* s, uint64_t request_id, mmsp_gpu_request_status* status);
+/* Block until the request is done or failed, or `timeout_s` passes
+ * (MMSP_GPU_ETIMEDOUT; the request keeps running). */
+int mmsp_gpu_server_wait(mmsp_gpu_server* s, uint64_t request_id, double timeout_s,
+                         mmsp_gpu_request_status* status);
+/* Copy a finished request's state to `host` and forget the request. */
+int mmsp_gpu_server_fetch(mmsp_gpu_server* s, uint64_t request_id, void* host, size_t bytes, int layout);
+/* Cancel a queued or running request (it ends with MMSP_GPU_ECANCELED). */
+int mmsp_gpu_server_cancel(mmsp_gpu_server* s, uint64_t request_id);
+int mmsp_gpu_server_get_stats(mmsp_gpu_server* s, mmsp_gpu_server_stats* stats);
+/* Stop the scheduler; requests not finished end with MMSP_GPU_ESTOPPED.
+ * Frees all device memory and the server. */
+int mmsp_gpu_server_stop(mmsp_gpu_server* s);
+
 /* Largest state (bytes) mmsp_gpu_step_noalloc can advance by more than one
  * step or in place: the size of the library's fixed device scratch array. */
 #define MMSP_GPU_NOALLOC_MAX_BYTES (16u << 20)

@@ -1,0 +1,369 @@
+// mmsp_gpu_server.cu -- the serving form (mmsp_gpu_server_*): a continuous
+// batching request loop over the single-grid handles.
+//
+// One scheduler thread owns the device work.  Each round it (1) admits
+// queued requests in arrival order while their footprint fits the HBM
+// budget, creating a handle and uploading the initial state, (2) queues up
+// to chunk_steps steps for every admitted request, each on its handle's own
+// stream so they run concurrently, and (3) waits for the round, retiring
+// requests that reached their step count: their mass and energy are
+// reduced, the state is copied to a host buffer and the handle's device
+// memory is freed before the next admission.  Clients only touch host
+// structures under the mutex.
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include <stdio.h>
+#include <string.h>
+
+#include "MMSP.gpu.h"
+#include "pf_internal.h"
+
+namespace {
+
+struct Request {
+    uint64_t id = 0;
+    mmsp_gpu_desc d;
+    int layout = MMSP_GPU_CELL_MAJOR;
+    int steps = 0;
+    std::atomic<int64_t> done{0};
+    std::vector<unsigned char> host;   // initial state, then the result
+    size_t footprint = 0;
+    mmsp_gpu_handle* h = nullptr;
+    int state = MMSP_GPU_REQ_QUEUED;
+    std::atomic<bool> cancel{false};
+    int chunk = 0;                     // steps queued in the current round
+    double submit_s = 0, admit_s = 0, finish_s = 0, mass = 0, energy = 0;
+    char message[160] = {0};
+};
+
+// Keep the handle's message of a failed call.
+static int note(Request* r, int rc, const char* what)
+{
+    if (rc && !r->message[0])
+        snprintf(r->message, sizeof(r->message), "%s: %s", what, r->h ? mmsp_gpu_last_error(r->h) : mmsp_gpu_strerror(rc));
+    return rc;
+}
+
+using Clock = std::chrono::steady_clock;
+
+}  // namespace
+
+struct mmsp_gpu_server {
+    int device = 0;
+    size_t budget = 0, in_use = 0;
+    int chunk = 200, max_active = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request*> queue;
+    std::vector<Request*> active;
+    std::unordered_map<uint64_t, Request*> all;
+    uint64_t next_id = 1;
+    bool stopping = false;
+    std::thread th;
+    Clock::time_point t0;
+    mmsp_gpu_server_stats st;
+};
+
+static double since(const mmsp_gpu_server* s) { return std::chrono::duration<double>(Clock::now() - s->t0).count(); }
+
+// Called with s->mu held.
+static void finish(mmsp_gpu_server* s, Request* r, int state)
+{
+    r->state = state;
+    r->finish_s = since(s);
+    if (state == MMSP_GPU_REQ_DONE) s->st.completed++;
+    else if (state == MMSP_GPU_ECANCELED) s->st.cancelled++;
+    else s->st.failed++;
+    s->cv_done.notify_all();
+}
+
+static void release_request(mmsp_gpu_server* s, Request* r)
+{
+    if (r->h) {
+        mmsp_gpu_destroy(r->h);
+        r->h = nullptr;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->in_use -= r->footprint;
+}
+
+static void scheduler(mmsp_gpu_server* s)
+{
+    cudaSetDevice(s->device);
+    std::vector<Request*> admitted;
+    while (true) {
+        admitted.clear();
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv_work.wait(lock, [&] { return s->stopping || !s->queue.empty() || !s->active.empty(); });
+            if (s->stopping) break;
+            while (!s->queue.empty()) {
+                Request* r = s->queue.front();
+                if (r->cancel) {
+                    s->queue.pop_front();
+                    finish(s, r, MMSP_GPU_ECANCELED);
+                    continue;
+                }
+                if (s->max_active > 0 && (int)(s->active.size() + admitted.size()) >= s->max_active) break;
+                if (s->in_use + r->footprint > s->budget) break;   // arrival order: wait for memory
+                s->queue.pop_front();
+                s->in_use += r->footprint;
+                admitted.push_back(r);
+            }
+        }
+        // admission: device state for the newly admitted requests
+        for (Request* r : admitted) {
+            int rc = note(r, mmsp_gpu_create(&r->h, &r->d), "create");
+            if (!rc) rc = note(r, mmsp_gpu_upload(r->h, r->host.data(), r->host.size(), r->layout), "upload");
+            std::lock_guard<std::mutex> lock(s->mu);
+            if (rc) {
+                if (r->h) mmsp_gpu_destroy(r->h);
+                r->h = nullptr;
+                s->in_use -= r->footprint;
+                finish(s, r, rc);
+                continue;
+            }
+            r->state = MMSP_GPU_REQ_RUNNING;
+            r->admit_s = since(s);
+            s->st.admitted++;
+            s->active.push_back(r);
+        }
+        std::vector<Request*> round;
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            round = s->active;
+            s->st.rounds++;
+        }
+        // one round: every active request advances up to `chunk` steps on its own stream
+        for (Request* r : round) {
+            r->chunk = (int)std::min<int64_t>(s->chunk, r->steps - r->done);
+            if (r->cancel || r->chunk <= 0) r->chunk = 0;
+            else if (note(r, mmsp_gpu_step(r->h, r->chunk), "step")) r->chunk = -1;
+        }
+        for (Request* r : round) {
+            int rc = (r->chunk < 0) ? MMSP_GPU_ECUDA : note(r, mmsp_gpu_synchronize(r->h), "synchronize");
+            if (r->chunk > 0 && !rc) r->done += r->chunk;
+            int end_state = 0;
+            bool end = false;
+            if (rc) {
+                end = true;
+                end_state = rc;
+            } else if (r->cancel) {
+                end = true;
+                end_state = MMSP_GPU_ECANCELED;
+            } else if (r->done >= r->steps) {
+                mmsp_gpu_stats stt;
+                rc = note(r, mmsp_gpu_reduce(r->h, &stt), "reduce");
+                if (!rc) rc = note(r, mmsp_gpu_download(r->h, r->host.data(), r->host.size(), r->layout), "download");
+                r->mass = stt.mass;
+                r->energy = stt.energy;
+                end = true;
+                end_state = rc ? rc : MMSP_GPU_REQ_DONE;
+            }
+            if (end) {
+                release_request(s, r);
+                std::lock_guard<std::mutex> lock(s->mu);
+                for (size_t i = 0; i < s->active.size(); i++)
+                    if (s->active[i] == r) {
+                        s->active.erase(s->active.begin() + i);
+                        break;
+                    }
+                finish(s, r, end_state);
+            }
+        }
+    }
+    // stopping: everything not finished ends with ESTOPPED
+    std::lock_guard<std::mutex> lock(s->mu);
+    for (Request* r : s->active) {
+        if (r->h) mmsp_gpu_destroy(r->h);
+        r->h = nullptr;
+        s->in_use -= r->footprint;
+        finish(s, r, MMSP_GPU_ESTOPPED);
+    }
+    s->active.clear();
+    for (Request* r : s->queue) finish(s, r, MMSP_GPU_ESTOPPED);
+    s->queue.clear();
+}
+
+static void fill_status(const Request* r, mmsp_gpu_request_status* st)
+{
+    st->state = r->state;
+    st->steps_total = r->steps;
+    st->steps_done = r->done.load();
+    st->submit_s = r->submit_s;
+    st->admit_s = r->admit_s;
+    st->finish_s = r->finish_s;
+    st->mass = r->mass;
+    st->energy = r->energy;
+    memcpy(st->message, r->message, sizeof(st->message));
+}
+
+static bool finished(const Request* r) { return r->state == MMSP_GPU_REQ_DONE || r->state < 0; }
+
+extern "C" int mmsp_gpu_server_start(mmsp_gpu_server** out, const mmsp_gpu_server_config* cfg)
+{
+    if (!out) return MMSP_GPU_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return MMSP_GPU_ENODEV;
+    }
+    mmsp_gpu_server* s = new (std::nothrow) mmsp_gpu_server();
+    if (!s) return MMSP_GPU_ENOMEM;
+    memset(&s->st, 0, sizeof(s->st));
+    cudaGetDevice(&s->device);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        delete s;
+        return MMSP_GPU_ECUDA;
+    }
+    s->budget = (cfg && cfg->hbm_budget_bytes) ? cfg->hbm_budget_bytes : (size_t)(0.8 * (double)free_b);
+    if (s->budget > free_b) s->budget = free_b;
+    if (cfg && cfg->chunk_steps > 0) s->chunk = cfg->chunk_steps;
+    if (cfg && cfg->max_active > 0) s->max_active = cfg->max_active;
+    s->st.device_bytes_budget = s->budget;
+    s->t0 = Clock::now();
+    try {
+        s->th = std::thread(scheduler, s);
+    } catch (...) {
+        delete s;
+        return MMSP_GPU_ENOMEM;
+    }
+    *out = s;
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_server_submit(mmsp_gpu_server* s, const mmsp_gpu_desc* desc, const void* host, size_t bytes,
+                                      int layout, int steps, uint64_t* id)
+{
+    if (!s || !desc || !host || steps < 0 || !id) return MMSP_GPU_EINVAL;
+    if (layout != MMSP_GPU_CELL_MAJOR && layout != MMSP_GPU_FIELD_MAJOR) return MMSP_GPU_EINVAL;
+    size_t fp = 0;
+    int rc = mmsp_gpu_footprint(desc, &fp);
+    if (rc) return rc;
+    size_t want = (size_t)desc->fields * (desc->dtype == MMSP_GPU_F64 ? 8 : 4);
+    for (int a = 0; a < desc->dim; a++) want *= (size_t)desc->n[a];
+    if (bytes != want) return MMSP_GPU_EINVAL;
+    Request* r = new (std::nothrow) Request();
+    if (!r) return MMSP_GPU_ENOMEM;
+    r->d = *desc;
+    r->layout = layout;
+    r->steps = steps;
+    r->footprint = fp;
+    try {
+        r->host.assign((const unsigned char*)host, (const unsigned char*)host + bytes);
+    } catch (...) {
+        delete r;
+        return MMSP_GPU_ENOMEM;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (s->stopping) {
+        delete r;
+        return MMSP_GPU_ESTOPPED;
+    }
+    if (fp > s->budget) {
+        delete r;
+        return MMSP_GPU_ENOMEM;   // could never be admitted
+    }
+    r->id = s->next_id++;
+    r->submit_s = since(s);
+    s->all[r->id] = r;
+    s->queue.push_back(r);
+    s->st.submitted++;
+    *id = r->id;
+    s->cv_work.notify_one();
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_server_poll(mmsp_gpu_server* s, uint64_t id, mmsp_gpu_request_status* st)
+{
+    if (!s || !st) return MMSP_GPU_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return MMSP_GPU_ENOTFOUND;
+    fill_status(it->second, st);
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_server_wait(mmsp_gpu_server* s, uint64_t id, double timeout_s, mmsp_gpu_request_status* st)
+{
+    if (!s) return MMSP_GPU_EINVAL;
+    std::unique_lock<std::mutex> lock(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return MMSP_GPU_ENOTFOUND;
+    Request* r = it->second;
+    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                             std::chrono::duration<double>(timeout_s < 0 ? 0 : timeout_s));
+    bool ok = s->cv_done.wait_until(lock, deadline, [&] { return finished(r); });
+    if (st) fill_status(r, st);
+    return ok ? MMSP_GPU_OK : MMSP_GPU_ETIMEDOUT;
+}
+
+extern "C" int mmsp_gpu_server_fetch(mmsp_gpu_server* s, uint64_t id, void* host, size_t bytes, int layout)
+{
+    if (!s || !host) return MMSP_GPU_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return MMSP_GPU_ENOTFOUND;
+    Request* r = it->second;
+    if (!finished(r)) return MMSP_GPU_EINVAL;
+    if (r->state != MMSP_GPU_REQ_DONE) {
+        int code = r->state;
+        s->all.erase(it);
+        delete r;
+        return code;
+    }
+    if (bytes != r->host.size() || layout != r->layout) return MMSP_GPU_EINVAL;
+    memcpy(host, r->host.data(), bytes);
+    s->all.erase(it);
+    delete r;
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_server_cancel(mmsp_gpu_server* s, uint64_t id)
+{
+    if (!s) return MMSP_GPU_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return MMSP_GPU_ENOTFOUND;
+    it->second->cancel = true;
+    s->cv_work.notify_one();
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_server_get_stats(mmsp_gpu_server* s, mmsp_gpu_server_stats* st)
+{
+    if (!s || !st) return MMSP_GPU_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    *st = s->st;
+    st->queued = (int)s->queue.size();
+    st->active = (int)s->active.size();
+    st->device_bytes_in_use = s->in_use;
+    st->device_bytes_budget = s->budget;
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_server_stop(mmsp_gpu_server* s)
+{
+    if (!s) return MMSP_GPU_OK;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stopping = true;
+        s->cv_work.notify_all();
+    }
+    if (s->th.joinable()) s->th.join();
+    for (auto& kv : s->all) delete kv.second;
+    s->all.clear();
+    delete s;
+    return MMSP_GPU_OK;
+}

@@ -147,7 +147,7 @@ cudaError_t plan_ac(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     }
     p->fn = dbl ? ac_pick<double>(g.dim, d.model, ty, c.unit_w) : ac_pick<float>(g.dim, d.model, ty, c.unit_w);
     p->block = dim3(kTZ, kThreadsY, 1);
-    cudaError_t e = cudaFuncSetAttribute(p->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+    cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e != cudaSuccess) return e;
     int tz = (g.Z + kTZ - 1) / kTZ, tyn = (g.Y + ty - 1) / ty;
     int segs = 1;

@@ -1,6 +1,9 @@
 // pf_aux.cu -- geometry/coefficients, FP64 compensated reductions, layout transposes.
 #include <math.h>
 
+#include <map>
+#include <mutex>
+
 #include "pf_device.cuh"
 #include "pf_internal.h"
 
@@ -16,6 +19,18 @@ int sm_count()
         n = v;
     }
     return n;
+}
+
+cudaError_t ensure_smem(const void* fn, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<const void*, size_t> set;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = set[fn];
+    if (bytes <= cur) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
 }
 
 Geom make_geom(const mmsp_gpu_desc& d)

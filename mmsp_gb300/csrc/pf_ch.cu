@@ -181,7 +181,7 @@ cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     int segs = 1;
     p->planes = 1;
     if (g.dim == 3) {
-        cudaError_t e = cudaFuncSetAttribute(p->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+        cudaError_t e = ensure_smem(p->fn, p->smem);
         if (e != cudaSuccess) return e;
         int per_sm = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, 256, p->smem);
@@ -198,7 +198,7 @@ cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
         p->planes = (g.X + segs - 1) / segs;
         segs = (g.X + p->planes - 1) / p->planes;
     } else {
-        cudaError_t e = cudaFuncSetAttribute(p->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+        cudaError_t e = ensure_smem(p->fn, p->smem);
         if (e != cudaSuccess) return e;
     }
     p->grid = dim3(tz, tyn, segs);

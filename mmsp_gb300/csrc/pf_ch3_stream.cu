@@ -329,7 +329,7 @@ cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     p->fn = pick_stream(g.Z, d.model == MMSP_GPU_CH, c.unit_w);
     p->smem = ch3_smem(kStreamR, g.Z, V);
     p->block = dim3(threads, 1, 1);
-    cudaError_t e = cudaFuncSetAttribute(p->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+    cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, threads, p->smem);

@@ -34,6 +34,10 @@ struct Coeffs {
 
 Geom make_geom(const mmsp_gpu_desc& d);
 int sm_count();                 // SMs of the current device
+// Allow `fn` at least `bytes` of dynamic shared memory.  The attribute is
+// process-wide per kernel, so it is only ever raised: lowering it for one
+// plan would break launches of another plan of the same kernel.
+cudaError_t ensure_smem(const void* fn, size_t bytes);
 Coeffs make_coeffs(const mmsp_gpu_desc& d);
 
 // A prepared launch of one explicit step.

@@ -33,7 +33,10 @@ EXPORTS = [
     "mmsp_gpu_batch_create", "mmsp_gpu_batch_destroy", "mmsp_gpu_batch_set_stream", "mmsp_gpu_batch_upload",
     "mmsp_gpu_batch_download", "mmsp_gpu_batch_step", "mmsp_gpu_batch_synchronize", "mmsp_gpu_batch_reduce",
     "mmsp_gpu_batch_tune", "mmsp_gpu_batch_get_info", "mmsp_gpu_batch_last_error",
+    "mmsp_gpu_server_start", "mmsp_gpu_server_submit", "mmsp_gpu_server_poll", "mmsp_gpu_server_wait",
+    "mmsp_gpu_server_fetch", "mmsp_gpu_server_cancel", "mmsp_gpu_server_get_stats", "mmsp_gpu_server_stop",
 ]
+REQ_QUEUED, REQ_RUNNING, REQ_DONE = 0, 1, 2
 NOALLOC_MAX_BYTES = 16 << 20   # MMSP_GPU_NOALLOC_MAX_BYTES
 
 
@@ -55,6 +58,23 @@ class BatchInfo(ctypes.Structure):
                 ("rows_per_item", ctypes.c_int), ("threads_per_block", ctypes.c_int), ("blocks", ctypes.c_int),
                 ("items", ctypes.c_int), ("tuned_from_cache", ctypes.c_int), ("tune_ms", ctypes.c_double),
                 ("device_bytes", ctypes.c_size_t)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("chunk_steps", ctypes.c_int), ("max_active", ctypes.c_int)]
+
+
+class RequestStatus(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("steps_total", ctypes.c_int), ("steps_done", ctypes.c_int64),
+                ("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("finish_s", ctypes.c_double),
+                ("mass", ctypes.c_double), ("energy", ctypes.c_double), ("message", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("admitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("failed", ctypes.c_int64), ("cancelled", ctypes.c_int64), ("queued", ctypes.c_int),
+                ("active", ctypes.c_int), ("device_bytes_in_use", ctypes.c_size_t),
+                ("device_bytes_budget", ctypes.c_size_t), ("rounds", ctypes.c_int64)]
 
 
 class GpuError(RuntimeError):
@@ -114,6 +134,14 @@ def load(build_if_missing: bool = False):
         "mmsp_gpu_batch_tune": (i, [vp, i]),
         "mmsp_gpu_batch_get_info": (i, [vp, ctypes.POINTER(BatchInfo)]),
         "mmsp_gpu_batch_last_error": (ctypes.c_char_p, [vp]),
+        "mmsp_gpu_server_start": (i, [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig)]),
+        "mmsp_gpu_server_submit": (i, [vp, dp, vp, sz, i, i, ctypes.POINTER(ctypes.c_uint64)]),
+        "mmsp_gpu_server_poll": (i, [vp, ctypes.c_uint64, ctypes.POINTER(RequestStatus)]),
+        "mmsp_gpu_server_wait": (i, [vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(RequestStatus)]),
+        "mmsp_gpu_server_fetch": (i, [vp, ctypes.c_uint64, vp, sz, i]),
+        "mmsp_gpu_server_cancel": (i, [vp, ctypes.c_uint64]),
+        "mmsp_gpu_server_get_stats": (i, [vp, ctypes.POINTER(ServerStats)]),
+        "mmsp_gpu_server_stop": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -327,3 +355,68 @@ class Batch:
         inf = BatchInfo()
         _bcheck(self.L.mmsp_gpu_batch_get_info(self.b, ctypes.byref(inf)), self.b, "info")
         return inf
+
+
+class Server:
+    """The request loop (mmsp_gpu_server_*)."""
+
+    def __init__(self, budget_bytes: int = 0, chunk_steps: int = 0, max_active: int = 0):
+        self.L = load()
+        cfg = ServerConfig(budget_bytes, chunk_steps, max_active)
+        s = ctypes.c_void_p()
+        _check(self.L.mmsp_gpu_server_start(ctypes.byref(s), ctypes.byref(cfg)), None, "server_start")
+        self.s = s
+        self.shapes = {}
+
+    def submit(self, desc: Desc, arr: np.ndarray, steps: int) -> int:
+        dt = np.float64 if desc.dtype == F64 else np.float32
+        a = np.ascontiguousarray(arr, dtype=dt)
+        rid = ctypes.c_uint64()
+        _check(self.L.mmsp_gpu_server_submit(self.s, ctypes.byref(desc), a.ctypes.data, a.nbytes, CELL_MAJOR,
+                                             int(steps), ctypes.byref(rid)), None, "submit")
+        self.shapes[rid.value] = (a.shape, dt)
+        return rid.value
+
+    def poll(self, rid: int) -> RequestStatus:
+        st = RequestStatus()
+        _check(self.L.mmsp_gpu_server_poll(self.s, rid, ctypes.byref(st)), None, "poll")
+        return st
+
+    def wait(self, rid: int, timeout: float = 600.0) -> RequestStatus:
+        st = RequestStatus()
+        rc = self.L.mmsp_gpu_server_wait(self.s, rid, float(timeout), ctypes.byref(st))
+        if rc not in (OK, ETIMEDOUT):
+            _check(rc, None, "wait")
+        return st
+
+    def fetch(self, rid: int) -> np.ndarray:
+        shape, dt = self.shapes[rid]
+        out = np.empty(shape, dtype=dt)
+        _check(self.L.mmsp_gpu_server_fetch(self.s, rid, out.ctypes.data, out.nbytes, CELL_MAJOR), None, "fetch")
+        del self.shapes[rid]
+        return out
+
+    def cancel(self, rid: int):
+        _check(self.L.mmsp_gpu_server_cancel(self.s, rid), None, "cancel")
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(self.L.mmsp_gpu_server_get_stats(self.s, ctypes.byref(st)), None, "stats")
+        return st
+
+    def stop(self):
+        if getattr(self, "s", None):
+            self.L.mmsp_gpu_server_stop(self.s)
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.stop()

@@ -94,3 +94,26 @@ def test_null_arguments_are_rejected(lib):
     assert lib.mmsp_gpu_step(None, 1) == native.EINVAL
     assert lib.mmsp_gpu_reduce(None, None) == native.EINVAL
     assert lib.mmsp_gpu_last_error(None) == b"NULL handle"
+
+
+def test_batch_and_server_refuse_without_a_device(lib):
+    """On a machine with no CUDA device the batched and serving entry points
+    return MMSP_GPU_ENODEV instead of failing later."""
+    import ctypes
+
+    from mmsp_gb300 import native
+
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a CUDA device is present")
+    except ImportError:
+        pass
+    d = native.make_desc((32, 32), 1, np.float32, "ch")
+    arr = (native.Desc * 1)(d)
+    b = ctypes.c_void_p()
+    assert lib.mmsp_gpu_batch_create(ctypes.byref(b), 1, arr) == native.ENODEV
+    s = ctypes.c_void_p()
+    cfg = native.ServerConfig(0, 0, 0)
+    assert lib.mmsp_gpu_server_start(ctypes.byref(s), ctypes.byref(cfg)) == native.ENODEV
+    assert lib.mmsp_gpu_batch_create(ctypes.byref(b), 0, arr) == native.EINVAL

@@ -299,3 +299,23 @@ def test_fp32_stream_kernel_against_fp64_oracle(gpu, oracle, shape, model):
     assert np.abs(got - want).max() <= TOL_F32 * max(1.0, np.abs(want).max())
     # the state must move, or the comparison pins nothing
     assert np.abs(want - c0).max() > 1e-4
+
+
+def test_handles_of_one_kernel_with_different_shared_memory(gpu, oracle):
+    """Two live handles that use the same kernel with different shared-memory
+    needs (16 and 3 fields): planning the second must not break the first."""
+    from mmsp_gb300 import inputs
+
+    big = inputs.voronoi_grains((10, 11, 12), 7, 16, 61)
+    small = inputs.voronoi_grains((10, 11, 12), 7, 3, 62)
+    d_big = gpu.make_desc(big.shape[:-1], 16, np.float64, "ac", gamma=1.5, kappa=2.0, dt=0.05)
+    d_small = gpu.make_desc(small.shape[:-1], 3, np.float64, "ac", gamma=1.5, kappa=2.0, dt=0.05)
+    with gpu.Stepper(d_big) as a:
+        a.upload(big)
+        with gpu.Stepper(d_small) as b:
+            b.upload(small)
+            a.step(4)
+            b.step(4)
+            got_a, got_b = a.download(), b.download()
+    assert np.array_equal(got_a, oracle.ac_baseline(big, 4, 1.5, 2.0, 1.0, 0.05))
+    assert np.array_equal(got_b, oracle.ac_baseline(small, 4, 1.5, 2.0, 1.0, 0.05))
