@@ -296,7 +296,7 @@ def run_gpu(args):
     alg_bytes = cells * 2 * 4                     # one read + one write of the FP32 state per step
     launch_s = ms_step / 1e3 / SOLVE_STEPS
     achieved = alg_bytes / launch_s / 1e9
-    traffic = profile_traffic("ch_step_kernel_f32_3d_256")
+    traffic = profile_traffic("ch3_stream_f32_256")
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -306,7 +306,7 @@ def run_gpu(args):
                    "l2": "flushed (256 MiB write) before every timed solve; FP32 working set 134 MB"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "ch_step_kernel<float,3,CH>", "peak_source": peak_kind,
+                     "kernel": "ch3_stream_f32<8,256,2,CH,unit>", "peak_source": peak_kind,
                      "alg_bytes_per_launch": alg_bytes},
         "e2e": {"value": e2e_val, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes32,
                 "d2h_bytes_per_step": nbytes32 + 16, "ms_per_step": e2e_s * 1e3},
@@ -553,6 +553,18 @@ def run_case(name: str, steps: int):
     the ncu summaries under profiles/ are captured from."""
     from mmsp_gb300 import inputs, native
 
+    if name == "batch_f32":
+        work = inputs.batched_cahn_hilliard(count=256, seed=4)
+        descs = [native.make_desc(c0.shape, 1, np.float32, "ch", kappa=k, mobility=1.0, dt=0.005) for c0, k in work]
+        with native.Batch(descs) as b:
+            for i, (c0, _) in enumerate(work):
+                b.upload(i, c0.astype(np.float32))
+            b.tune()          # 10 candidates x 4 launches before the measured steps
+            b.step(steps)
+            b.synchronize()
+            inf = b.info()
+        print("case batch_f32: %d steps, rows/item %d, threads %d" % (steps, inf.rows_per_item, inf.threads_per_block))
+        return 0
     shape, fields, dtype, model, params = CASES[name]
     if fields == 1:
         x = inputs.noisy_composition(shape, MEAN, AMP, SEED)
@@ -575,7 +587,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--case", choices=sorted(CASES), help="run one workload untimed (for ncu)")
+    ap.add_argument("--case", choices=sorted(CASES) + ["batch_f32"], help="run one workload untimed (for ncu)")
     ap.add_argument("--case-steps", type=int, default=5)
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "batch", "serve"])
     ap.add_argument("--serve-requests", type=int, default=300)

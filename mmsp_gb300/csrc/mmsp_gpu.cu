@@ -329,7 +329,7 @@ static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s)
     const void* in = h->buf[h->cur];
     void* out = h->buf[h->cur ^ 1];
     cudaError_t e = ch ? pf::launch_ch(h->plan, h->d, h->g, h->c, in, out, h->flags, s)
-                       : pf::launch_ac(h->plan, h->d, h->g, h->c, in, out, s);
+                       : pf::launch_ac(h->plan, h->d, h->g, h->c, in, out, h->flags, s);
     h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913
     return e;
 }

@@ -330,7 +330,7 @@ static cudaError_t step_once(mmsp_gpu_batch* b, cudaStream_t s, int in, int out)
         void* dst = (char*)b->pool[out] + mm.off * b->esize;
         const bool ch = mm.d.model == MMSP_GPU_CH || mm.d.model == MMSP_GPU_CH_POLY;
         e = ch ? launch_ch(mm.plan, mm.d, mm.g, mm.c, src, dst, b->counters + 2, s)
-               : launch_ac(mm.plan, mm.d, mm.g, mm.c, src, dst, s);
+               : launch_ac(mm.plan, mm.d, mm.g, mm.c, src, dst, b->counters + 2, s);
     }
     return e;
 }

@@ -107,7 +107,7 @@ extern "C" int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, 
         void* dst;
         if (in_place) dst = ((k & 1) == 1) ? scratch : out;
         else dst = ((steps - k) & 1) == 0 ? out : scratch;
-        e = ch ? pf::launch_ch(plan, d, g, c, src, dst, flag, s) : pf::launch_ac(plan, d, g, c, src, dst, s);
+        e = ch ? pf::launch_ch(plan, d, g, c, src, dst, flag, s) : pf::launch_ac(plan, d, g, c, src, dst, flag, s);
         src = dst;
     }
     if (e == cudaSuccess && src != out) e = cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToDevice, s);

@@ -135,6 +135,7 @@ static const void* ac_pick(int dim, int model, int ty, bool unit)
 
 cudaError_t plan_ac(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
+    if (ac3_stream_eligible(d, g)) return plan_ac3_stream(d, g, p);
     Coeffs c = make_coeffs(d);
     bool dbl = d.dtype == MMSP_GPU_F64;
     size_t es = dbl ? sizeof(double) : sizeof(float);
@@ -174,8 +175,9 @@ cudaError_t plan_ac(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 }
 
 cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
-                      const void* in, void* out, cudaStream_t s)
+                      const void* in, void* out, int* err, cudaStream_t s)
 {
+    if (p.kind == 2) return launch_ac3_stream(p, g, c, in, out, err, s);
     int planes = p.planes, n = d.fields;
     if (d.dtype == MMSP_GPU_F64) {
         P<double> q = narrow<double>(c, g.dim);

@@ -72,11 +72,29 @@ static __device__ __forceinline__ T lap2(const T (&lo)[V], const T (&ce)[V], con
 {
     using A = Ar<T>;
     const T y = ce[j];
-    const T y2 = A::mul(T(2), y);
-    T lap = lap_axis<T, UNIT>(T(0), hi[j], y2, lo[j], w0);
     const T zl = j == 0 ? left : ce[j - 1];
     const T zh = j == V - 1 ? right : ce[j + 1];
-    return lap_axis<T, UNIT>(lap, zh, y2, zl, w1);
+    if constexpr (sizeof(T) == 4) {
+        // precision form: neighbour sums, one multiply-add per axis
+        if (UNIT) return fmaf(-4.0f, y, (hi[j] + lo[j]) + (zh + zl));
+        return fmaf(w0, hi[j] + lo[j], fmaf(w1, zh + zl, -2.0f * (w0 + w1) * y));
+    } else {
+        const T y2 = A::mul(T(2), y);
+        T lap = lap_axis<T, UNIT>(T(0), hi[j], y2, lo[j], w0);
+        return lap_axis<T, UNIT>(lap, zh, y2, zl, w1);
+    }
+}
+
+// mu of the Cahn-Hilliard models; Horner's form in the precision form.
+template <typename T, int MODEL>
+static __device__ __forceinline__ T mu2(T c, T lap, const P<T>& p)
+{
+    if constexpr (sizeof(T) == 4) {
+        const float fp = MODEL == MMSP_GPU_CH ? c * fmaf(fmaf(4.0f, c, -6.0f), c, 2.0f) : c * fmaf(p.u, c * c, p.neg_r);
+        return fmaf(-p.kappa, lap, fp);
+    } else {
+        return ch_mu<T, MODEL>(c, lap, p);
+    }
 }
 
 template <typename T, int V, int MODEL, bool UNIT>
@@ -97,43 +115,41 @@ static __device__ void run_rows(const BatchInst& bi, int xs, int xe, const T* __
     const unsigned FULL = 0xffffffffu;
     const int lm = (lane + 31) & 31, lp = (lane + 1) & 31;
 
-    T ca[V], cb[V], cc[V], nx[V];
-    T ma[V], mb[V], mc[V];
-    ld_row<T, V>(ca, base_in + (long long)wrapi(xs - 2, n0) * n1);
-    ld_row<T, V>(cb, base_in + (long long)wrapi(xs - 1, n0) * n1);
+    // c0 = c(x), c1 = c(x+1), c2 = c(x+2); m0 = mu(x-1), m1 = mu(x), m2 = mu(x+1).
+    // The rotation is register moves rather than a three-way unrolled body:
+    // the kernel holds 16 row widths, and a smaller body keeps them in the
+    // instruction cache.
+    T c0[V], c1[V], c2[V], nx[V];
+    T m0[V], m1[V], m2[V];
+    ld_row<T, V>(c0, base_in + (long long)wrapi(xs - 2, n0) * n1);
+    ld_row<T, V>(c1, base_in + (long long)wrapi(xs - 1, n0) * n1);
     ld_row<T, V>(nx, base_in + (long long)wrapi(xs, n0) * n1);
 #pragma unroll
-    for (int j = 0; j < V; j++) ma[j] = mb[j] = T(0);
-
-    // a = c(x), b = c(x+1), c = c(x+2); ma = mu(x-1), mb = mu(x), mc = mu(x+1)
-    auto iter = [&](int x, T (&a)[V], T (&b)[V], T (&c)[V], T (&xa)[V], T (&xb)[V], T (&xc)[V]) {
+    for (int j = 0; j < V; j++) m0[j] = m1[j] = T(0);
+#pragma unroll 1
+    for (int x = xs - 2; x < xe; x++) {
 #pragma unroll
-        for (int j = 0; j < V; j++) c[j] = nx[j];
+        for (int j = 0; j < V; j++) c2[j] = nx[j];
         if (x + 3 <= xe + 1) ld_row<T, V>(nx, base_in + (long long)wrapi(x + 3, n0) * n1);
-        const T bl = __shfl_sync(FULL, b[V - 1], lm);
-        const T br = __shfl_sync(FULL, b[0], lp);
+        const T bl = __shfl_sync(FULL, c1[V - 1], lm);
+        const T br = __shfl_sync(FULL, c1[0], lp);
 #pragma unroll
-        for (int j = 0; j < V; j++) xc[j] = ch_mu<T, MODEL>(b[j], lap2<T, V, UNIT>(a, b, c, bl, br, j, w0, w1), p);
+        for (int j = 0; j < V; j++) m2[j] = mu2<T, MODEL>(c1[j], lap2<T, V, UNIT>(c0, c1, c2, bl, br, j, w0, w1), p);
         if (x >= xs) {
-            const T ml = __shfl_sync(FULL, xb[V - 1], lm);
-            const T mr = __shfl_sync(FULL, xb[0], lp);
+            const T ml = __shfl_sync(FULL, m1[V - 1], lm);
+            const T mr = __shfl_sync(FULL, m1[0], lp);
             T o[V];
 #pragma unroll
-            for (int j = 0; j < V; j++) o[j] = A::add(a[j], A::mul(p.dtm, lap2<T, V, UNIT>(xa, xb, xc, ml, mr, j, w0, w1)));
+            for (int j = 0; j < V; j++) o[j] = A::add(c0[j], A::mul(p.dtm, lap2<T, V, UNIT>(m0, m1, m2, ml, mr, j, w0, w1)));
             st_row<T, V>(base_out + (long long)x * n1, o);
         }
-    };
-    int x = xs - 2;
-    while (true) {
-        if (x >= xe) break;
-        iter(x, ca, cb, cc, ma, mb, mc);
-        x++;
-        if (x >= xe) break;
-        iter(x, cb, cc, ca, mb, mc, ma);
-        x++;
-        if (x >= xe) break;
-        iter(x, cc, ca, cb, mc, ma, mb);
-        x++;
+#pragma unroll
+        for (int j = 0; j < V; j++) {
+            c0[j] = c1[j];
+            c1[j] = c2[j];
+            m0[j] = m1[j];
+            m1[j] = m2[j];
+        }
     }
 }
 

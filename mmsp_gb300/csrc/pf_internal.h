@@ -47,7 +47,8 @@ struct StepPlan {
     size_t smem;
     int planes;        // planes of axis X per block (3D streaming)
     int fields;
-    int kind;          // 0: generic tile kernel, 1: FP32 3D register-streaming kernel
+    int kind;          // 0: generic tile kernel, 1: FP32 3D CH streaming, 2: FP32 3D AC streaming
+    int ring;          // planes in the shared-memory ring (streaming kernels)
     bool ok;
 };
 
@@ -61,12 +62,18 @@ cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c, const void* in, void* out,
                               int* err, cudaStream_t s);
 
+// FP32 3D Allen-Cahn on whole rows (pf_ac3_stream.cu).
+bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g);
+cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
+cudaError_t launch_ac3_stream(const StepPlan& p, const Geom& g, const Coeffs& c, const void* in, void* out,
+                              int* err, cudaStream_t s);
+
 // One step in -> out on `s`.  `err` is a device word a kernel sets when a
 // bounded wait runs out.
 cudaError_t launch_ch(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
                       const void* in, void* out, int* err, cudaStream_t s);
 cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
-                      const void* in, void* out, cudaStream_t s);
+                      const void* in, void* out, int* err, cudaStream_t s);
 
 // Reductions: partial sums of (mass, energy) per block into `partials`
 // (4 doubles per block: mass sum, mass compensation, energy sum, energy

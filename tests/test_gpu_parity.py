@@ -319,3 +319,33 @@ def test_handles_of_one_kernel_with_different_shared_memory(gpu, oracle):
             got_a, got_b = a.download(), b.download()
     assert np.array_equal(got_a, oracle.ac_baseline(big, 4, 1.5, 2.0, 1.0, 0.05))
     assert np.array_equal(got_b, oracle.ac_baseline(small, 4, 1.5, 2.0, 1.0, 0.05))
+
+
+# FP32 3D Allen-Cahn grids with rows of 32..256 cells take the streaming
+# kernel (all fields staged per plane by bulk copies): partial strips, Y wrap
+# at both ends, 1 to 16 fields, each model.
+AC_STREAM = [((6, 13, 32), 3, "ac"), ((9, 7, 64), 8, "ac"), ((5, 20, 128), 16, "ac"), ((3, 10, 256), 2, "gg"),
+             ((7, 9, 32), 1, "ac_poly"), ((12, 6, 64), 5, "gg")]
+
+
+@pytest.mark.parametrize("shape,fields,model", AC_STREAM, ids=["%s-%d-%s" % ("x".join(map(str, s)), f, m) for s, f, m in AC_STREAM])
+def test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, model):
+    from mmsp_gb300 import inputs
+
+    steps = 40
+    if model == "ac_poly":
+        x = inputs.noisy_composition(shape, 0.0, 0.8, 700 + shape[0])
+        d = gpu.make_desc(shape, 1, np.float32, "ac_poly", r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=0.01)
+        want = oracle.ac_scalar_shipped(x, steps, 1.0, 1.0, 1.0, 1.0, 0.01)
+    else:
+        x = inputs.voronoi_grains(shape, 7, fields, 710 + shape[0]) * 0.8 + 0.05
+        if model == "ac":
+            d = gpu.make_desc(shape, fields, np.float32, "ac", gamma=1.5, kappa=2.0, mobility=1.0, dt=0.05,
+                              dx=[1.0, 1.1, 0.9])
+            want = oracle.ac_baseline(x, steps, 1.5, 2.0, 1.0, 0.05, dx=[1.0, 1.1, 0.9])
+        else:
+            d = gpu.make_desc(shape, fields, np.float32, "gg", dt=0.01)
+            want = oracle.ac_graingrowth(x, steps, 0.01)
+    got = run_gpu(gpu, d, x.astype(np.float32), steps).astype(np.float64)
+    assert np.abs(got - want).max() <= TOL_F32
+    assert np.abs(want - x).max() > 1e-3
