@@ -46,6 +46,26 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest value of x over the ranks of the default process group
+    (x itself without one).  Replicas time their own solves; the job's time is
+    the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: float, slowest_seconds: float, world: int) -> float:
+    """Whole-job throughput of independent replicas: all ranks' units over
+    the slowest rank's time (weak scaling)."""
+    return world * units_per_rank / slowest_seconds
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -176,6 +196,46 @@ def run_reference(args):
     return 0
 
 
+def other_configs(native, inputs, stream):
+    """The other single-grid configurations, timed with CUDA events on
+    `stream`: 2D CH 256^2 FP64 (2000 steps) and 3D AC 128^3 x 8 (500 steps,
+    dt 0.05; dt 0.1 diverges) in FP32 and FP64."""
+    import torch
+
+    def timed(desc, x, steps):
+        s = native.Stepper(desc)
+        s.set_stream(stream.cuda_stream)
+        s.upload(x)
+        s.step(min(steps, 64))
+        s.synchronize()
+        s.upload(x)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            s.step(steps)
+            e1.record(stream)
+        stream.synchronize()
+        out = s.download()
+        s.close()
+        return e0.elapsed_time(e1), out
+
+    res = {}
+    c2 = inputs.noisy_composition((256, 256), 0.5, 0.01, 1)
+    ms, _ = timed(native.make_desc((256, 256), 1, np.float64, "ch", dt=0.005), c2, 2000)
+    res["ch2d_256_f64_2000"] = {"ms": ms, "cell_updates_per_s": 256 * 256 * 2000 / (ms / 1e3)}
+    e = inputs.voronoi_grains((128, 128, 128), 200, 8, 3)
+    ms32, o32 = timed(native.make_desc((128, 128, 128), 8, np.float32, "ac", gamma=1.5, kappa=2.0, dt=0.05),
+                      e.astype(np.float32), 500)
+    ms64, o64 = timed(native.make_desc((128, 128, 128), 8, np.float64, "ac", gamma=1.5, kappa=2.0, dt=0.05), e, 500)
+    vals = 128 ** 3 * 8 * 500
+    res["ac3d_128_n8_500"] = {"f32_ms": ms32, "f64_ms": ms64, "f32_value_updates_per_s": vals / (ms32 / 1e3),
+                              "f64_value_updates_per_s": vals / (ms64 / 1e3),
+                              "f32_roofline_frac": 2 * 4 * vals / (ms32 / 1e3) / 1e9 / peaks()[0],
+                              "f32_max_err_vs_f64": float(np.abs(o32.astype(np.float64) - o64).max())}
+    return res
+
+
 def run_gpu(args):
     import torch
 
@@ -239,13 +299,8 @@ def run_gpu(args):
     barrier()
     clk = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in evs]
-    ms_step = float(np.mean(ms))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_step], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = ws * cells * SOLVE_STEPS / (ms_step / 1e3)
+    ms_step = max_over_ranks(float(np.mean(ms)), "cuda")
+    value = job_throughput(cells * SOLVE_STEPS, ms_step / 1e3, ws)
     # accuracy of the timed form: FP32 result vs the FP64 plain form, mass drift
     st32 = s32.reduce()
     out32 = s32.download().astype(np.float64)
@@ -284,13 +339,8 @@ def run_gpu(args):
             raise native.GpuError(rc, "mmsp_gpu_update")
         if i >= args.warmup:
             e2e_t.append(t2 - t1)
-    e2e_s = float(np.mean(e2e_t))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_val = ws * cells * SOLVE_STEPS / e2e_s
+    e2e_s = max_over_ranks(float(np.mean(e2e_t)), "cuda")
+    e2e_val = job_throughput(cells * SOLVE_STEPS, e2e_s, ws)
 
     peak, peak_kind = peaks()
     alg_bytes = cells * 2 * 4                     # one read + one write of the FP32 state per step
@@ -321,6 +371,7 @@ def run_gpu(args):
         "clocks": clk,
         "wall_s_timed_region": wall,
     }
+    line["configs"] = other_configs(native, inputs, stream)
     if rank == 0 and args.cpu_baseline:
         v, n, el = cpu_sample(1)
         line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",

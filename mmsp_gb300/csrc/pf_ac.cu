@@ -75,11 +75,9 @@ ac_step_kernel(const T* __restrict__ ein, T* __restrict__ eout, Geom g, P<T> p, 
             for (int f = 0; f < N; f++) {
                 const int o = f * CP + ci;
                 T y = C[o];
-                T y2 = A::mul(T(2), y);
-                T lap = T(0);
-                if (DIM == 3) lap = lap_axis<T, UNIT_W>(lap, H[o], y2, L[o], p.wx);
-                if (DIM >= 2) lap = lap_axis<T, UNIT_W>(lap, C[o + CW], y2, C[o - CW], p.wy);
-                lap = lap_axis<T, UNIT_W>(lap, C[o + 1], y2, C[o - 1], p.wz);
+                T y2 = twice(y);
+                T lap = lap_ref<T, UNIT_W, DIM>(y2, H[o], L[o], C[o + CW], C[o - CW], C[o + 1], C[o - 1], p.wx, p.wy,
+                                                p.wz);
                 dst[f * cells] = ac_new<T, MODEL>(y, sum, lap, p);
             }
         }

@@ -79,8 +79,8 @@ static __device__ __forceinline__ T lap2(const T (&lo)[V], const T (&ce)[V], con
         if (UNIT) return fmaf(-4.0f, y, (hi[j] + lo[j]) + (zh + zl));
         return fmaf(w0, hi[j] + lo[j], fmaf(w1, zh + zl, -2.0f * (w0 + w1) * y));
     } else {
-        const T y2 = A::mul(T(2), y);
-        T lap = lap_axis<T, UNIT>(T(0), hi[j], y2, lo[j], w0);
+        const T y2 = twice(y);
+        T lap = lap_axis<T, UNIT, true>(T(0), hi[j], y2, lo[j], w0);
         return lap_axis<T, UNIT>(lap, zh, y2, zl, w1);
     }
 }

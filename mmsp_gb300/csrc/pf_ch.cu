@@ -76,11 +76,9 @@ ch_step_kernel(const T* __restrict__ cin, T* __restrict__ cout, Geom g, P<T> p, 
             int my = e / MW, mz = e - my * MW;
             int ci = (my + 1) * CW + (mz + 1);
             T y = C[ci];
-            T y2 = A::mul(T(2), y);
-            T lap = T(0);
-            if (DIM == 3) lap = lap_axis<T, UNIT_W>(lap, H[ci], y2, L[ci], p.wx);
-            if (DIM >= 2) lap = lap_axis<T, UNIT_W>(lap, C[ci + CW], y2, C[ci - CW], p.wy);
-            lap = lap_axis<T, UNIT_W>(lap, C[ci + 1], y2, C[ci - 1], p.wz);
+            T y2 = twice(y);
+            T lap = lap_ref<T, UNIT_W, DIM>(y2, H[ci], L[ci], C[ci + CW], C[ci - CW], C[ci + 1], C[ci - 1], p.wx,
+                                            p.wy, p.wz);
             M[e] = ch_mu<T, MODEL>(y, lap, p);
         }
     };
@@ -97,11 +95,9 @@ ch_step_kernel(const T* __restrict__ cin, T* __restrict__ cout, Geom g, P<T> p, 
             if (gy >= g.Y) break;
             int mi = (ly + 1) * MW + (lz + 1);
             T y = M[mi];
-            T y2 = A::mul(T(2), y);
-            T lap = T(0);
-            if (DIM == 3) lap = lap_axis<T, UNIT_W>(lap, MH[mi], y2, ML[mi], p.wx);
-            if (DIM >= 2) lap = lap_axis<T, UNIT_W>(lap, M[mi + MW], y2, M[mi - MW], p.wy);
-            lap = lap_axis<T, UNIT_W>(lap, M[mi + 1], y2, M[mi - 1], p.wz);
+            T y2 = twice(y);
+            T lap = lap_ref<T, UNIT_W, DIM>(y2, MH[mi], ML[mi], M[mi + MW], M[mi - MW], M[mi + 1], M[mi - 1], p.wx,
+                                            p.wy, p.wz);
             T c = C[(ly + 2) * CW + (lz + 2)];
             cout[(long long)gx * g.YZ + (long long)gy * g.Z + gz] = A::add(c, A::mul(p.dtm, lap));
         }

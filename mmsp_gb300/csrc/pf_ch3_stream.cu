@@ -30,7 +30,7 @@ namespace pf {
 #define PF_CH3_RING 4
 #endif
 #ifndef PF_CH3_MINB
-#define PF_CH3_MINB 1
+#define PF_CH3_MINB 3
 #endif
 #ifndef PF_CH3_R
 #define PF_CH3_R 8
@@ -43,49 +43,52 @@ struct F32Coef {
     float kappa, dtm, neg_r, u;
 };
 
-template <int MODEL>
-static __device__ __forceinline__ float mu_f32(float c, float lap, const F32Coef& q)
+// A thread's cells: float (one cell) or float2 (two adjacent cells).  float2
+// arithmetic uses the packed FP32x2 instructions, one instruction for both
+// cells.
+template <int V> struct Cells;
+template <> struct Cells<1> { using type = float; };
+template <> struct Cells<2> { using type = float2; };
+
+static __device__ __forceinline__ float vadd(float a, float b) { return a + b; }
+static __device__ __forceinline__ float2 vadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+static __device__ __forceinline__ float vmul(float a, float b) { return a * b; }
+static __device__ __forceinline__ float2 vmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+static __device__ __forceinline__ float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+static __device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+template <typename VT> static __device__ __forceinline__ VT vset(float k);
+template <> __device__ __forceinline__ float vset<float>(float k) { return k; }
+template <> __device__ __forceinline__ float2 vset<float2>(float k) { return make_float2(k, k); }
+static __device__ __forceinline__ float vfirst(float a) { return a; }
+static __device__ __forceinline__ float vfirst(float2 a) { return a.x; }
+static __device__ __forceinline__ float vlast(float a) { return a; }
+static __device__ __forceinline__ float vlast(float2 a) { return a.y; }
+// Sum of the two Z neighbours of each cell, given the cells just left and
+// just right of the thread's run.
+static __device__ __forceinline__ float vzsum(float, float left, float right) { return left + right; }
+static __device__ __forceinline__ float2 vzsum(float2 c, float left, float right)
 {
-    float fp;
-    if (MODEL == MMSP_GPU_CH) {
-        // 2c(1-c)(1-2c) = c*(2 + c*(-6 + 4c))
-        fp = c * fmaf(fmaf(4.0f, c, -6.0f), c, 2.0f);
-    } else {
-        // -r c + u c^3 = c*(u c^2 - r)
-        fp = c * fmaf(q.u, c * c, q.neg_r);
-    }
-    return fmaf(-q.kappa, lap, fp);
+    return __fadd2_rn(make_float2(left, c.x), make_float2(c.y, right));
+}
+
+template <int MODEL, typename VT>
+static __device__ __forceinline__ VT mu_v(VT c, VT lap, const F32Coef& q)
+{
+    VT fp;
+    if (MODEL == MMSP_GPU_CH)   // 2c(1-c)(1-2c) = c*(2 + c*(-6 + 4c))
+        fp = vmul(c, vfma(vfma(vset<VT>(4.0f), c, vset<VT>(-6.0f)), c, vset<VT>(2.0f)));
+    else                        // -r c + u c^3 = c*(u c^2 - r)
+        fp = vmul(c, vfma(vset<VT>(q.u), vmul(c, c), vset<VT>(q.neg_r)));
+    return vfma(vset<VT>(-q.kappa), lap, fp);
 }
 
 // wx*sx + wy*sy + wz*sz - 2(wx+wy+wz)*c, with sx, sy, sz the sums of the two
 // neighbours along each axis.
-template <bool UNIT>
-static __device__ __forceinline__ float lap_f32(float sx, float sy, float sz, float c, const F32Coef& q)
+template <bool UNIT, typename VT>
+static __device__ __forceinline__ VT lap_v(VT sx, VT sy, VT sz, VT c, const F32Coef& q)
 {
-    if (UNIT) return fmaf(-6.0f, c, (sx + sy) + sz);
-    return fmaf(q.wx, sx, fmaf(q.wy, sy, fmaf(q.wz, sz, -q.w2 * c)));
-}
-
-template <int V>
-static __device__ __forceinline__ void lds_vec(float (&dst)[V], const float* src)
-{
-    if constexpr (V == 1) {
-        dst[0] = src[0];
-    } else {
-        float2 t = *reinterpret_cast<const float2*>(src);
-        dst[0] = t.x;
-        dst[1] = t.y;
-    }
-}
-
-template <int V>
-static __device__ __forceinline__ void stg_vec(float* dst, const float (&v)[V])
-{
-    if constexpr (V == 1) {
-        dst[0] = v[0];
-    } else {
-        *reinterpret_cast<float2*>(dst) = make_float2(v[0], v[1]);
-    }
+    if (UNIT) return vfma(vset<VT>(-6.0f), c, vadd(vadd(sx, sy), sz));
+    return vfma(vset<VT>(q.wx), sx, vfma(vset<VT>(q.wy), sy, vfma(vset<VT>(q.wz), sz, vmul(vset<VT>(-q.w2), c))));
 }
 
 // Shared memory: kRing slots of (R+4) x Z floats, the warp-end mu buffers
@@ -98,7 +101,7 @@ static size_t ch3_smem(int R, int Z, int V)
 }
 
 template <int R, int Z, int V, int MODEL, bool UNIT>
-__global__ void __launch_bounds__(Z / V, PF_CH3_MINB)
+__global__ void __launch_bounds__(Z / V, (Z / V) <= 128 ? PF_CH3_MINB : 1)
 ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, F32Coef q, int planes,
                int* __restrict__ err)
 {
@@ -165,8 +168,9 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     if (t == 0)
         for (int pl = x_first; pl < x_first + kRing && pl <= x_last; pl++) fill(pl);
 
-    float cA[RR][V], cB[RR][V], cC[RR][V];
-    float mA[R + 2][V], mB[R + 2][V], mC[R + 2][V];
+    using VT = typename Cells<V>::type;
+    VT cA[RR], cB[RR], cC[RR];
+    VT mA[R + 2], mB[R + 2], mC[R + 2];
     wait_plane(x_first);
     wait_plane(x_first + 1);
     {
@@ -174,38 +178,32 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         const float* s1 = slot_of(x_first + 1) + z0;
 #pragma unroll
         for (int i = 0; i < RR; i++) {
-            lds_vec<V>(cA[i], s0 + i * Z);
-            lds_vec<V>(cB[i], s1 + i * Z);
+            cA[i] = *reinterpret_cast<const VT*>(s0 + i * Z);
+            cB[i] = *reinterpret_cast<const VT*>(s1 + i * Z);
         }
     }
 #pragma unroll
-    for (int i = 0; i < R + 2; i++)
-#pragma unroll
-        for (int j = 0; j < V; j++) mA[i][j] = mB[i][j] = 0.0f;
+    for (int i = 0; i < R + 2; i++) mA[i] = mB[i] = vset<VT>(0.0f);
     __syncthreads();
     if (t == 0 && !s_err && x_first + kRing <= x_last) fill(x_first + kRing);   // slot of x_first is free
 
     // One plane: a = c(x), b = c(x+1), c = c(x+2) (loaded here); ma = mu(x-1),
     // mb = mu(x), mc = mu(x+1) (computed here); writes c'(x) when x >= xs.
-    auto iter = [&](int x, float (&a)[RR][V], float (&b)[RR][V], float (&c)[RR][V], float (&ma)[R + 2][V],
-                    float (&mb)[R + 2][V], float (&mc)[R + 2][V]) -> bool {
+    auto iter = [&](int x, VT (&a)[RR], VT (&b)[RR], VT (&c)[RR], VT (&ma)[R + 2], VT (&mb)[R + 2],
+                    VT (&mc)[R + 2]) -> bool {
         wait_plane(x + 2);
         const float* s2 = slot_of(x + 2) + z0;
 #pragma unroll
-        for (int i = 0; i < RR; i++) lds_vec<V>(c[i], s2 + i * Z);
+        for (int i = 0; i < RR; i++) c[i] = *reinterpret_cast<const VT*>(s2 + i * Z);
         const float* s1 = slot_of(x + 1);
 #pragma unroll
         for (int r = -1; r <= R; r++) {
             const int i = r + 2;
             const float left = s1[i * Z + zl];
             const float right = s1[i * Z + zh];
-#pragma unroll
-            for (int j = 0; j < V; j++) {
-                const float cc = b[i][j];
-                const float sz = (j == 0 ? left : b[i][j - 1]) + (j == V - 1 ? right : b[i][j + 1]);
-                const float lap = lap_f32<UNIT>(a[i][j] + c[i][j], b[i - 1][j] + b[i + 1][j], sz, cc, q);
-                mc[r + 1][j] = mu_f32<MODEL>(cc, lap, q);
-            }
+            const VT cc = b[i];
+            const VT lap = lap_v<UNIT>(vadd(a[i], c[i]), vadd(b[i - 1], b[i + 1]), vzsum(cc, left, right), cc, q);
+            mc[r + 1] = mu_v<MODEL>(cc, lap, q);
         }
         // warp ends publish mu(x+1) of rows 0..R-1 for the neighbouring warps
         float* e1 = edges + (((x + 1) & 1) * W + warp) * 2 * R;
@@ -216,8 +214,8 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
 #pragma unroll
             for (int r = 0; r < R; r += 4)
                 *reinterpret_cast<float4*>(dst + r) = make_float4(
-                    first ? mc[r + 1][0] : mc[r + 1][V - 1], first ? mc[r + 2][0] : mc[r + 2][V - 1],
-                    first ? mc[r + 3][0] : mc[r + 3][V - 1], first ? mc[r + 4][0] : mc[r + 4][V - 1]);
+                    first ? vfirst(mc[r + 1]) : vlast(mc[r + 1]), first ? vfirst(mc[r + 2]) : vlast(mc[r + 2]),
+                    first ? vfirst(mc[r + 3]) : vlast(mc[r + 3]), first ? vfirst(mc[r + 4]) : vlast(mc[r + 4]));
         }
         if (x >= xs) {
             // the neighbouring warps' end cells: every lane reads the same
@@ -235,19 +233,14 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
             const int rows = min(R, g.Y - y0);
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                const float up = __shfl_up_sync(0xffffffffu, mb[r + 1][V - 1], 1);
-                const float down = __shfl_down_sync(0xffffffffu, mb[r + 1][0], 1);
+                const float up = __shfl_up_sync(0xffffffffu, vlast(mb[r + 1]), 1);
+                const float down = __shfl_down_sync(0xffffffffu, vfirst(mb[r + 1]), 1);
                 const float left = lane == 0 ? el[r] : up;
                 const float right = lane == 31 ? eh[r] : down;
-                float o[V];
-#pragma unroll
-                for (int j = 0; j < V; j++) {
-                    const float m = mb[r + 1][j];
-                    const float sz = (j == 0 ? left : mb[r + 1][j - 1]) + (j == V - 1 ? right : mb[r + 1][j + 1]);
-                    const float lap = lap_f32<UNIT>(ma[r + 1][j] + mc[r + 1][j], mb[r][j] + mb[r + 2][j], sz, m, q);
-                    o[j] = fmaf(q.dtm, lap, a[r + 2][j]);
-                }
-                if (r < rows) stg_vec<V>(dst + (long long)r * Z, o);
+                const VT m = mb[r + 1];
+                const VT lap = lap_v<UNIT>(vadd(ma[r + 1], mc[r + 1]), vadd(mb[r], mb[r + 2]), vzsum(m, left, right), m, q);
+                const VT o = vfma(vset<VT>(q.dtm), lap, a[r + 2]);
+                if (r < rows) *reinterpret_cast<VT*>(dst + (long long)r * Z) = o;
             }
         }
         __syncthreads();

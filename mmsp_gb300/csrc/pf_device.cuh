@@ -48,15 +48,60 @@ template <typename T> struct P {
     T kappa, dtm, gamma2, neg_r, u;
 };
 
+// 2.0*y, which is exact.  For FP64 a normal y whose double stays finite is
+// doubled by adding 1 to its exponent on the integer pipe; zeros,
+// subnormals, values near overflow, infinities and NaNs take the multiply.
+// Either way the bits are those of __dmul_rn(2.0, y).
+static __device__ __forceinline__ double twice(double y)
+{
+    const long long b = __double_as_longlong(y);
+    const unsigned e = (unsigned)((b >> 52) & 0x7ff);
+    if (e - 1u < 2045u) return __longlong_as_double(b + (1LL << 52));
+    return __dmul_rn(2.0, y);
+}
+static __device__ __forceinline__ float twice(float y) { return 2.0f * y; }
+
+// 0.0 + t, which is t except that -0.0 becomes +0.0: a select on the bits
+// instead of an FP64 add.
+static __device__ __forceinline__ double plus_zero(double t)
+{
+    const long long b = __double_as_longlong(t);
+    return b == (long long)0x8000000000000000ULL ? 0.0 : t;
+}
+static __device__ __forceinline__ float plus_zero(float t) { return t + 0.0f; }
+
 // One axis of MMSP::laplacian (grid.cpp:2055-2064):
 //   acc + weight * (yh - 2.0*y + yl), with y2 = 2.0*y precomputed (exact).
-template <typename T, bool UNIT_W>
+// FIRST marks the first axis, where acc is the initial 0.0.
+template <typename T, bool UNIT_W, bool FIRST = false>
 static __device__ __forceinline__ T lap_axis(T acc, T yh, T y2, T yl, T w)
 {
     using A = Ar<T>;
     T t = A::add(A::sub(yh, y2), yl);
     if (!UNIT_W) t = A::mul(w, t);
+    if (FIRST) return plus_zero(t);
     return A::add(acc, t);
+}
+
+// The whole Laplacian of a DIM-dimensional grid in the reference's axis
+// order (axis 0 first): padded axes X (DIM 3), Y (DIM >= 2), Z.
+template <typename T, bool UNIT_W, int DIM>
+static __device__ __forceinline__ T lap_ref(T y2, T xh, T xl, T yh, T yl, T zh, T zl, T wx, T wy, T wz)
+{
+    T lap = T(0);
+    if (DIM == 3) lap = lap_axis<T, UNIT_W, true>(lap, xh, y2, xl, wx);
+    if (DIM == 3) lap = lap_axis<T, UNIT_W, false>(lap, yh, y2, yl, wy);
+    if (DIM == 2) lap = lap_axis<T, UNIT_W, true>(lap, yh, y2, yl, wy);
+    if (DIM >= 2) lap = lap_axis<T, UNIT_W, false>(lap, zh, y2, zl, wz);
+    else lap = lap_axis<T, UNIT_W, true>(lap, zh, y2, zl, wz);
+    return lap;
+}
+
+// kappa*lap, skipping the multiply when kappa is exactly 1 (1.0*x == x).
+template <typename T>
+static __device__ __forceinline__ T kappa_times(T kappa, T lap)
+{
+    return kappa == T(1) ? lap : Ar<T>::mul(kappa, lap);
 }
 
 // Chemical potential of the Cahn-Hilliard models.
@@ -66,13 +111,13 @@ static __device__ __forceinline__ T ch_mu(T phi, T lap, const P<T>& p)
     using A = Ar<T>;
     if (MODEL == MMSP_GPU_CH) {
         // 2.0*phi*(1.0-phi)*(1.0-2.0*phi) - K*lap
-        T t2 = A::mul(T(2), phi);
+        T t2 = twice(phi);
         T fp = A::mul(A::mul(t2, A::sub(T(1), phi)), A::sub(T(1), t2));
-        return A::sub(fp, A::mul(p.kappa, lap));
+        return A::sub(fp, kappa_times(p.kappa, lap));
     } else {
         // -r*phi + u*pow(phi,3) - K*lap   (cahn-hilliard.cpp:71)
         T a = A::add(A::mul(p.neg_r, phi), A::mul(p.u, cube(phi)));
-        return A::sub(a, A::mul(p.kappa, lap));
+        return A::sub(a, kappa_times(p.kappa, lap));
     }
 }
 
@@ -87,15 +132,15 @@ static __device__ __forceinline__ T ac_new(T phi, T sum, T lap, const P<T>& p)
         T p3 = A::mul(p2, phi);
         T a = A::add(-phi, p3);
         T g = A::mul(A::mul(p.gamma2, phi), A::sub(sum, p2));
-        T c = A::sub(A::add(a, g), A::mul(p.kappa, lap));
+        T c = A::sub(A::add(a, g), kappa_times(p.kappa, lap));
         return A::sub(phi, A::mul(p.dtm, c));
     } else if (MODEL == MMSP_GPU_GG) {
         // phi - dt*(-phi - pow(phi,3) + 2.0*(phi*sum - lap))   (graingrowth.cpp:105)
-        T e = A::add(A::sub(-phi, cube(phi)), A::mul(T(2), A::sub(A::mul(phi, sum), lap)));
+        T e = A::add(A::sub(-phi, cube(phi)), twice(A::sub(A::mul(phi, sum), lap)));
         return A::sub(phi, A::mul(p.dtm, e));
     } else {
         // phi - dt*M*(-r*phi + u*pow(phi,3) - K*lap)   (allen-cahn.cpp:70)
-        T e = A::sub(A::add(A::mul(p.neg_r, phi), A::mul(p.u, cube(phi))), A::mul(p.kappa, lap));
+        T e = A::sub(A::add(A::mul(p.neg_r, phi), A::mul(p.u, cube(phi))), kappa_times(p.kappa, lap));
         return A::sub(phi, A::mul(p.dtm, e));
     }
 }
