@@ -1,14 +1,15 @@
 // pf_ac3_stream.cu -- FP32 3D multi-order Allen-Cahn step, streaming along X.
 //
-// The precision-form kernel for 3D grids whose rows (axis Z) hold 32, 64,
-// 128 or 256 cells.  A block owns R rows (axis Y) of full Z extent, one
+// The precision-form kernel for 3D grids with rows (axis Z) of up to 256
+// cells.  A block owns R rows (axis Y) of full Z extent, one
 // thread per cell of a row, and a run of X planes.  For every plane the
 // block's R+2 rows (one halo row each side, wrapped periodically) of all N
 // fields arrive in shared memory through cp.async.bulk (one copy per field,
 // two where the rows wrap) on a D-deep mbarrier ring.  With D = 3 the copy
 // of plane x+2 is issued as soon as plane x-1 is released; the copies of the
-// several blocks resident on an SM overlap each other's computation.  Per cell the sum of squares
-// over the fields comes first, then each field's new value from its own
+// several blocks resident on an SM overlap each other's computation.  Per
+// cell the sum of squares over the fields comes first, then each field's
+// new value from its own
 // 7-point Laplacian; Y neighbours are registers, X and Z neighbours are read
 // from shared memory (Z wraps across the row).  There is no Z halo, and the
 // Y halo costs 2 extra rows per R-row strip in reads only.
@@ -42,20 +43,29 @@ static __device__ __forceinline__ float ac_new_f32(float c, float sum, float lap
     }
 }
 
-static size_t ac3_smem(int R, int Z, int N, int D) { return sizeof(float) * (size_t)D * N * (R + 2) * Z + sizeof(uint64_t) * D; }
+static size_t ac3_smem(int R, int Z, int N, int D)
+{
+    return sizeof(float) * (((size_t)D * N * (R + 2) * Z + 1) & ~(size_t)1) + sizeof(uint64_t) * D;
+}
 
-template <int R, int Z, int MODEL>
-__global__ void __launch_bounds__(Z)
+// BULK: rows are a multiple of 16 bytes, and thread 0 stages each field's
+// rows with cp.async.bulk (transaction-counted mbarrier, one arrival).
+// Otherwise every thread copies its own cells with 4-byte cp.async and
+// arrives on the mbarrier when they land (one arrival per thread).
+template <int R, int MODEL, bool BULK>
+__global__ void __launch_bounds__(256)
 ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, AcF32 q, int planes, int N, int D,
                int* __restrict__ err)
 {
     constexpr int RR = R + 2;
-    const int z = threadIdx.x;
+    const int Z = g.Z;
+    const int t = threadIdx.x;
+    const bool on = t < Z;
+    const int z = on ? t : 0;
     extern __shared__ __align__(128) unsigned char sm[];
     float* slots = reinterpret_cast<float*>(sm);
     const size_t slot_elems = (size_t)N * RR * Z;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(slots + (size_t)D * slot_elems);
-    __shared__ int s_err;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(slots + (((size_t)D * slot_elems + 1) & ~(size_t)1));
 
     const int y0 = blockIdx.x * R;
     const int xs = blockIdx.y * planes;
@@ -66,53 +76,64 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
     const int x_first = xs - 1, x_last = xe;   // planes read from global memory
     const long long cells = g.cells;
 
+    // BULK: called by thread 0 only; otherwise by every thread
     auto fill = [&](int pl) {
         const int k = pl - x_first, s = k % D;
         uint64_t* bar = &bars[s];
         float* dst0 = slots + (size_t)s * slot_elems;
         const long long plane = (long long)wrapi(pl, g.X) * g.YZ;
-        constexpr uint32_t row = (uint32_t)Z * sizeof(float);
-        fence_proxy_async();
-        mbar_expect_tx(bar, (uint32_t)N * RR * row);
-        const int a = y0 - 1, b = y0 + R + 1;
-        for (int f = 0; f < N; f++) {
-            const float* base = ein + (long long)f * cells + plane;
-            float* dst = dst0 + (size_t)f * RR * Z;
-            if (a >= 0 && b <= g.Y) {
-                bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
-            } else if (a < 0) {
-                bulk_g2s(dst, base + (long long)(g.Y - 1) * Z, row, bar);
-                bulk_g2s(dst + Z, base, (RR - 1) * row, bar);
-            } else {
-                const int n1 = g.Y - a;
-                bulk_g2s(dst, base + (long long)a * Z, n1 * row, bar);
-                bulk_g2s(dst + (size_t)n1 * Z, base, (RR - n1) * row, bar);
+        if constexpr (BULK) {
+            const uint32_t row = (uint32_t)Z * sizeof(float);
+            fence_proxy_async();
+            mbar_expect_tx(bar, (uint32_t)N * RR * row);
+            const int a = y0 - 1, b = y0 + R + 1;
+            for (int f = 0; f < N; f++) {
+                const float* base = ein + (long long)f * cells + plane;
+                float* dst = dst0 + (size_t)f * RR * Z;
+                if (a >= 0 && b <= g.Y) {
+                    bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
+                } else if (a < 0) {
+                    bulk_g2s(dst, base + (long long)(g.Y - 1) * Z, row, bar);
+                    bulk_g2s(dst + Z, base, (RR - 1) * row, bar);
+                } else {
+                    const int n1 = g.Y - a;
+                    bulk_g2s(dst, base + (long long)a * Z, n1 * row, bar);
+                    bulk_g2s(dst + (size_t)n1 * Z, base, (RR - n1) * row, bar);
+                }
             }
+        } else {
+            if (on)
+                for (int f = 0; f < N; f++) {
+                    const float* base = ein + (long long)f * cells + plane + z;
+                    float* dst = dst0 + (size_t)f * RR * Z + z;
+#pragma unroll
+                    for (int r = 0; r < RR; r++) cp_async4(dst + r * Z, base + (long long)wrapi(y0 - 1 + r, g.Y) * Z);
+                }
+            cp_async_arrive(bar);
         }
     };
     auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % D) * slot_elems; };
-    auto wait_plane = [&](int pl) {
+    auto arrived = [&](int pl) {
         const int k = pl - x_first;
-        if (!mbar_wait(&bars[k % D], (uint32_t)(k / D) & 1u)) {
-            s_err = 1;
-            atomicExch(err, 1);
-        }
+        return mbar_wait(&bars[k % D], (uint32_t)(k / D) & 1u);
     };
 
-    if (z == 0) {
-        for (int s = 0; s < D; s++) mbar_init(&bars[s], 1);
+    if (t == 0) {
+        for (int s = 0; s < D; s++) mbar_init(&bars[s], BULK ? 1 : blockDim.x);
         mbar_fence_init();
-        s_err = 0;
     }
     __syncthreads();
-    if (z == 0)
-        for (int pl = x_first; pl < x_first + D && pl <= x_last; pl++) fill(pl);
-    wait_plane(x_first);
-    wait_plane(x_first + 1);
+    int issued = min(x_first + D - 1, x_last);   // last plane whose fill was issued
+    if (!BULK || t == 0)
+        for (int pl = x_first; pl <= issued; pl++) fill(pl);
+    bool bad = !arrived(x_first);
+    bad |= !arrived(x_first + 1);
+    // The decision to stop is taken block-wide (__syncthreads_or), so every
+    // thread leaves the loop at the same barrier.
+    bool stop = __syncthreads_or(bad);
 
-    int x = xs;
-    for (; x < xe && !s_err; x++) {
-        wait_plane(x + 1);
+    for (int x = xs; x < xe && !stop; x++) {
+        bad = !arrived(x + 1);
         const float* SL = slot_of(x - 1);
         const float* SC = slot_of(x);
         const float* SH = slot_of(x + 1);
@@ -138,43 +159,41 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
             float* dst = eout + (long long)f * cells + (long long)x * g.YZ + (long long)y0 * Z + z;
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                const int o = (int)fo + (r + 1) * Z;
+                const size_t o = fo + (size_t)(r + 1) * Z;
                 const float cc = col[r + 1];
                 const float sx = SL[o + z] + SH[o + z];
                 const float sy = col[r] + col[r + 2];
                 const float sz = SC[o + zl] + SC[o + zh];
                 const float lap = fmaf(q.wx, sx, fmaf(q.wy, sy, fmaf(q.wz, sz, -q.w2 * cc)));
-                if (r < rows) dst[(long long)r * Z] = ac_new_f32<MODEL>(cc, sum[r], lap, q);
+                if (on && r < rows) dst[(long long)r * Z] = ac_new_f32<MODEL>(cc, sum[r], lap, q);
             }
         }
-        __syncthreads();
-        if (z == 0 && !s_err && x - 1 + D <= x_last) fill(x - 1 + D);   // slot of x-1 is free now
-    }
-    if (s_err && z == 0) {
-        for (int pl = max(x - 1, x_first); pl <= min(x - 1 + D, x_last); pl++) {
-            const int k = pl - x_first;
-            mbar_wait(&bars[k % D], (uint32_t)(k / D) & 1u);
+        stop = __syncthreads_or(bad);
+        if (!stop && x - 1 + D <= x_last) {   // the slot of x-1 is free now
+            if (!BULK || t == 0) fill(x - 1 + D);
+            issued = x - 1 + D;
         }
     }
+    if (stop) {
+        if (t == 0) atomicExch(err, 1);
+        // leave no copy in flight: wait (bounded) for the last fill of every slot
+        for (int pl = max(x_first, issued - D + 1); pl <= issued; pl++) arrived(pl);
+    }
 }
 
-template <int R, int Z>
+template <int R, bool BULK>
 static const void* ac3_pick_model(int model)
 {
-    if (model == MMSP_GPU_AC) return (const void*)&ac3_stream_f32<R, Z, MMSP_GPU_AC>;
-    if (model == MMSP_GPU_GG) return (const void*)&ac3_stream_f32<R, Z, MMSP_GPU_GG>;
-    return (const void*)&ac3_stream_f32<R, Z, MMSP_GPU_AC_POLY>;
+    if (model == MMSP_GPU_AC) return (const void*)&ac3_stream_f32<R, MMSP_GPU_AC, BULK>;
+    if (model == MMSP_GPU_GG) return (const void*)&ac3_stream_f32<R, MMSP_GPU_GG, BULK>;
+    return (const void*)&ac3_stream_f32<R, MMSP_GPU_AC_POLY, BULK>;
 }
 
-template <int R>
-static const void* ac3_pick_z(int Z, int model)
+static const void* ac3_pick(int R, bool bulk, int model)
 {
-    switch (Z) {
-    case 32: return ac3_pick_model<R, 32>(model);
-    case 64: return ac3_pick_model<R, 64>(model);
-    case 128: return ac3_pick_model<R, 128>(model);
-    default: return ac3_pick_model<R, 256>(model);
-    }
+    if (R == 4) return bulk ? ac3_pick_model<4, true>(model) : ac3_pick_model<4, false>(model);
+    if (R == 2) return bulk ? ac3_pick_model<2, true>(model) : ac3_pick_model<2, false>(model);
+    return bulk ? ac3_pick_model<1, true>(model) : ac3_pick_model<1, false>(model);
 }
 
 constexpr size_t kAcSmemCap = 200 * 1024;
@@ -192,9 +211,9 @@ static bool ac3_shape(const Geom& g, int N, int* R, int* D)
         return true;
     }
 #endif
-    static const int kR[] = {4, 2, 2, 2};
-    static const int kD[] = {3, 3, 3, 3};
-    for (int i = 0; i < 4; i++)
+    static const int kR[] = {4, 2, 1};
+    static const int kD[] = {3, 3, 3};
+    for (int i = 0; i < 3; i++)
         if (g.Y >= kR[i] + 2 && ac3_smem(kR[i], g.Z, N, kD[i]) <= kAcSmemCap) {
             *R = kR[i];
             *D = kD[i];
@@ -206,8 +225,7 @@ static bool ac3_shape(const Geom& g, int N, int* R, int* D)
 bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
     int R, D;
-    const bool rows = g.Z == 32 || g.Z == 64 || g.Z == 128 || g.Z == 256;
-    return d.dtype == MMSP_GPU_F32 && g.dim == 3 && rows &&
+    return d.dtype == MMSP_GPU_F32 && g.dim == 3 && g.Z <= 256 &&
            (d.model == MMSP_GPU_AC || d.model == MMSP_GPU_GG || d.model == MMSP_GPU_AC_POLY) &&
            ac3_shape(g, d.fields, &R, &D);
 }
@@ -216,13 +234,15 @@ cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     int R = 4, D = 4;
     ac3_shape(g, d.fields, &R, &D);
-    p->fn = R == 4 ? ac3_pick_z<4>(g.Z, d.model) : ac3_pick_z<2>(g.Z, d.model);
+    const bool bulk = g.Z % 4 == 0;   // 16-byte rows
+    const int threads = (g.Z + 31) / 32 * 32;
+    p->fn = ac3_pick(R, bulk, d.model);
     p->smem = ac3_smem(R, g.Z, d.fields, D);
-    p->block = dim3(g.Z, 1, 1);
+    p->block = dim3(threads, 1, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, g.Z, p->smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, threads, p->smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int strips = (g.Y + R - 1) / R;

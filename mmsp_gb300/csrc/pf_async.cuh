@@ -78,4 +78,18 @@ static __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint
         : "memory");
 }
 
+// Per-thread asynchronous 4-byte copy global -> shared (no alignment needs
+// beyond the element's own).
+static __device__ __forceinline__ void cp_async4(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// Arrive on `bar` once this thread's earlier cp.async copies have landed; the
+// barrier's expected count must include one arrival per calling thread.
+static __device__ __forceinline__ void cp_async_arrive(uint64_t* bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 }  // namespace pf

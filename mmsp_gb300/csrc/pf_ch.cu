@@ -165,6 +165,7 @@ static const void* ch_pick(int dim, int model, int ty, bool unit)
 cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     if (ch3_stream_eligible(d, g)) return plan_ch3_stream(d, g, p);
+    if (ch_rows_eligible(d, g)) return plan_ch_rows(d, g, p);
     p->kind = 0;
     Coeffs c = make_coeffs(d);
     int ty = g.Y >= 16 ? 16 : 8;
@@ -207,6 +208,7 @@ cudaError_t launch_ch(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, 
                       const void* in, void* out, int* err, cudaStream_t s)
 {
     if (p.kind == 1) return launch_ch3_stream(p, g, c, in, out, err, s);
+    if (p.kind == 3) return launch_ch_rows(p, d, c, in, out, s);
     int planes = p.planes;
     if (d.dtype == MMSP_GPU_F64) {
         P<double> q = narrow<double>(c, g.dim);

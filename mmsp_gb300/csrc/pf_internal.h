@@ -47,7 +47,8 @@ struct StepPlan {
     size_t smem;
     int planes;        // planes of axis X per block (3D streaming)
     int fields;
-    int kind;          // 0: generic tile kernel, 1: FP32 3D CH streaming, 2: FP32 3D AC streaming
+    int kind;          // 0: generic tile kernel, 1: FP32 3D CH streaming, 2: FP32 3D AC streaming,
+                       // 3: FP32 CH rows of any length
     int ring;          // planes in the shared-memory ring (streaming kernels)
     bool ok;
 };
@@ -61,6 +62,12 @@ bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g);
 cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c, const void* in, void* out,
                               int* err, cudaStream_t s);
+
+// FP32 2D/3D Cahn-Hilliard for any row length up to 1024 (pf_rows.cu).
+bool ch_rows_eligible(const mmsp_gpu_desc& d, const Geom& g);
+cudaError_t plan_ch_rows(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
+cudaError_t launch_ch_rows(const StepPlan& p, const mmsp_gpu_desc& d, const Coeffs& c, const void* in, void* out,
+                           cudaStream_t s);
 
 // FP32 3D Allen-Cahn on whole rows (pf_ac3_stream.cu).
 bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g);

@@ -321,11 +321,15 @@ def test_handles_of_one_kernel_with_different_shared_memory(gpu, oracle):
     assert np.array_equal(got_b, oracle.ac_baseline(small, 4, 1.5, 2.0, 1.0, 0.05))
 
 
-# FP32 3D Allen-Cahn grids with rows of 32..256 cells take the streaming
-# kernel (all fields staged per plane by bulk copies): partial strips, Y wrap
-# at both ends, 1 to 16 fields, each model.
+# FP32 3D Allen-Cahn grids with rows of up to 256 cells take the streaming
+# kernel: all fields staged per plane by bulk copies where rows are 16-byte
+# multiples (Z % 4 == 0), by per-thread 4-byte asynchronous copies otherwise.
+# Partial strips, Y wrap at both ends, strips of 4, 2 and 1 rows (Y = 3..5),
+# 1 to 16 fields, each model.
 AC_STREAM = [((6, 13, 32), 3, "ac"), ((9, 7, 64), 8, "ac"), ((5, 20, 128), 16, "ac"), ((3, 10, 256), 2, "gg"),
-             ((7, 9, 32), 1, "ac_poly"), ((12, 6, 64), 5, "gg")]
+             ((7, 9, 32), 1, "ac_poly"), ((12, 6, 64), 5, "gg"),
+             ((8, 11, 37), 4, "ac"), ((5, 9, 100), 8, "ac"), ((4, 6, 255), 3, "gg"), ((10, 3, 1), 2, "ac"),
+             ((6, 4, 3), 5, "ac_poly"), ((9, 5, 200), 6, "gg"), ((3, 17, 61), 16, "ac"), ((2, 7, 12), 2, "ac")]
 
 
 @pytest.mark.parametrize("shape,fields,model", AC_STREAM, ids=["%s-%d-%s" % ("x".join(map(str, s)), f, m) for s, f, m in AC_STREAM])
@@ -349,3 +353,23 @@ def test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, m
     got = run_gpu(gpu, d, x.astype(np.float32), steps).astype(np.float64)
     assert np.abs(got - want).max() <= TOL_F32
     assert np.abs(want - x).max() > 1e-3
+
+
+# FP32 Cahn-Hilliard grids whose rows are not 32..512 cells in powers of two
+# take the row kernel (any row length, plain loads): 2D rows of odd lengths
+# up to 1024, 3D grids with few rows per plane and odd rows.
+ROWS = [(50, 77), (7, 1024), (3, 33), (1, 100), (20, 9, 45), (6, 3, 70), (11, 1, 33), (5, 40, 500), (9, 30, 1)]
+
+
+@pytest.mark.parametrize("shape", ROWS, ids=["x".join(map(str, s)) for s in ROWS])
+def test_fp32_rows_kernel_against_fp64_oracle(gpu, oracle, shape):
+    from mmsp_gb300 import inputs
+
+    steps = 50
+    dt = 0.004 if len(shape) == 2 else 0.002
+    c0 = inputs.noisy_composition(shape, 0.45, 0.05, 800 + sum(shape))
+    d = gpu.make_desc(shape, 1, np.float32, "ch", kappa=1.2, mobility=0.9, dt=dt, dx=[1.0, 1.1, 0.95][: len(shape)])
+    got = run_gpu(gpu, d, c0.astype(np.float32), steps).astype(np.float64)
+    want = oracle.ch_baseline(c0, steps, 1.2, 0.9, dt, dx=[1.0, 1.1, 0.95][: len(shape)])
+    assert np.abs(got - want).max() <= TOL_F32
+    assert np.abs(want - c0).max() > 1e-4
