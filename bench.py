@@ -80,6 +80,7 @@ def profile_traffic(kernel_tag: str):
     if not os.path.exists(p):
         return None
     for line in open(p):
+        line = line.strip()
         if line.startswith("traffic_bytes_per_launch:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])

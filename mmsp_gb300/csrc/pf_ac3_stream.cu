@@ -1,18 +1,19 @@
 // pf_ac3_stream.cu -- FP32 3D multi-order Allen-Cahn step, streaming along X.
 //
 // The precision-form kernel for 3D grids with rows (axis Z) of up to 256
-// cells.  A block owns R rows (axis Y) of full Z extent, one
-// thread per cell of a row, and a run of X planes.  For every plane the
-// block's R+2 rows (one halo row each side, wrapped periodically) of all N
-// fields arrive in shared memory through cp.async.bulk (one copy per field,
-// two where the rows wrap) on a D-deep mbarrier ring.  With D = 3 the copy
-// of plane x+2 is issued as soon as plane x-1 is released; the copies of the
-// several blocks resident on an SM overlap each other's computation.  Per
-// cell the sum of squares over the fields comes first, then each field's
-// new value from its own
-// 7-point Laplacian; Y neighbours are registers, X and Z neighbours are read
-// from shared memory (Z wraps across the row).  There is no Z halo, and the
-// Y halo costs 2 extra rows per R-row strip in reads only.
+// cells.  A block owns R rows (axis Y) of full Z extent and a run of X
+// planes, with one or two threads per cell of a row (each over R or R/2
+// rows).  For every plane the block's R+2 rows (one halo row each side,
+// wrapped periodically) of all N fields arrive in shared memory on a D-deep
+// mbarrier ring: by cp.async.bulk (one copy per field, two where the rows
+// wrap) when rows are 16-byte multiples, by per-thread 4-byte cp.async
+// otherwise.  With D = 3 the copy of plane x+2 is issued as soon as plane
+// x-1 is released; the copies of the several blocks resident on an SM
+// overlap each other's computation.  Per cell the sum of squares over the
+// fields comes first, then each field's new value from its own 7-point
+// Laplacian; Y neighbours are registers, X and Z neighbours are read from
+// shared memory (Z wraps across the row).  There is no Z halo, and the Y
+// halo costs 2 extra rows per R-row strip in reads only.
 #include "pf_async.cuh"
 #include "pf_device.cuh"
 #include "pf_internal.h"
@@ -48,39 +49,54 @@ static size_t ac3_smem(int R, int Z, int N, int D)
     return sizeof(float) * (((size_t)D * N * (R + 2) * Z + 1) & ~(size_t)1) + sizeof(uint64_t) * D;
 }
 
+#ifndef PF_AC3_FUNROLL
+#define PF_AC3_FUNROLL 2
+#endif
+constexpr int kAcFieldUnroll = PF_AC3_FUNROLL;   // fields updated per loop trip
+
+// A block is Zt x TY threads (Zt = Z rounded up to a warp), R = RT * TY rows:
+// thread (z, ty) owns cell z of rows ty*RT .. ty*RT+RT-1 of the strip.  ZT is
+// the row length when it is a compile-time constant (shared-memory and store
+// offsets become immediates), 0 when it is taken from the grid.  Shared
+// offsets are 32-bit.
+//
 // BULK: rows are a multiple of 16 bytes, and thread 0 stages each field's
 // rows with cp.async.bulk (transaction-counted mbarrier, one arrival).
-// Otherwise every thread copies its own cells with 4-byte cp.async and
-// arrives on the mbarrier when they land (one arrival per thread).
-template <int R, int MODEL, bool BULK>
+// Otherwise every thread copies cells with 4-byte cp.async and arrives on
+// the mbarrier when they land (one arrival per thread).
+template <int RT, int TY, int ZT, int MODEL, bool BULK>
 __global__ void __launch_bounds__(256)
 ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, AcF32 q, int planes, int N, int D,
                int* __restrict__ err)
 {
-    constexpr int RR = R + 2;
-    const int Z = g.Z;
-    const int t = threadIdx.x;
+    constexpr int R = RT * TY, RR = R + 2;
+    const int Z = ZT ? ZT : g.Z;
+    const int t = threadIdx.x, ty = TY > 1 ? threadIdx.y : 0;
+    const int tid = t + ty * blockDim.x;
     const bool on = t < Z;
     const int z = on ? t : 0;
     extern __shared__ __align__(128) unsigned char sm[];
     float* slots = reinterpret_cast<float*>(sm);
-    const size_t slot_elems = (size_t)N * RR * Z;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(slots + (((size_t)D * slot_elems + 1) & ~(size_t)1));
+    const int chunk = RR * Z;   // floats of one field's rows in a slot
+    const int slot_elems = N * chunk;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(slots + ((D * slot_elems + 1) & ~1));
 
     const int y0 = blockIdx.x * R;
     const int xs = blockIdx.y * planes;
     const int xe = min(xs + planes, g.X);
     if (xs >= xe) return;
-    const int zl = z == 0 ? Z - 1 : z - 1;
-    const int zh = z == Z - 1 ? 0 : z + 1;
-    const int x_first = xs - 1, x_last = xe;   // planes read from global memory
+    const int dl = z == 0 ? Z - 1 : -1;          // offset of the low Z neighbour
+    const int dh = z == Z - 1 ? 1 - Z : 1;       // offset of the high Z neighbour
+    const int x_first = xs - 1, x_last = xe;     // planes read from global memory
     const long long cells = g.cells;
+    const int nrows = min(RT, g.Y - y0 - ty * RT);   // rows of this thread inside the grid (may be <= 0)
+    const int me = z + ty * RT * Z;              // this thread's cell in the halo row above its rows
 
     // BULK: called by thread 0 only; otherwise by every thread
     auto fill = [&](int pl) {
         const int k = pl - x_first, s = k % D;
         uint64_t* bar = &bars[s];
-        float* dst0 = slots + (size_t)s * slot_elems;
+        float* dst0 = slots + s * slot_elems;
         const long long plane = (long long)wrapi(pl, g.X) * g.YZ;
         if constexpr (BULK) {
             const uint32_t row = (uint32_t)Z * sizeof(float);
@@ -89,7 +105,7 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
             const int a = y0 - 1, b = y0 + R + 1;
             for (int f = 0; f < N; f++) {
                 const float* base = ein + (long long)f * cells + plane;
-                float* dst = dst0 + (size_t)f * RR * Z;
+                float* dst = dst0 + f * chunk;
                 if (a >= 0 && b <= g.Y) {
                     bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
                 } else if (a < 0) {
@@ -98,33 +114,33 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
                 } else {
                     const int n1 = g.Y - a;
                     bulk_g2s(dst, base + (long long)a * Z, n1 * row, bar);
-                    bulk_g2s(dst + (size_t)n1 * Z, base, (RR - n1) * row, bar);
+                    bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
                 }
             }
         } else {
             if (on)
                 for (int f = 0; f < N; f++) {
                     const float* base = ein + (long long)f * cells + plane + z;
-                    float* dst = dst0 + (size_t)f * RR * Z + z;
-#pragma unroll
-                    for (int r = 0; r < RR; r++) cp_async4(dst + r * Z, base + (long long)wrapi(y0 - 1 + r, g.Y) * Z);
+                    float* dst = dst0 + f * chunk + z;
+                    for (int r = ty; r < RR; r += TY) cp_async4(dst + r * Z, base + (long long)wrapi(y0 - 1 + r, g.Y) * Z);
                 }
             cp_async_arrive(bar);
         }
     };
-    auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % D) * slot_elems; };
+    auto slot_of = [&](int pl) -> const float* { return slots + ((pl - x_first) % D) * slot_elems; };
     auto arrived = [&](int pl) {
         const int k = pl - x_first;
         return mbar_wait(&bars[k % D], (uint32_t)(k / D) & 1u);
     };
+    const bool producer = !BULK || tid == 0;
 
-    if (t == 0) {
-        for (int s = 0; s < D; s++) mbar_init(&bars[s], BULK ? 1 : blockDim.x);
+    if (tid == 0) {
+        for (int s = 0; s < D; s++) mbar_init(&bars[s], BULK ? 1 : blockDim.x * blockDim.y);
         mbar_fence_init();
     }
     __syncthreads();
     int issued = min(x_first + D - 1, x_last);   // last plane whose fill was issued
-    if (!BULK || t == 0)
+    if (producer)
         for (int pl = x_first; pl <= issued; pl++) fill(pl);
     bool bad = !arrived(x_first);
     bad |= !arrived(x_first + 1);
@@ -134,66 +150,96 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
 
     for (int x = xs; x < xe && !stop; x++) {
         bad = !arrived(x + 1);
-        const float* SL = slot_of(x - 1);
-        const float* SC = slot_of(x);
-        const float* SH = slot_of(x + 1);
-        float sum[R];
+        const float* SL = slot_of(x - 1) + me + Z;   // centre rows of the planes either side
+        const float* SH = slot_of(x + 1) + me + Z;
+        const float* SC = slot_of(x) + me;           // rows ty*RT .. ty*RT+RT+1 of plane x
+        float sum[RT];
 #pragma unroll
-        for (int r = 0; r < R; r++) sum[r] = 0.0f;
+        for (int i = 0; i < RT; i++) sum[i] = 0.0f;
 #pragma unroll 1
         for (int f = 0; f < N; f++) {
-            const float* c = SC + (size_t)f * RR * Z + z;
+            const float* c = SC + f * chunk + Z;
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-                const float v = c[(r + 1) * Z];
-                sum[r] = fmaf(v, v, sum[r]);
-            }
+            for (int i = 0; i < RT; i++) sum[i] = fmaf(c[i * Z], c[i * Z], sum[i]);
         }
-        const int rows = min(R, g.Y - y0);
-#pragma unroll 1
+        float* dst = eout + (long long)x * g.YZ + (long long)(y0 + ty * RT) * Z + z;
+#pragma unroll kAcFieldUnroll
         for (int f = 0; f < N; f++) {
-            const size_t fo = (size_t)f * RR * Z;
-            float col[RR];
+            const int fo = f * chunk;
+            float col[RT + 2];
 #pragma unroll
-            for (int r = 0; r < RR; r++) col[r] = SC[fo + r * Z + z];
-            float* dst = eout + (long long)f * cells + (long long)x * g.YZ + (long long)y0 * Z + z;
+            for (int i = 0; i < RT + 2; i++) col[i] = SC[fo + i * Z];
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-                const size_t o = fo + (size_t)(r + 1) * Z;
-                const float cc = col[r + 1];
-                const float sx = SL[o + z] + SH[o + z];
-                const float sy = col[r] + col[r + 2];
-                const float sz = SC[o + zl] + SC[o + zh];
+            for (int i = 0; i < RT; i++) {
+                const int o = fo + i * Z;
+                const float cc = col[i + 1];
+                const float sx = SL[o] + SH[o];
+                const float sy = col[i] + col[i + 2];
+                const float sz = SC[o + Z + dl] + SC[o + Z + dh];
                 const float lap = fmaf(q.wx, sx, fmaf(q.wy, sy, fmaf(q.wz, sz, -q.w2 * cc)));
-                if (on && r < rows) dst[(long long)r * Z] = ac_new_f32<MODEL>(cc, sum[r], lap, q);
+                if (on && i < nrows) dst[(long long)f * cells + i * Z] = ac_new_f32<MODEL>(cc, sum[i], lap, q);
             }
         }
         stop = __syncthreads_or(bad);
         if (!stop && x - 1 + D <= x_last) {   // the slot of x-1 is free now
-            if (!BULK || t == 0) fill(x - 1 + D);
+            if (producer) fill(x - 1 + D);
             issued = x - 1 + D;
         }
     }
     if (stop) {
-        if (t == 0) atomicExch(err, 1);
+        if (tid == 0) atomicExch(err, 1);
         // leave no copy in flight: wait (bounded) for the last fill of every slot
         for (int pl = max(x_first, issued - D + 1); pl <= issued; pl++) arrived(pl);
     }
 }
 
-template <int R, bool BULK>
-static const void* ac3_pick_model(int model)
+// Thread rows per block for a strip of R rows of Z cells and N fields.
+// Measured on 128^3 grids: two thread rows (twice the warps at the same
+// shared memory) win from 8 fields up (47 -> 41 us per step at N = 8,
+// 196 -> 142 us at N = 16) but lose at N = 4 and with per-thread copies
+// (rows that are not 16-byte multiples).
+static void ac3_threads(int R, int Z, int N, int* RT, int* TY)
 {
-    if (model == MMSP_GPU_AC) return (const void*)&ac3_stream_f32<R, MMSP_GPU_AC, BULK>;
-    if (model == MMSP_GPU_GG) return (const void*)&ac3_stream_f32<R, MMSP_GPU_GG, BULK>;
-    return (const void*)&ac3_stream_f32<R, MMSP_GPU_AC_POLY, BULK>;
+    const int zt = (Z + 31) / 32 * 32;
+#ifdef PF_AC3_TY
+    int ty = PF_AC3_TY;
+    (void)N;
+#else
+    int ty = (N > 4 && Z % 4 == 0) ? 2 : 1;
+#endif
+    if (R % ty || zt * ty > 256) ty = 1;
+    *TY = ty;
+    *RT = R / ty;
 }
 
-static const void* ac3_pick(int R, bool bulk, int model)
+template <int RT, int TY, int ZT, bool BULK>
+static const void* ac3_pick_model(int model)
 {
-    if (R == 4) return bulk ? ac3_pick_model<4, true>(model) : ac3_pick_model<4, false>(model);
-    if (R == 2) return bulk ? ac3_pick_model<2, true>(model) : ac3_pick_model<2, false>(model);
-    return bulk ? ac3_pick_model<1, true>(model) : ac3_pick_model<1, false>(model);
+    if (model == MMSP_GPU_AC) return (const void*)&ac3_stream_f32<RT, TY, ZT, MMSP_GPU_AC, BULK>;
+    if (model == MMSP_GPU_GG) return (const void*)&ac3_stream_f32<RT, TY, ZT, MMSP_GPU_GG, BULK>;
+    return (const void*)&ac3_stream_f32<RT, TY, ZT, MMSP_GPU_AC_POLY, BULK>;
+}
+
+template <int RT, int TY>
+static const void* ac3_pick_z(int Z, int model)
+{
+    if (Z % 4) return ac3_pick_model<RT, TY, 0, false>(model);
+    if (Z == 64) return ac3_pick_model<RT, TY, 64, true>(model);
+    if (Z == 128) return ac3_pick_model<RT, TY, 128, true>(model);
+    if (Z == 256) return ac3_pick_model<RT, TY, 256, true>(model);
+    return ac3_pick_model<RT, TY, 0, true>(model);
+}
+
+// nullptr for a shape without an instantiation
+static const void* ac3_pick(int RT, int TY, int Z, int model)
+{
+    if (TY == 2 && RT == 2) return ac3_pick_z<2, 2>(Z, model);
+    if (TY == 2 && RT == 1) return ac3_pick_z<1, 2>(Z, model);
+    if (TY != 1) return nullptr;
+    if (RT == 4) return ac3_pick_z<4, 1>(Z, model);
+    if (RT == 2) return ac3_pick_z<2, 1>(Z, model);
+    if (RT == 1) return ac3_pick_z<1, 1>(Z, model);
+    return nullptr;
 }
 
 constexpr size_t kAcSmemCap = 200 * 1024;
@@ -234,11 +280,14 @@ cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     int R = 4, D = 4;
     ac3_shape(g, d.fields, &R, &D);
-    const bool bulk = g.Z % 4 == 0;   // 16-byte rows
-    const int threads = (g.Z + 31) / 32 * 32;
-    p->fn = ac3_pick(R, bulk, d.model);
+    int RT, TY;
+    ac3_threads(R, g.Z, d.fields, &RT, &TY);
+    const int zt = (g.Z + 31) / 32 * 32;
+    const int threads = zt * TY;
+    p->fn = ac3_pick(RT, TY, g.Z, d.model);   // bulk copies when rows are 16-byte multiples
+    if (!p->fn) return cudaErrorInvalidConfiguration;
     p->smem = ac3_smem(R, g.Z, d.fields, D);
-    p->block = dim3(threads, 1, 1);
+    p->block = dim3(zt, TY, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;

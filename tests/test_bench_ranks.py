@@ -54,3 +54,14 @@ def test_reference_arm_prints_on_rank_zero_only():
                        capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_roofline_traffic_is_read_from_the_committed_profile():
+    """The DRAM traffic of the bench's dominant kernel comes from the ncu
+    summary under profiles/ (indented key lines included)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    t = bench.profile_traffic("ch3_stream_f32_256")
+    assert t is not None and 1e7 < t < 1e9
+    assert bench.profile_traffic("no_such_kernel") is None
