@@ -56,6 +56,7 @@ extern "C" {
 #define MMSP_GPU_ENOTFOUND    -7  /* unknown request id (server) */
 #define MMSP_GPU_ECANCELED    -8  /* request cancelled (server) */
 #define MMSP_GPU_ESTOPPED     -9  /* server stopped */
+#define MMSP_GPU_EIO         -10  /* a grid file could not be opened or written */
 
 /* Boundary-condition codes, identical to include/MMSP.utility.h:23-29. */
 #define MMSP_GPU_BC_MIRROR    0
@@ -169,6 +170,51 @@ const char* mmsp_gpu_last_error(const mmsp_gpu_handle* h);
  * download into `host`, destroy.  `stats` may be NULL. */
 int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t bytes, int layout,
                     int steps, mmsp_gpu_stats* stats);
+
+/* ---------------------------------------------------------------------------
+ * Output path: MMSP grid files.
+ *
+ * Replaces grid::output (include/MMSP.grid.cpp:1358-1402), write_buffer
+ * (include/MMSP.grid.cpp:1818-1909) and to_buffer (:1146-1157) of a serial
+ * run: the same ASCII header, one block, zlib payload, so the reference's
+ * grid::input (and mmsp2png / mmsp2tsv) read the files.  Payloads up to
+ * 1 MiB are compressed by one compress2 call as the reference does and are
+ * byte-identical to its files; larger payloads are deflated in 1 MiB pieces
+ * on several host threads and joined into one zlib stream (same data, other
+ * compressed bytes; independent of the thread count). */
+typedef struct mmsp_gpu_output_opts {
+    int level;        /* zlib level 1..9 (the reference writes 9); 0: uncompressed,
+                         as the reference's RAW build writes */
+    int threads;      /* host threads compressing one file; <= 0: every hardware thread */
+    int vector;       /* 1: grid<dim,vector<T>> cells (int32 N, then N values);
+                         0: scalar cells; < 0: vector when fields > 1 */
+    int fields_line;  /* the header's "fields" value; < 0: N for vector grids, 0 for
+                         scalar ones (the examples' generate() builds those with 0) */
+    int g0[3];        /* global lower corner per axis; the upper corner is g0 + n */
+} mmsp_gpu_output_opts;
+
+/* Defaults: level 9, all threads, vector when fields > 1, g0 = 0. */
+int mmsp_gpu_output_opts_init(mmsp_gpu_output_opts* opts);
+
+/* Write host values (layout as for mmsp_gpu_upload) as a grid file of
+ * `desc`'s shape, spacing and boundary codes.  Needs no device.  `opts`
+ * may be NULL.  Synchronous. */
+int mmsp_gpu_write_grid(const char* filename, const mmsp_gpu_desc* desc, const void* host, size_t bytes,
+                        int layout, const mmsp_gpu_output_opts* opts);
+
+/* Snapshot the handle's state, as ordered after the work queued so far,
+ * into `filename`.  The device packs the cells in to_buffer order (vector
+ * grids get their per-cell length) into a staging buffer on the handle's
+ * stream; the copy to pinned host memory runs on a second stream and the
+ * compression and file write on a host thread, so later steps overlap
+ * them.  Returns once the snapshot is queued; it blocks only while two
+ * earlier snapshots are still being written.  Allocates the staging buffer
+ * and two pinned host buffers on first use (held until mmsp_gpu_destroy). */
+int mmsp_gpu_output(mmsp_gpu_handle* h, const char* filename, const mmsp_gpu_output_opts* opts);
+
+/* Wait until every queued snapshot is on disk; returns the first failure
+ * among them (message in mmsp_gpu_last_error). */
+int mmsp_gpu_output_wait(mmsp_gpu_handle* h);
 
 /* ---------------------------------------------------------------------------
  * Batched form: many independent grids of uneven sizes and parameters

@@ -68,7 +68,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp"
-        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lz"])
         os.replace(tmp, LIB)
     return LIB
 

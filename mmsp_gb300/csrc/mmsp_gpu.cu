@@ -7,32 +7,12 @@
 #include <new>
 
 #include "MMSP.gpu.h"
+#include "pf_handle.h"
 #include "pf_internal.h"
 
 using pf::Coeffs;
 using pf::Geom;
 using pf::StepPlan;
-
-struct mmsp_gpu_handle {
-    mmsp_gpu_desc d;
-    Geom g;
-    Coeffs c;
-    StepPlan plan;
-    int device;
-    size_t esize, elems, bytes;
-    void* buf[2];
-    int cur;                 // buf[cur] holds the state
-    double* partials;        // reduction scratch
-    int* flags;              // device error word: a kernel's bounded wait ran out
-    cudaStream_t own;        // private stream
-    cudaStream_t stream;     // stream in use
-    cudaEvent_t ev0, ev1;
-    bool timed;              // ev0/ev1 bracket the last step call
-    int64_t steps;
-    // CUDA graph of kGraphSteps steps starting from buf[0] (an even count ends in buf[0])
-    cudaGraphExec_t graph;
-    char err[512];
-};
 
 static const int kGraphSteps = 64;
 static const int kGraphMin = 2 * kGraphSteps;   // replay only for runs this long
@@ -67,6 +47,7 @@ extern "C" const char* mmsp_gpu_strerror(int code)
     case MMSP_GPU_ENOTFOUND: return "unknown request";
     case MMSP_GPU_ECANCELED: return "cancelled";
     case MMSP_GPU_ESTOPPED: return "server stopped";
+    case MMSP_GPU_EIO: return "grid file could not be written";
     default: return "unknown status";
     }
 }
@@ -157,6 +138,7 @@ extern "C" int mmsp_gpu_footprint(const mmsp_gpu_desc* d, size_t* bytes)
 
 static void release(mmsp_gpu_handle* h)
 {
+    if (h->out) pf::output_release(h);   // waits for snapshots still being written
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);

@@ -1,0 +1,36 @@
+// pf_handle.h -- the handle behind mmsp_gpu_handle*, shared by the
+// translation units of the C ABI (steps in mmsp_gpu.cu, file output in
+// mmsp_gpu_output.cu).
+#pragma once
+
+#include "MMSP.gpu.h"
+#include "pf_internal.h"
+
+namespace pf {
+struct OutputState;
+// Wait for the handle's snapshots still being written, then free what the
+// output path allocated.
+void output_release(mmsp_gpu_handle* h);
+}  // namespace pf
+
+struct mmsp_gpu_handle {
+    mmsp_gpu_desc d;
+    pf::Geom g;
+    pf::Coeffs c;
+    pf::StepPlan plan;
+    int device;
+    size_t esize, elems, bytes;
+    void* buf[2];
+    int cur;                 // buf[cur] holds the state
+    double* partials;        // reduction scratch
+    int* flags;              // device error word: a kernel's bounded wait ran out
+    cudaStream_t own;        // private stream
+    cudaStream_t stream;     // stream in use
+    cudaEvent_t ev0, ev1;
+    bool timed;              // ev0/ev1 bracket the last step call
+    int64_t steps;
+    // CUDA graph of kGraphSteps steps starting from buf[0] (an even count ends in buf[0])
+    cudaGraphExec_t graph;
+    pf::OutputState* out;    // snapshot writer (mmsp_gpu_output), created on first use
+    char err[512];
+};

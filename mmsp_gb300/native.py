@@ -13,8 +13,8 @@ import numpy as np
 
 from . import build as _build
 
-OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED, ESTOPPED = \
-    0, -1, -2, -3, -4, -5, -6, -7, -8, -9
+OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED, ESTOPPED, EIO = \
+    0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10
 BC_MIRROR, BC_NEUMANN, BC_PERIODIC, BC_PARALLEL, BC_DIRICHLET = 0, 1, 2, 3, 4
 F64, F32 = 0, 1
 CH, CH_POLY, AC, GG, AC_POLY = 0, 1, 2, 3, 4
@@ -30,6 +30,7 @@ EXPORTS = [
     "mmsp_gpu_upload", "mmsp_gpu_download", "mmsp_gpu_upload_device", "mmsp_gpu_download_device",
     "mmsp_gpu_step", "mmsp_gpu_synchronize", "mmsp_gpu_reduce", "mmsp_gpu_state",
     "mmsp_gpu_last_error", "mmsp_gpu_update", "mmsp_gpu_step_noalloc",
+    "mmsp_gpu_output_opts_init", "mmsp_gpu_write_grid", "mmsp_gpu_output", "mmsp_gpu_output_wait",
     "mmsp_gpu_batch_create", "mmsp_gpu_batch_destroy", "mmsp_gpu_batch_set_stream", "mmsp_gpu_batch_upload",
     "mmsp_gpu_batch_download", "mmsp_gpu_batch_step", "mmsp_gpu_batch_synchronize", "mmsp_gpu_batch_reduce",
     "mmsp_gpu_batch_tune", "mmsp_gpu_batch_get_info", "mmsp_gpu_batch_last_error",
@@ -46,6 +47,11 @@ class Desc(ctypes.Structure):
                 ("dx", ctypes.c_double * 3), ("dt", ctypes.c_double), ("kappa", ctypes.c_double),
                 ("mobility", ctypes.c_double), ("gamma", ctypes.c_double), ("r", ctypes.c_double),
                 ("u", ctypes.c_double)]
+
+
+class OutputOpts(ctypes.Structure):
+    _fields_ = [("level", ctypes.c_int), ("threads", ctypes.c_int), ("vector", ctypes.c_int),
+                ("fields_line", ctypes.c_int), ("g0", ctypes.c_int * 3)]
 
 
 class Stats(ctypes.Structure):
@@ -123,6 +129,10 @@ def load(build_if_missing: bool = False):
         "mmsp_gpu_last_error": (ctypes.c_char_p, [vp]),
         "mmsp_gpu_update": (i, [dp, vp, sz, i, i, ctypes.POINTER(Stats)]),
         "mmsp_gpu_step_noalloc": (i, [dp, vp, vp, i, vp]),
+        "mmsp_gpu_output_opts_init": (i, [ctypes.POINTER(OutputOpts)]),
+        "mmsp_gpu_write_grid": (i, [ctypes.c_char_p, dp, vp, sz, i, ctypes.POINTER(OutputOpts)]),
+        "mmsp_gpu_output": (i, [vp, ctypes.c_char_p, ctypes.POINTER(OutputOpts)]),
+        "mmsp_gpu_output_wait": (i, [vp]),
         "mmsp_gpu_batch_create": (i, [ctypes.POINTER(vp), i, dp]),
         "mmsp_gpu_batch_destroy": (i, [vp]),
         "mmsp_gpu_batch_set_stream": (i, [vp, vp]),
@@ -258,12 +268,41 @@ class Stepper:
         _check(self.L.mmsp_gpu_state(self.h, ctypes.byref(p)), self.h, "state")
         return p.value
 
+    def output(self, filename: str, **opts):
+        """mmsp_gpu_output: queue a snapshot of the state as an MMSP grid file."""
+        o = output_opts(**opts)
+        _check(self.L.mmsp_gpu_output(self.h, os.fsencode(filename), ctypes.byref(o)), self.h, "output")
+
+    def output_wait(self):
+        _check(self.L.mmsp_gpu_output_wait(self.h), self.h, "output_wait")
+
     def upload_device(self, ptr: int, nbytes: int, layout: int = FIELD_MAJOR):
         _check(self.L.mmsp_gpu_upload_device(self.h, ctypes.c_void_p(ptr), nbytes, layout), self.h, "upload_device")
 
     def download_device(self, ptr: int, nbytes: int, layout: int = FIELD_MAJOR):
         _check(self.L.mmsp_gpu_download_device(self.h, ctypes.c_void_p(ptr), nbytes, layout), self.h,
                "download_device")
+
+
+def output_opts(level: int = 9, threads: int = 0, vector: int = -1, fields_line: int = -1, g0=None) -> OutputOpts:
+    """mmsp_gpu_output_opts_init, then overrides."""
+    o = OutputOpts()
+    load().mmsp_gpu_output_opts_init(ctypes.byref(o))
+    o.level, o.threads, o.vector, o.fields_line = int(level), int(threads), int(vector), int(fields_line)
+    for a, v in enumerate(g0 or []):
+        o.g0[a] = int(v)
+    return o
+
+
+def write_grid(filename: str, arr: np.ndarray, desc: Desc, layout: int = CELL_MAJOR, **opts):
+    """mmsp_gpu_write_grid: host values as an MMSP grid file (no device needed)."""
+    L = load()
+    a = np.ascontiguousarray(arr)
+    if a.dtype != (np.float64 if desc.dtype == F64 else np.float32):
+        raise ValueError("array dtype does not match the descriptor")
+    o = output_opts(**opts)
+    _check(L.mmsp_gpu_write_grid(os.fsencode(filename), ctypes.byref(desc), a.ctypes.data_as(ctypes.c_void_p),
+                                 a.nbytes, layout, ctypes.byref(o)), None, "write_grid")
 
 
 def update(arr: np.ndarray, steps: int, desc: Desc, layout: int = CELL_MAJOR):
