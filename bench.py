@@ -237,6 +237,44 @@ def other_configs(native, inputs, stream):
     return res
 
 
+def output_path(native, inputs):
+    """Snapshots of the 256^3 FP32 grid as MMSP grid files (zlib level 9, as
+    the reference writes them): three snapshots 100 steps apart through
+    mmsp_gpu_output, timed from the first step call until the last file is
+    on disk, against one compress2 call on one thread of the same payload
+    (the reference's write_buffer)."""
+    import shutil
+    import tempfile
+    import zlib
+
+    td = tempfile.mkdtemp(prefix="mmsp_out_")
+    try:
+        x = inputs.noisy_composition(SHAPE, MEAN, AMP, SEED).astype(np.float32)
+        d = native.make_desc(SHAPE, 1, np.float32, "ch", dt=DT, kappa=KAPPA, mobility=MOB)
+        with native.Stepper(d) as s:
+            s.upload(x)
+            s.output(os.path.join(td, "warm.dat"))   # first use allocates the buffers
+            s.output_wait()
+            t0 = time.perf_counter()
+            for i in range(3):
+                s.step(100)
+                s.output(os.path.join(td, "s%d.dat" % i))
+            s.output_wait()
+            wall = time.perf_counter() - t0
+            raw = s.download().tobytes()
+        size = os.path.getsize(os.path.join(td, "s2.dat"))
+        t1 = time.perf_counter()
+        zlib.compress(raw, 9)
+        ref = time.perf_counter() - t1
+    finally:
+        shutil.rmtree(td, ignore_errors=True)
+    return {"grid": "256^3 f32", "snapshots": 3, "steps_between": 100, "level": 9, "wall_s": wall,
+            "s_per_snapshot": wall / 3, "payload_mb": len(raw) / 1e6, "file_mb": size / 1e6,
+            "host_threads": os.cpu_count(), "reference_write_s": ref,
+            "reference_write": "one compress2 (zlib level 9) call on one thread, as write_buffer does",
+            "speedup_vs_reference_write": ref / (wall / 3)}
+
+
 def run_gpu(args):
     import torch
 
@@ -373,6 +411,8 @@ def run_gpu(args):
         "wall_s_timed_region": wall,
     }
     line["configs"] = other_configs(native, inputs, stream)
+    if rank == 0:
+        line["output"] = output_path(native, inputs)
     if rank == 0 and args.cpu_baseline:
         v, n, el = cpu_sample(1)
         line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
