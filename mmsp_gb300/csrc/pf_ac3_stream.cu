@@ -244,10 +244,14 @@ static const void* ac3_pick(int RT, int TY, int Z, int model)
 
 constexpr size_t kAcSmemCap = 200 * 1024;
 
-// Rows per strip and ring depth: the first pair whose shared memory fits.
-// Measured on 128^3 grids (N = 4, 8, 16 fields), more resident blocks beat a
-// deeper ring: a 3-plane ring (no plane in flight beyond the three being
-// read) with 4-row strips was fastest wherever it fit.
+// Blocks of `smem` bytes that fit the 228 KB of shared memory of an SM
+// (1 KB of each block's share is reserved by the hardware).
+static int ac3_blocks_per_sm(size_t smem) { return (int)((228u * 1024u) / (smem + 1024u)); }
+
+// Rows per strip and ring depth: the tallest strip (4, 2, 1 rows) whose
+// 3-slot ring fits.  4-row strips beat 2-row ones everywhere measured (the
+// Y halo is read twice as often with 2 rows), and more resident blocks beat
+// a deeper ring unless the ring already limits the SM to 2 blocks or fewer.
 static bool ac3_shape(const Geom& g, int N, int* R, int* D)
 {
 #if defined(PF_AC3_FORCE_R) && defined(PF_AC3_FORCE_D)
@@ -258,11 +262,16 @@ static bool ac3_shape(const Geom& g, int N, int* R, int* D)
     }
 #endif
     static const int kR[] = {4, 2, 1};
-    static const int kD[] = {3, 3, 3};
     for (int i = 0; i < 3; i++)
-        if (g.Y >= kR[i] + 2 && ac3_smem(kR[i], g.Z, N, kD[i]) <= kAcSmemCap) {
+        if (g.Y >= kR[i] + 2 && ac3_smem(kR[i], g.Z, N, 3) <= kAcSmemCap) {
             *R = kR[i];
-            *D = kD[i];
+            *D = 3;
+            // A fourth slot (one plane of copy lead per block) pays where the
+            // 3-slot ring already leaves at most 2 blocks per SM: measured
+            // 142 -> 129 us at 128^3 x 16 and 65 -> 53 us at 96x200x200 x 6,
+            // but 41 -> 43 us at 128^3 x 8 (3 blocks per SM with 3 slots).
+            if (ac3_blocks_per_sm(ac3_smem(kR[i], g.Z, N, 3)) <= 2 && ac3_smem(kR[i], g.Z, N, 4) <= kAcSmemCap)
+                *D = 4;
             return true;
         }
     return false;

@@ -329,7 +329,8 @@ def test_handles_of_one_kernel_with_different_shared_memory(gpu, oracle):
 AC_STREAM = [((6, 13, 32), 3, "ac"), ((9, 7, 64), 8, "ac"), ((5, 20, 128), 16, "ac"), ((3, 10, 256), 2, "gg"),
              ((7, 9, 32), 1, "ac_poly"), ((12, 6, 64), 5, "gg"),
              ((8, 11, 37), 4, "ac"), ((5, 9, 100), 8, "ac"), ((4, 6, 255), 3, "gg"), ((10, 3, 1), 2, "ac"),
-             ((6, 4, 3), 5, "ac_poly"), ((9, 5, 200), 6, "gg"), ((3, 17, 61), 16, "ac"), ((2, 7, 12), 2, "ac")]
+             ((6, 4, 3), 5, "ac_poly"), ((9, 5, 200), 6, "gg"), ((3, 17, 61), 16, "ac"), ((2, 7, 12), 2, "ac"),
+             ((7, 9, 150), 12, "ac"), ((6, 10, 200), 6, "gg")]   # 4-slot rings (per-thread / bulk copies)
 
 
 @pytest.mark.parametrize("shape,fields,model", AC_STREAM, ids=["%s-%d-%s" % ("x".join(map(str, s)), f, m) for s, f, m in AC_STREAM])
