@@ -80,6 +80,10 @@ extern "C" {
                                 e' = e - dt*(-e - e^3 + 2 (e sum e^2 - lap e))                */
 #define MMSP_GPU_AC_POLY  4  /* scalar Allen-Cahn as shipped (allen-cahn.cpp:70), fields=1:
                                 p' = p - dt*mobility*(-r p + u p^3 - kappa*lap p)             */
+#define MMSP_GPU_ZENER    5  /* isotropic phase-field Zener pinning as shipped
+                                (examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:121-138):
+                                MMSP_GPU_GG with field 0 (the particles) held fixed; the sum of
+                                squares still runs over every field                            */
 
 /* Host/device layouts of vector-valued grids (fields > 1). */
 #define MMSP_GPU_CELL_MAJOR  0  /* value j of cell i at i*fields + j (grid<dim,vector<T>> order) */
@@ -90,7 +94,7 @@ typedef struct mmsp_gpu_desc {
     int n[3];         /* extents per axis (x1-x0), axis 0 slowest; unused axes ignored */
     int fields;       /* values per cell: 1 for grid<dim,T>, N for grid<dim,vector<T>> */
     int dtype;        /* MMSP_GPU_F64 or MMSP_GPU_F32 */
-    int model;        /* MMSP_GPU_CH ... MMSP_GPU_AC_POLY */
+    int model;        /* MMSP_GPU_CH ... MMSP_GPU_ZENER */
     int bc[3][2];     /* lower/upper boundary per axis; the device path takes periodic only */
     double dx[3];     /* cell spacing per axis */
     double dt;        /* time step */

@@ -71,6 +71,13 @@ inline Model grain_growth_shipped(double dt)
     Model m = {MMSP_GPU_GG, dt, 2.0, 1.0, 1.0, 0.0, 0.0};
     return m;
 }
+// examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:113-138 as shipped:
+// grain growth with field 0 (the particles) held fixed
+inline Model zener_pinning_shipped(double dt)
+{
+    Model m = {MMSP_GPU_ZENER, dt, 2.0, 1.0, 1.0, 0.0, 0.0};
+    return m;
+}
 // allen-cahn.cpp:57-70 as shipped (scalar grid)
 inline Model allen_cahn_shipped(double r, double u, double K, double M, double dt)
 {

@@ -76,6 +76,7 @@ extern "C" int mmsp_gpu_desc_init(mmsp_gpu_desc* d, int dim, const int* n, int f
     case MMSP_GPU_AC: d->dt = 0.05; d->kappa = 2.0; d->gamma = 1.5; break;
     case MMSP_GPU_GG: d->dt = 0.01; d->kappa = 2.0; break;        // graingrowth.cpp:84
     case MMSP_GPU_AC_POLY: d->dt = 0.01; break;                   // allen-cahn.cpp:57-61
+    case MMSP_GPU_ZENER: d->dt = 0.01; d->kappa = 2.0; break;     // zener.cpp:115
     default: return MMSP_GPU_EINVAL;
     }
     return mmsp_gpu_validate(d);
@@ -87,7 +88,7 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     if (!d) BAD(MMSP_GPU_EINVAL, "NULL descriptor");
     if (d->dim < 1 || d->dim > 3) BAD(MMSP_GPU_EINVAL, "dim %d outside 1..3", d->dim);
     if (d->dtype != MMSP_GPU_F64 && d->dtype != MMSP_GPU_F32) BAD(MMSP_GPU_EINVAL, "dtype %d", d->dtype);
-    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_AC_POLY) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
+    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_ZENER) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
     long long cells = 1;
     for (int a = 0; a < d->dim; a++) {
         if (d->n[a] < 1) BAD(MMSP_GPU_EINVAL, "extent n[%d]=%d", a, d->n[a]);

@@ -78,7 +78,8 @@ ac_step_kernel(const T* __restrict__ ein, T* __restrict__ eout, Geom g, P<T> p, 
                 T y2 = twice(y);
                 T lap = lap_ref<T, UNIT_W, DIM>(y2, H[o], L[o], C[o + CW], C[o - CW], C[o + 1], C[o - 1], p.wx, p.wy,
                                                 p.wz);
-                dst[f * cells] = ac_new<T, MODEL>(y, sum, lap, p);
+                // Zener pinning: the particles (field 0) have zero mobility (zener.cpp:134)
+                dst[f * cells] = (MODEL == MMSP_GPU_ZENER && f == 0) ? y : ac_new<T, MODEL>(y, sum, lap, p);
             }
         }
     };
@@ -120,6 +121,7 @@ static const void* ac_pick_model(int model, int ty, bool unit)
 {
     if (model == MMSP_GPU_AC) return ac_pick_ty<T, DIM, MMSP_GPU_AC>(ty, unit);
     if (model == MMSP_GPU_GG) return ac_pick_ty<T, DIM, MMSP_GPU_GG>(ty, unit);
+    if (model == MMSP_GPU_ZENER) return ac_pick_ty<T, DIM, MMSP_GPU_ZENER>(ty, unit);
     return ac_pick_ty<T, DIM, MMSP_GPU_AC_POLY>(ty, unit);
 }
 

@@ -33,7 +33,7 @@ static __device__ __forceinline__ float ac_new_f32(float c, float sum, float lap
         // -c + c^3 + 2 gamma c (sum - c^2) - kappa lap
         const float df = c * fmaf(q.gamma2, sum - c2, c2 - 1.0f);
         return fmaf(-q.dtm, fmaf(-q.kappa, lap, df), c);
-    } else if (MODEL == MMSP_GPU_GG) {
+    } else if (MODEL == MMSP_GPU_GG || MODEL == MMSP_GPU_ZENER) {
         // -c - c^3 + 2 (c sum - lap)
         const float e = fmaf(2.0f, fmaf(c, sum, -lap), -c * fmaf(c, c, 1.0f));
         return fmaf(-q.dtm, e, c);
@@ -177,7 +177,9 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
                 const float sy = col[i] + col[i + 2];
                 const float sz = SC[o + Z + dl] + SC[o + Z + dh];
                 const float lap = fmaf(q.wx, sx, fmaf(q.wy, sy, fmaf(q.wz, sz, -q.w2 * cc)));
-                if (on && i < nrows) dst[(long long)f * cells + i * Z] = ac_new_f32<MODEL>(cc, sum[i], lap, q);
+                // Zener pinning: the particles (field 0) have zero mobility
+                const float v = (MODEL == MMSP_GPU_ZENER && f == 0) ? cc : ac_new_f32<MODEL>(cc, sum[i], lap, q);
+                if (on && i < nrows) dst[(long long)f * cells + i * Z] = v;
             }
         }
         stop = __syncthreads_or(bad);
@@ -217,6 +219,7 @@ static const void* ac3_pick_model(int model)
 {
     if (model == MMSP_GPU_AC) return (const void*)&ac3_stream_f32<RT, TY, ZT, MMSP_GPU_AC, BULK>;
     if (model == MMSP_GPU_GG) return (const void*)&ac3_stream_f32<RT, TY, ZT, MMSP_GPU_GG, BULK>;
+    if (model == MMSP_GPU_ZENER) return (const void*)&ac3_stream_f32<RT, TY, ZT, MMSP_GPU_ZENER, BULK>;
     return (const void*)&ac3_stream_f32<RT, TY, ZT, MMSP_GPU_AC_POLY, BULK>;
 }
 
@@ -281,7 +284,8 @@ bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
     int R, D;
     return d.dtype == MMSP_GPU_F32 && g.dim == 3 && g.Z <= 256 &&
-           (d.model == MMSP_GPU_AC || d.model == MMSP_GPU_GG || d.model == MMSP_GPU_AC_POLY) &&
+           (d.model == MMSP_GPU_AC || d.model == MMSP_GPU_GG || d.model == MMSP_GPU_AC_POLY ||
+            d.model == MMSP_GPU_ZENER) &&
            ac3_shape(g, d.fields, &R, &D);
 }
 

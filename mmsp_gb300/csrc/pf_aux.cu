@@ -63,7 +63,7 @@ Coeffs make_coeffs(const mmsp_gpu_desc& d)
     c.gamma2 = 2.0 * d.gamma;
     c.neg_r = -d.r;
     c.u = d.u;
-    c.dtm = d.model == MMSP_GPU_GG ? d.dt : d.dt * d.mobility;
+    c.dtm = (d.model == MMSP_GPU_GG || d.model == MMSP_GPU_ZENER) ? d.dt : d.dt * d.mobility;
     return c;
 }
 
@@ -209,12 +209,13 @@ cudaError_t launch_reduce(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c
     RedArgs a{};
     for (int k = 0; k < d.dim; k++) a.wg[3 - d.dim + k] = c.wg[k];
     a.kappa = d.kappa;
-    a.gamma = d.model == MMSP_GPU_GG ? 1.0 : d.gamma;
+    const bool gg = d.model == MMSP_GPU_GG || d.model == MMSP_GPU_ZENER;
+    a.gamma = gg ? 1.0 : d.gamma;
     a.r = d.r;
     a.u = d.u;
     a.model = d.model;
     int N = d.fields;
-    if (d.model == MMSP_GPU_GG) a.kappa = 2.0;   // graingrowth.cpp:105: lap enters as 2*lap
+    if (gg) a.kappa = 2.0;   // graingrowth.cpp:105, zener.cpp:135: lap enters as 2*lap
     if (d.dtype == MMSP_GPU_F64)
         reduce_kernel<double><<<kReduceBlocks, 256, 0, s>>>((const double*)state, g, N, a, partials);
     else

@@ -134,8 +134,8 @@ static __device__ __forceinline__ T ac_new(T phi, T sum, T lap, const P<T>& p)
         T g = A::mul(A::mul(p.gamma2, phi), A::sub(sum, p2));
         T c = A::sub(A::add(a, g), kappa_times(p.kappa, lap));
         return A::sub(phi, A::mul(p.dtm, c));
-    } else if (MODEL == MMSP_GPU_GG) {
-        // phi - dt*(-phi - pow(phi,3) + 2.0*(phi*sum - lap))   (graingrowth.cpp:105)
+    } else if (MODEL == MMSP_GPU_GG || MODEL == MMSP_GPU_ZENER) {
+        // phi - dt*(-phi - pow(phi,3) + 2.0*(phi*sum - lap))   (graingrowth.cpp:105, zener.cpp:135)
         T e = A::add(A::sub(-phi, cube(phi)), twice(A::sub(A::mul(phi, sum), lap)));
         return A::sub(phi, A::mul(p.dtm, e));
     } else {

@@ -105,3 +105,24 @@ def graingrowth_circles(shape, fields: int = 2) -> np.ndarray:
     eta[..., 0] = np.where(inside, 0.0, 1.0)
     eta[..., 1] = np.where(inside, 1.0, 0.0)
     return eta
+
+
+def zener_particles(shape, particles: int, seed: int) -> np.ndarray:
+    """The shipped Zener-pinning start state
+    (examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:14-95),
+    with seeded positions: field 0 holds the particles, fields 1 and 2 the
+    matrix grain and the period-64 circles of graingrowth_circles; each
+    particle sets a 3-cell cube (3 cells per axis, wrapped periodically)
+    to (1, 0, 0)."""
+    shape = tuple(int(s) for s in shape)
+    eta = np.zeros(shape + (3,), dtype=np.float64)
+    eta[..., 1:] = graingrowth_circles(shape, 2)
+    n = int(np.prod(shape))
+    centre = (uniform(seed, particles) * n).astype(np.int64)
+    for c in centre:
+        x = np.unravel_index(int(c), shape)
+        offs = np.indices((3,) * len(shape)).reshape(len(shape), -1).T - 1
+        for o in offs:
+            p = tuple((xi + oi) % si for xi, oi, si in zip(x, o, shape))
+            eta[p] = (1.0, 0.0, 0.0)
+    return eta

@@ -17,10 +17,10 @@ OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED
     0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10
 BC_MIRROR, BC_NEUMANN, BC_PERIODIC, BC_PARALLEL, BC_DIRICHLET = 0, 1, 2, 3, 4
 F64, F32 = 0, 1
-CH, CH_POLY, AC, GG, AC_POLY = 0, 1, 2, 3, 4
+CH, CH_POLY, AC, GG, AC_POLY, ZENER = 0, 1, 2, 3, 4, 5
 CELL_MAJOR, FIELD_MAJOR = 0, 1
 
-MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY}
+MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY, "zener": ZENER}
 DTYPES = {np.dtype(np.float64): F64, np.dtype(np.float32): F32}
 
 # Every symbol include/MMSP.gpu.h declares (checked by the CPU test suite).

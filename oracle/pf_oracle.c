@@ -207,7 +207,10 @@ int pfo_ch_shipped(const pfo_grid* g, double* c, int steps,
 
 /* Single-pass multi-field Allen-Cahn in the structure of graingrowth.cpp:86-110.
  * form 0: BASELINE free energy with gamma; form 1: graingrowth.cpp:105 as
- * shipped; form 2: allen-cahn.cpp:70 as shipped (N must be 1). */
+ * shipped; form 2: allen-cahn.cpp:70 as shipped (N must be 1); form 3:
+ * isotropic phase-field Zener pinning as shipped
+ * (examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:121-138):
+ * form 1 with field 0 (the particles) copied unchanged. */
 static int ac_run(const pfo_grid* g, int N, double* eta, int steps, int form,
                   double gamma, double kappa, double L, double r, double u,
                   double dt, int threads)
@@ -247,6 +250,7 @@ static int ac_run(const pfo_grid* g, int N, double* eta, int steps, int form,
                     } else {
                         for (int j = 0; j < N; j++)
                             out[j] = phi[j] - dt * (-phi[j] - pow(phi[j], 3) + 2.0 * (phi[j] * sum - lap[j]));
+                        if (form == 3) out[0] = phi[0];   /* particles have zero mobility (zener.cpp:134) */
                     }
                 }
         double* t = old;
@@ -272,6 +276,11 @@ int pfo_ac_graingrowth(const pfo_grid* g, int N, double* eta, int steps,
                        double dt, int threads)
 {
     return ac_run(g, N, eta, steps, 1, 0.0, 0.0, 1.0, 0.0, 0.0, dt, threads);
+}
+
+int pfo_ac_zener(const pfo_grid* g, int N, double* eta, int steps, double dt, int threads)
+{
+    return ac_run(g, N, eta, steps, 3, 0.0, 0.0, 1.0, 0.0, 0.0, dt, threads);
 }
 
 int pfo_ac_scalar_shipped(const pfo_grid* g, double* phi, int steps,

@@ -74,6 +74,12 @@ int pfo_ac_baseline(const pfo_grid* g, int N, double* eta, int steps,
 int pfo_ac_graingrowth(const pfo_grid* g, int N, double* eta, int steps,
                        double dt, int threads);
 
+/* Isotropic phase-field Zener pinning exactly as shipped
+ * (examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:121-138):
+ * grain growth with field 0, the particles, held fixed; the sum of squares
+ * still runs over every field. */
+int pfo_ac_zener(const pfo_grid* g, int N, double* eta, int steps, double dt, int threads);
+
 /* Scalar Allen-Cahn exactly as shipped (allen-cahn.cpp:70):
  *   p' = p - dt*M*(-r*p + u*pow(p,3) - K*lap(p)). */
 int pfo_ac_scalar_shipped(const pfo_grid* g, double* phi, int steps,

@@ -45,6 +45,7 @@ def lib():
             ("pfo_ch_shipped", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int]),
             ("pfo_ac_baseline", [gp, ctypes.c_int, dp, ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int]),
             ("pfo_ac_graingrowth", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+            ("pfo_ac_zener", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
             ("pfo_ac_scalar_shipped", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int]),
             ("pfo_laplacian", [gp, dp, dp]),
             ("pfo_ch_mass_energy", [gp, dp, ctypes.c_double, dp, dp]),
@@ -108,6 +109,14 @@ def ac_graingrowth(eta, steps, dt=0.01, dx=None, bc=None, threads=0):
     g = _grid(out.shape[:-1], dx, bc)
     _check(lib().pfo_ac_graingrowth(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps), dt, threads),
            "ac_graingrowth")
+    return out
+
+
+def ac_zener(eta, steps, dt=0.01, dx=None, bc=None, threads=0):
+    """Zener pinning as shipped: grain growth with field 0 (particles) fixed."""
+    out = np.array(eta, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape[:-1], dx, bc)
+    _check(lib().pfo_ac_zener(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps), dt, threads), "ac_zener")
     return out
 
 

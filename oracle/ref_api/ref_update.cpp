@@ -8,6 +8,7 @@
 //   examples/phase_transitions/cahn-hilliard/explicit/cahn-hilliard.cpp:47-81
 //   examples/coarsening/grain_growth/isotropic/phase_field/graingrowth.cpp:73-111
 //   examples/phase_transitions/allen-cahn/allen-cahn.cpp:47-75
+//   examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:103-143
 // The "shipped" models are those loops with the examples' own expressions;
 // the "baseline" models substitute f(c)=c^2(1-c)^2 for Cahn-Hilliard and
 // f = sum(-e^2/2+e^4/4) + gamma*sum_{i<j} e_i^2 e_j^2 for grain growth, with
@@ -18,6 +19,7 @@
 //   ch_shipped       r u K M dt
 //   ac_baseline      gamma kappa L dt
 //   graingrowth      dt
+//   zener            dt
 //   ac_scalar        r u K M dt
 // Prints "update_seconds <t>" (std::chrono around update() only).
 #include "MMSP.hpp"
@@ -103,6 +105,33 @@ template <int dim> void gg_update(grid<dim, vector<double> >& oldGrid, int steps
 	}
 }
 
+// examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:103-143
+// with dt from the command line.
+template <int dim> void zener_update(grid<dim, vector<double> >& oldGrid, int steps,
+                                     const std::vector<double>& p)
+{
+	ghostswap(oldGrid);
+	grid<dim, vector<double> > newGrid(oldGrid);
+	double dt = p[0];
+	for (int step = 0; step < steps; step++) {
+		for (int i = 0; i < nodes(oldGrid); i++) {
+			vector<double> lap = laplacian(oldGrid, i);
+			double sum = 0.0;
+			for (int j = 0; j < fields(oldGrid); j++) {
+				double phi = oldGrid(i)[j];
+				sum += phi * phi;
+			}
+			for (int j = 0; j < fields(oldGrid); j++) {
+				double phi = oldGrid(i)[j];
+				if (j == 0) newGrid(i)[j] = phi;
+				else newGrid(i)[j] = phi - dt * (-phi - pow(phi, 3) + 2.0 * (phi * sum - lap[j]));
+			}
+		}
+		swap(oldGrid, newGrid);
+		ghostswap(oldGrid);
+	}
+}
+
 } // namespace MMSP
 
 static double now_s()
@@ -133,6 +162,7 @@ template <int dim> int run_vector(const std::string& model, const char* in, cons
 	double t0 = now_s();
 	if (model == "ac_baseline") MMSP::gg_update(g, steps, false, p);
 	else if (model == "graingrowth") MMSP::gg_update(g, steps, true, p);
+	else if (model == "zener") MMSP::zener_update(g, steps, p);
 	else return 2;
 	double t1 = now_s();
 	std::printf("update_seconds %.9f\n", t1 - t0);
@@ -151,7 +181,7 @@ int main(int argc, char* argv[])
 	std::vector<double> p;
 	for (int i = 5; i < argc; i++) p.push_back(std::atof(argv[i]));
 	size_t need = (model == "ch_baseline") ? 3 : (model == "ch_shipped" || model == "ac_scalar") ? 5
-	            : (model == "ac_baseline") ? 4 : (model == "graingrowth") ? 1 : 0;
+	            : (model == "ac_baseline") ? 4 : (model == "graingrowth" || model == "zener") ? 1 : 0;
 	if (need == 0 || p.size() != need) {
 		std::cerr << "bad model or parameter count" << std::endl;
 		return 1;

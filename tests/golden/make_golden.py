@@ -54,6 +54,8 @@ SMALL = [
     ("ac3d_baseline_n3", "ac_baseline", (8, 9, 10), 3, ("voronoi", 9, 21), (1.2, 1.5, 0.8, 0.04), 25, {}),
     ("gg2d_shipped", "graingrowth", (64, 64), 2, ("circles",), (0.01,), 100, {}),
     ("gg3d_shipped", "graingrowth", (36, 36, 4), 2, ("circles",), (0.01,), 40, {}),
+    ("zener2d_shipped", "zener", (64, 64), 3, ("zener", 40, 22), (0.01,), 100, {}),
+    ("zener3d_shipped", "zener", (24, 24, 12), 3, ("zener", 30, 23), (0.01,), 40, {}),
 ]
 
 
@@ -67,6 +69,9 @@ def start_state(shape, fields, spec):
         return inputs.voronoi_grains(shape, pts, fields, seed)
     if kind == "circles":
         return inputs.graingrowth_circles(shape, fields)
+    if kind == "zener":
+        _, particles, seed = spec
+        return inputs.zener_particles(shape, particles, seed)
     raise ValueError(kind)
 
 
@@ -93,8 +98,10 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
 
 
-def make_small():
+def make_small(only=None):
     for name, model, shape, fields, spec, params, steps, extra in SMALL:
+        if only and name not in only:
+            continue
         x0 = start_state(shape, fields, spec)
         vector = fields > 0
         out, secs = run_ref(model, x0, vector, fields, steps, params, extra.get("dx"), extra.get("bc"))
@@ -163,9 +170,10 @@ def make_full():
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--full", action="store_true")
+    ap.add_argument("--only", nargs="*", help="names of the small fixtures to (re)make")
     args = ap.parse_args()
     if not pf_oracle.ref_available():
         sys.exit("build the reference program first: make -C oracle ref")
-    make_small()
+    make_small(set(args.only) if args.only else None)
     if args.full:
         make_full()

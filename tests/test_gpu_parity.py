@@ -36,6 +36,8 @@ def desc_for(native, model, params, shape, fields, dtype, dx=None, bc=None):
         return native.make_desc(shape, fields, dtype, "ac", gamma=p[0], kappa=p[1], mobility=p[2], dt=p[3], **kw)
     if model == "graingrowth":
         return native.make_desc(shape, fields, dtype, "gg", dt=p[0], **kw)
+    if model == "zener":
+        return native.make_desc(shape, fields, dtype, "zener", dt=p[0], **kw)
     raise ValueError(model)
 
 
@@ -55,7 +57,7 @@ def test_fp64_matches_reference_fixture(gpu, path):
     z = np.load(path)
     model = str(z["model"])
     x = z["start"]
-    vector = model in ("ac_baseline", "graingrowth")
+    vector = model in ("ac_baseline", "graingrowth", "zener")
     shape = x.shape[:-1] if vector else x.shape
     fields = x.shape[-1] if vector else 1
     bc = z["bc"].tolist()
@@ -330,7 +332,8 @@ AC_STREAM = [((6, 13, 32), 3, "ac"), ((9, 7, 64), 8, "ac"), ((5, 20, 128), 16, "
              ((7, 9, 32), 1, "ac_poly"), ((12, 6, 64), 5, "gg"),
              ((8, 11, 37), 4, "ac"), ((5, 9, 100), 8, "ac"), ((4, 6, 255), 3, "gg"), ((10, 3, 1), 2, "ac"),
              ((6, 4, 3), 5, "ac_poly"), ((9, 5, 200), 6, "gg"), ((3, 17, 61), 16, "ac"), ((2, 7, 12), 2, "ac"),
-             ((7, 9, 150), 12, "ac"), ((6, 10, 200), 6, "gg")]   # 4-slot rings (per-thread / bulk copies)
+             ((7, 9, 150), 12, "ac"), ((6, 10, 200), 6, "gg"),   # 4-slot rings (per-thread / bulk copies)
+             ((8, 12, 64), 3, "zener"), ((5, 9, 45), 6, "zener")]
 
 
 @pytest.mark.parametrize("shape,fields,model", AC_STREAM, ids=["%s-%d-%s" % ("x".join(map(str, s)), f, m) for s, f, m in AC_STREAM])
@@ -348,9 +351,12 @@ def test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, m
             d = gpu.make_desc(shape, fields, np.float32, "ac", gamma=1.5, kappa=2.0, mobility=1.0, dt=0.05,
                               dx=[1.0, 1.1, 0.9])
             want = oracle.ac_baseline(x, steps, 1.5, 2.0, 1.0, 0.05, dx=[1.0, 1.1, 0.9])
-        else:
+        elif model == "gg":
             d = gpu.make_desc(shape, fields, np.float32, "gg", dt=0.01)
             want = oracle.ac_graingrowth(x, steps, 0.01)
+        else:
+            d = gpu.make_desc(shape, fields, np.float32, "zener", dt=0.01)
+            want = oracle.ac_zener(x, steps, 0.01)
     got = run_gpu(gpu, d, x.astype(np.float32), steps).astype(np.float64)
     assert np.abs(got - want).max() <= TOL_F32
     assert np.abs(want - x).max() > 1e-3
@@ -374,3 +380,20 @@ def test_fp32_rows_kernel_against_fp64_oracle(gpu, oracle, shape):
     want = oracle.ch_baseline(c0, steps, 1.2, 0.9, dt, dx=[1.0, 1.1, 0.95][: len(shape)])
     assert np.abs(got - want).max() <= TOL_F32
     assert np.abs(want - c0).max() > 1e-4
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("shape", [(40, 36), (20, 16, 64), (9, 11, 37)])
+def test_zener_particles_do_not_move(gpu, oracle, dtype, shape):
+    """Zener pinning: field 0 (the particles) is copied bit for bit every step
+    while the grains (fields 1, 2) evolve around it (zener.cpp:134)."""
+    from mmsp_gb300 import inputs
+
+    x = inputs.zener_particles(shape, 12, 40 + len(shape)).astype(dtype)
+    d = gpu.make_desc(shape, 3, dtype, "zener", dt=0.01)
+    got = run_gpu(gpu, d, x, 60)
+    assert np.array_equal(got[..., 0], x[..., 0])
+    want = oracle.ac_zener(x.astype(np.float64), 60, 0.01)
+    tol = TOL_SHIPPED if dtype == np.float64 else TOL_F32
+    assert np.abs(got.astype(np.float64) - want).max() <= tol * max(1.0, np.abs(want).max())
+    assert np.abs(want[..., 1:] - x[..., 1:]).max() > 1e-3

@@ -36,6 +36,8 @@ def run_oracle(o, z, x=None, steps=None):
         return o.ac_baseline(x, st, *p, dx=dx, bc=bc)
     if m == "graingrowth":
         return o.ac_graingrowth(x, st, *p, dx=dx, bc=bc)
+    if m == "zener":
+        return o.ac_zener(x, st, *p, dx=dx, bc=bc)
     raise ValueError(m)
 
 
