@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define MMSP_GPU_ABI_VERSION 1
+#define MMSP_GPU_ABI_VERSION 2
 
 /* Status codes. */
 #define MMSP_GPU_OK            0
@@ -84,6 +84,18 @@ extern "C" {
                                 (examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:121-138):
                                 MMSP_GPU_GG with field 0 (the particles) held fixed; the sum of
                                 squares still runs over every field                            */
+#define MMSP_GPU_OSTWALD  6  /* isotropic phase-field Ostwald ripening as shipped
+                                (examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:56-123),
+                                fields >= 2: field 0 the composition C, fields 1.. the order
+                                parameters e_i; two passes per step:
+                                w   = -A(C-Cm) + B(C-Cm)^3 + Da(C-Ca)^3 + Db(C-Cb)^3
+                                      - g (C-Ca) sum e_i^2 - kappa lap C
+                                C'  = C + dt*D*lap w
+                                e_i'= e_i - dt*L*(-g (C-Ca)^2 + delta e_i^3 + eps e_i (sum - e_i^2)
+                                      - kappa lap e_i)
+                                with Cm = (Ca+Cb)/2, B = A/(Cb-Cm)^2, g = 2/(Cb-Ca)^2,
+                                Da = Db = g/delta^2 (ostwald.cpp:67-80); L = mobility;
+                                D, Ca, Cb, A, delta, eps in aux[0..5]                         */
 
 /* Host/device layouts of vector-valued grids (fields > 1). */
 #define MMSP_GPU_CELL_MAJOR  0  /* value j of cell i at i*fields + j (grid<dim,vector<T>> order) */
@@ -94,7 +106,7 @@ typedef struct mmsp_gpu_desc {
     int n[3];         /* extents per axis (x1-x0), axis 0 slowest; unused axes ignored */
     int fields;       /* values per cell: 1 for grid<dim,T>, N for grid<dim,vector<T>> */
     int dtype;        /* MMSP_GPU_F64 or MMSP_GPU_F32 */
-    int model;        /* MMSP_GPU_CH ... MMSP_GPU_ZENER */
+    int model;        /* MMSP_GPU_CH ... MMSP_GPU_OSTWALD */
     int bc[3][2];     /* lower/upper boundary per axis; the device path takes periodic only */
     double dx[3];     /* cell spacing per axis */
     double dt;        /* time step */
@@ -102,6 +114,7 @@ typedef struct mmsp_gpu_desc {
     double mobility;  /* M (Cahn-Hilliard) or L (Allen-Cahn) */
     double gamma;     /* grain-boundary coupling (MMSP_GPU_AC) */
     double r, u;      /* polynomial coefficients (MMSP_GPU_CH_POLY, MMSP_GPU_AC_POLY) */
+    double aux[6];    /* further model parameters: MMSP_GPU_OSTWALD takes D, Ca, Cb, A, delta, eps */
 } mmsp_gpu_desc;
 
 typedef struct mmsp_gpu_stats {
@@ -225,6 +238,8 @@ int mmsp_gpu_output_wait(mmsp_gpu_handle* h);
  * advanced together.  The reference has no batched path (one update() per
  * grid, cahn-hilliard.cpp:47-81); this replaces a loop of those calls.
  *
+ * MMSP_GPU_OSTWALD grids are not batched (EUNSUPPORTED); handles and the
+ * server take them.
  * 2D Cahn-Hilliard grids (MMSP_GPU_CH / MMSP_GPU_CH_POLY, fields=1) whose
  * rows hold a multiple of 32 cells up to 512 share one persistent kernel per
  * step: a work list of (grid, run of rows) items is drained by all warps of
@@ -351,7 +366,8 @@ int mmsp_gpu_server_stop(mmsp_gpu_server* s);
  * out.  The first call on a device looks up the array's device address
  * with that device current; make that first call before any stream capture.
  * Calls that overlap on the GPU (from several threads or streams) share the
- * scratch array and race: serialise them. */
+ * scratch array and race: serialise them.  MMSP_GPU_OSTWALD, whose step
+ * needs a work grid beside the state, returns MMSP_GPU_EUNSUPPORTED. */
 int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, void* out, int steps,
                           void* cuda_stream);
 

@@ -45,6 +45,7 @@ namespace gpu {
 struct Model {
     int model;
     double dt, kappa, mobility, gamma, r, u;
+    double aux[6];   // further parameters (mmsp_gpu_desc.aux); zero unless the model takes them
 };
 
 // f = c^2(1-c)^2: mu = 2c(1-c)(1-2c) - kappa*lap c; dc/dt = M lap mu
@@ -76,6 +77,15 @@ inline Model grain_growth_shipped(double dt)
 inline Model zener_pinning_shipped(double dt)
 {
     Model m = {MMSP_GPU_ZENER, dt, 2.0, 1.0, 1.0, 0.0, 0.0};
+    return m;
+}
+// examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:56-123 as shipped,
+// on grid<dim,vector<T> > with field 0 the composition and fields 1.. the order parameters
+inline Model ostwald_ripening_shipped(double dt = 0.001, double L = 1.0, double D = 1.0, double Calpha = 0.05,
+                                      double Cbeta = 0.95, double A = 2.0, double delta = 1.0,
+                                      double epsilon = 3.0, double kappa = 2.0)
+{
+    Model m = {MMSP_GPU_OSTWALD, dt, kappa, L, 1.0, 0.0, 0.0, {D, Calpha, Cbeta, A, delta, epsilon}};
     return m;
 }
 // allen-cahn.cpp:57-70 as shipped (scalar grid)
@@ -111,6 +121,7 @@ int describe(const G& g, int dim, int fields, int dtype, const Model& m, mmsp_gp
     d->gamma = m.gamma;
     d->r = m.r;
     d->u = m.u;
+    for (int k = 0; k < 6; k++) d->aux[k] = m.aux[k];
     return mmsp_gpu_validate(d);
 }
 

@@ -77,6 +77,16 @@ extern "C" int mmsp_gpu_desc_init(mmsp_gpu_desc* d, int dim, const int* n, int f
     case MMSP_GPU_GG: d->dt = 0.01; d->kappa = 2.0; break;        // graingrowth.cpp:84
     case MMSP_GPU_AC_POLY: d->dt = 0.01; break;                   // allen-cahn.cpp:57-61
     case MMSP_GPU_ZENER: d->dt = 0.01; d->kappa = 2.0; break;     // zener.cpp:115
+    case MMSP_GPU_OSTWALD:                                        // ostwald.cpp:66-80
+        d->dt = 0.001;
+        d->kappa = 2.0;
+        d->aux[0] = 1.0;    // D
+        d->aux[1] = 0.05;   // Calpha
+        d->aux[2] = 0.95;   // Cbeta
+        d->aux[3] = 2.0;    // A
+        d->aux[4] = 1.0;    // delta
+        d->aux[5] = 3.0;    // epsilon
+        break;
     default: return MMSP_GPU_EINVAL;
     }
     return mmsp_gpu_validate(d);
@@ -88,7 +98,7 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     if (!d) BAD(MMSP_GPU_EINVAL, "NULL descriptor");
     if (d->dim < 1 || d->dim > 3) BAD(MMSP_GPU_EINVAL, "dim %d outside 1..3", d->dim);
     if (d->dtype != MMSP_GPU_F64 && d->dtype != MMSP_GPU_F32) BAD(MMSP_GPU_EINVAL, "dtype %d", d->dtype);
-    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_ZENER) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
+    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_OSTWALD) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
     long long cells = 1;
     for (int a = 0; a < d->dim; a++) {
         if (d->n[a] < 1) BAD(MMSP_GPU_EINVAL, "extent n[%d]=%d", a, d->n[a]);
@@ -105,6 +115,11 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     bool scalar_model = d->model == MMSP_GPU_CH || d->model == MMSP_GPU_CH_POLY || d->model == MMSP_GPU_AC_POLY;
     if (scalar_model && d->fields != 1) BAD(MMSP_GPU_EINVAL, "model %d takes fields=1, got %d", d->model, d->fields);
     if (d->fields < 1) BAD(MMSP_GPU_EINVAL, "fields=%d", d->fields);
+    if (d->model == MMSP_GPU_OSTWALD && d->fields < 2)
+        BAD(MMSP_GPU_EINVAL, "Ostwald ripening takes a composition and at least one order parameter, fields=%d",
+            d->fields);
+    if (d->model == MMSP_GPU_OSTWALD && (!(d->aux[2] != d->aux[1]) || !(d->aux[4] != 0.0)))
+        BAD(MMSP_GPU_EINVAL, "Ostwald ripening needs Calpha != Cbeta and delta != 0");
     if (d->fields > 32) BAD(MMSP_GPU_EUNSUPPORTED, "fields=%d above 32", d->fields);
     long long yz = 1;
     for (int a = (d->dim >= 2 ? d->dim - 2 : 0); a < d->dim; a++) yz *= d->n[a];
@@ -128,12 +143,20 @@ static size_t state_bytes(const mmsp_gpu_desc* d)
     return n * esize_of(d);
 }
 
+// Device scratch of a model beyond the two state buffers: the Ostwald
+// model's chemical-potential grid (one value per cell).
+static size_t work_bytes(const mmsp_gpu_desc* d)
+{
+    if (d->model != MMSP_GPU_OSTWALD) return 0;
+    return state_bytes(d) / (size_t)d->fields;
+}
+
 extern "C" int mmsp_gpu_footprint(const mmsp_gpu_desc* d, size_t* bytes)
 {
     int rc = mmsp_gpu_validate(d);
     if (rc) return rc;
     if (!bytes) return MMSP_GPU_EINVAL;
-    *bytes = 2 * state_bytes(d) + pf::kPartialsBytes;
+    *bytes = 2 * state_bytes(d) + pf::kPartialsBytes + work_bytes(d);
     return MMSP_GPU_OK;
 }
 
@@ -146,6 +169,7 @@ static void release(mmsp_gpu_handle* h)
     if (h->buf[0]) cudaFree(h->buf[0]);
     if (h->buf[1]) cudaFree(h->buf[1]);
     if (h->partials) cudaFree(h->partials);
+    if (h->work) cudaFree(h->work);
     if (h->flags) cudaFree(h->flags);
     if (h->own) cudaStreamDestroy(h->own);
 }
@@ -153,7 +177,8 @@ static void release(mmsp_gpu_handle* h)
 static int make_plan(mmsp_gpu_handle* h)
 {
     bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
-    cudaError_t e = ch ? pf::plan_ch(h->d, h->g, &h->plan) : pf::plan_ac(h->d, h->g, &h->plan);
+    cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::plan_ostwald(h->d, h->g, &h->plan)
+                    : ch ? pf::plan_ch(h->d, h->g, &h->plan) : pf::plan_ac(h->d, h->g, &h->plan);
     if (e != cudaSuccess) {
         if (!h->plan.ok && !ch) return fail(h, MMSP_GPU_EUNSUPPORTED, "%s", "too many fields for shared memory");
         return cuda_fail(h, e, "plan");
@@ -190,7 +215,8 @@ extern "C" int mmsp_gpu_create(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc)
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) goto cuda_err;
     if (cudaMalloc(&h->buf[0], h->bytes) != cudaSuccess || cudaMalloc(&h->buf[1], h->bytes) != cudaSuccess ||
         cudaMalloc((void**)&h->partials, pf::kPartialsBytes) != cudaSuccess ||
-        cudaMalloc((void**)&h->flags, 256) != cudaSuccess || cudaMemset(h->flags, 0, 256) != cudaSuccess) {
+        cudaMalloc((void**)&h->flags, 256) != cudaSuccess || cudaMemset(h->flags, 0, 256) != cudaSuccess ||
+        (work_bytes(&h->d) && cudaMalloc(&h->work, work_bytes(&h->d)) != cudaSuccess)) {
         cudaGetLastError();
         release(h);
         delete h;
@@ -311,8 +337,9 @@ static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s)
     bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
     const void* in = h->buf[h->cur];
     void* out = h->buf[h->cur ^ 1];
-    cudaError_t e = ch ? pf::launch_ch(h->plan, h->d, h->g, h->c, in, out, h->flags, s)
-                       : pf::launch_ac(h->plan, h->d, h->g, h->c, in, out, h->flags, s);
+    cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, h->c, in, out, h->work, s)
+                    : ch ? pf::launch_ch(h->plan, h->d, h->g, h->c, in, out, h->flags, s)
+                         : pf::launch_ac(h->plan, h->d, h->g, h->c, in, out, h->flags, s);
     h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913
     return e;
 }

@@ -64,6 +64,23 @@ Coeffs make_coeffs(const mmsp_gpu_desc& d)
     c.neg_r = -d.r;
     c.u = d.u;
     c.dtm = (d.model == MMSP_GPU_GG || d.model == MMSP_GPU_ZENER) ? d.dt : d.dt * d.mobility;
+    if (d.model == MMSP_GPU_OSTWALD) {
+        // ostwald.cpp:67-80, with the same pow calls
+        OstConst& o = c.ost;
+        o.Ca = d.aux[1];
+        o.Cb = d.aux[2];
+        o.Cm = 0.5 * (o.Ca + o.Cb);
+        o.A = d.aux[3];
+        o.B = o.A / pow(o.Cb - o.Cm, 2);
+        o.g = 2.0 / pow(o.Cb - o.Ca, 2);
+        o.delta = d.aux[4];
+        o.eps = d.aux[5];
+        o.Da = o.g / pow(o.delta, 2);
+        o.Db = o.g / pow(o.delta, 2);
+        o.kappa = d.kappa;
+        o.dtD = d.dt * d.aux[0];
+        o.dtL = d.dt * d.mobility;
+    }
     return c;
 }
 
@@ -95,6 +112,7 @@ static __device__ __forceinline__ NS ncombine(NS a, NS b)
 struct RedArgs {
     double wg[3];          // gradient weights of padded axes X, Y, Z (0 for padding)
     double kappa, gamma, r, u;
+    OstConst ost;
     int model;
 };
 
@@ -147,6 +165,28 @@ __global__ void __launch_bounds__(256) reduce_kernel(const T* __restrict__ st, G
             }
             nadd(e, f + 0.5 * a.kappa * gsq(st, g, a, x, y, z));
             nadd(m, C);
+        } else if (a.model == MMSP_GPU_OSTWALD) {
+            // f = -A/2 (C-Cm)^2 + B/4 (C-Cm)^4 + Da/4 (C-Ca)^4 + Db/4 (C-Cb)^4 - g/2 (C-Ca)^2 sum e^2
+            //     + delta/4 sum e^4 + eps/2 sum_{i<j} e_i^2 e_j^2 + kappa/2 sum over all fields |grad|^2,
+            // whose C-derivative is the chemical potential of ostwald.cpp:97-99
+            const OstConst& o = a.ost;
+            const double C = (double)st[i];
+            const double dm = C - o.Cm, da = C - o.Ca, db = C - o.Cb;
+            double grad = gsq(st, g, a, x, y, z), sq = 0.0, quart = 0.0, pair = 0.0;
+            nadd(m, C);
+            for (int j = 1; j < N; j++) {
+                const T* f = st + (long long)j * g.cells;
+                const double p = (double)f[i];
+                const double p2 = p * p;
+                quart += p2 * p2;
+                pair += p2 * sq;
+                sq += p2;
+                grad += gsq(f, g, a, x, y, z);
+                nadd(m, p);
+            }
+            const double dm2 = dm * dm, da2 = da * da, db2 = db * db;
+            nadd(e, -0.5 * o.A * dm2 + 0.25 * o.B * dm2 * dm2 + 0.25 * o.Da * da2 * da2 + 0.25 * o.Db * db2 * db2 -
+                        0.5 * o.g * da2 * sq + 0.25 * o.delta * quart + 0.5 * o.eps * pair + 0.5 * o.kappa * grad);
         } else {
             double bulk = 0.0, pair = 0.0, grad = 0.0, sq = 0.0;
             for (int j = 0; j < N; j++) {
@@ -214,6 +254,7 @@ cudaError_t launch_reduce(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c
     a.r = d.r;
     a.u = d.u;
     a.model = d.model;
+    a.ost = c.ost;
     int N = d.fields;
     if (gg) a.kappa = 2.0;   // graingrowth.cpp:105, zener.cpp:135: lap enters as 2*lap
     if (d.dtype == MMSP_GPU_F64)

@@ -23,6 +23,7 @@ struct mmsp_gpu_handle {
     void* buf[2];
     int cur;                 // buf[cur] holds the state
     double* partials;        // reduction scratch
+    void* work;              // MMSP_GPU_OSTWALD: the chemical-potential grid (cells values)
     int* flags;              // device error word: a kernel's bounded wait ran out
     cudaStream_t own;        // private stream
     cudaStream_t stream;     // stream in use

@@ -19,6 +19,13 @@ struct Geom {
     long long cells;   // X*Y*Z
 };
 
+// Constants of the Ostwald-ripening model, derived from the descriptor as
+// ostwald.cpp:67-80 derives them (Cm, B, gamma, Da, Db).
+struct OstConst {
+    double Cm, Ca, Cb, A, B, Da, Db, g, delta, eps, kappa;
+    double dtD, dtL;   // dt*D and dt*L, as the update multiplies them (ostwald.cpp:108,117)
+};
+
 // Model constants in double; the launchers narrow them to the state type.
 struct Coeffs {
     double w[3];       // 1/(dx*dx) per real axis, MMSP axis order (grid.cpp:2062)
@@ -30,6 +37,7 @@ struct Coeffs {
     double gamma;      // gamma (energy)
     double dV;         // cell volume
     bool unit_w;       // every w == 1.0 exactly
+    OstConst ost;      // MMSP_GPU_OSTWALD
 };
 
 Geom make_geom(const mmsp_gpu_desc& d);
@@ -48,7 +56,7 @@ struct StepPlan {
     int planes;        // planes of axis X per block (3D streaming)
     int fields;
     int kind;          // 0: generic tile kernel, 1: FP32 3D CH streaming, 2: FP32 3D AC streaming,
-                       // 3: FP32 CH rows of any length
+                       // 3: FP32 CH rows of any length, 4: Ostwald ripening (two kernels)
     int ring;          // planes in the shared-memory ring (streaming kernels)
     bool ok;
 };
@@ -81,6 +89,12 @@ cudaError_t launch_ch(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, 
                       const void* in, void* out, int* err, cudaStream_t s);
 cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
                       const void* in, void* out, int* err, cudaStream_t s);
+
+// Ostwald ripening (pf_ostwald.cu): the chemical potential of the
+// composition into `work` (cells values), then the update of every field.
+cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
+cudaError_t launch_ostwald(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
+                           const void* in, void* out, void* work, cudaStream_t s);
 
 // Reductions: partial sums of (mass, energy) per block into `partials`
 // (4 doubles per block: mass sum, mass compensation, energy sum, energy

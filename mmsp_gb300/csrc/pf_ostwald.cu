@@ -1,0 +1,203 @@
+// pf_ostwald.cu -- explicit Ostwald-ripening step, two kernels per step.
+//
+// The reference's update (examples/coarsening/ostwald_ripening/isotropic/
+// phase_field/ostwald.cpp:84-122) makes two passes over the grid: the
+// chemical potential of the composition C (field 0) into a scalar work grid
+// (:89-100), ghostswap, then the new composition from the Laplacian of that
+// grid and the new order parameters (fields 1..N-1) from their own
+// Laplacians (:103-120).  Here each pass is one kernel over all cells, the
+// work grid is a device buffer of the handle, and the periodic halo is index
+// arithmetic.  Neighbour values come through the L1/L2 caches: the state of
+// the shipped examples (a few fields of at most 128 x 64 x 16 cells) stays
+// in L2, so the passes are bound by FP64 arithmetic, not by DRAM.
+//
+// FP64 follows the reference's operation order with separately rounded
+// operations (pow(x,3) as the compensated cube of pf_device.cuh, pow(x,2)
+// as x*x); FP32 uses the same expressions in float.
+#include "pf_device.cuh"
+#include "pf_internal.h"
+
+namespace pf {
+
+template <typename T> struct OstP {
+    T wx, wy, wz;
+    T Cm, Ca, Cb, negA, B, Da, Db, g, neg_g, delta, eps, kappa, dtD, dtL;
+};
+
+template <typename T>
+static OstP<T> ost_narrow(const Coeffs& c, int dim)
+{
+    const P<T> w = narrow<T>(c, dim);
+    const OstConst& o = c.ost;
+    OstP<T> p;
+    p.wx = w.wx;
+    p.wy = w.wy;
+    p.wz = w.wz;
+    p.Cm = (T)o.Cm;
+    p.Ca = (T)o.Ca;
+    p.Cb = (T)o.Cb;
+    p.negA = (T)(-o.A);
+    p.B = (T)o.B;
+    p.Da = (T)o.Da;
+    p.Db = (T)o.Db;
+    p.g = (T)o.g;
+    p.neg_g = (T)(-o.g);
+    p.delta = (T)o.delta;
+    p.eps = (T)o.eps;
+    p.kappa = (T)o.kappa;
+    p.dtD = (T)o.dtD;
+    p.dtL = (T)o.dtL;
+    return p;
+}
+
+// Offsets of the six periodic neighbours of cell i (padded axes X, Y, Z).
+struct Nb {
+    long long xh, xl, yh, yl, zh, zl;
+};
+
+static __device__ __forceinline__ Nb neighbours(const Geom& g, long long i)
+{
+    const int x = (int)(i / g.YZ);
+    const long long r = i - (long long)x * g.YZ;
+    const int y = (int)(r / g.Z);
+    const int z = (int)(r - (long long)y * g.Z);
+    Nb n;
+    n.xh = (x + 1 == g.X ? -(long long)x : 1LL) * g.YZ;
+    n.xl = (x == 0 ? (long long)(g.X - 1) : -1LL) * g.YZ;
+    n.yh = (y + 1 == g.Y ? -(long long)y : 1LL) * g.Z;
+    n.yl = (y == 0 ? (long long)(g.Y - 1) : -1LL) * g.Z;
+    n.zh = z + 1 == g.Z ? -(long long)z : 1LL;
+    n.zl = z == 0 ? (long long)(g.Z - 1) : -1LL;
+    return n;
+}
+
+template <typename T, int DIM, bool UNIT>
+static __device__ __forceinline__ T lap_at(const T* __restrict__ f, long long i, const Nb& n, const OstP<T>& p)
+{
+    return lap_ref<T, UNIT, DIM>(twice(f[i]), f[i + n.xh], f[i + n.xl], f[i + n.yh], f[i + n.yl], f[i + n.zh],
+                                 f[i + n.zl], p.wx, p.wy, p.wz);
+}
+
+// sum_{j>=1} pow(e_j,2), ostwald.cpp:91-93 (0.0 + x == x for x >= 0)
+template <typename T>
+static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long i, long long cells, int N)
+{
+    using A = Ar<T>;
+    T sum = T(0);
+    for (int j = 1; j < N; j++) {
+        const T e = s[(long long)j * cells + i];
+        sum = j == 1 ? A::mul(e, e) : A::add(sum, A::mul(e, e));
+    }
+    return sum;
+}
+
+// Pass 1, ostwald.cpp:95-99:
+//   w = -A*(C-Cm) + B*pow(C-Cm,3) + Da*pow(C-Ca,3) + Db*pow(C-Cb,3) - g*(C-Ca)*sum - kappa*lap C
+template <typename T, int DIM, bool UNIT>
+__global__ void __launch_bounds__(256)
+ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
+{
+    using A = Ar<T>;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g.cells;
+         i += (long long)gridDim.x * blockDim.x) {
+        const Nb n = neighbours(g, i);
+        const T sum = order_sum(s, i, g.cells, N);
+        const T C = s[i];
+        const T lap = lap_at<T, DIM, UNIT>(s, i, n, p);
+        const T dm = A::sub(C, p.Cm), da = A::sub(C, p.Ca), db = A::sub(C, p.Cb);
+        T v = A::mul(p.negA, dm);
+        v = A::add(v, A::mul(p.B, cube(dm)));
+        v = A::add(v, A::mul(p.Da, cube(da)));
+        v = A::add(v, A::mul(p.Db, cube(db)));
+        v = A::sub(v, A::mul(A::mul(p.g, da), sum));
+        w[i] = A::sub(v, kappa_times(p.kappa, lap));
+    }
+}
+
+// Pass 2, ostwald.cpp:103-120:
+//   C'   = C + dt*D*lap w
+//   e_j' = e_j - dt*L*(-g*pow(C-Ca,2) + delta*pow(e_j,3) + eps*e_j*(sum - pow(e_j,2)) - kappa*lap e_j)
+template <typename T, int DIM, bool UNIT>
+__global__ void __launch_bounds__(256)
+ostwald_update(const T* __restrict__ s, const T* __restrict__ w, T* __restrict__ out, Geom g, OstP<T> p, int N)
+{
+    using A = Ar<T>;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g.cells;
+         i += (long long)gridDim.x * blockDim.x) {
+        const Nb n = neighbours(g, i);
+        const T C = s[i];
+        out[i] = A::add(C, A::mul(p.dtD, lap_at<T, DIM, UNIT>(w, i, n, p)));
+        const T sum = order_sum(s, i, g.cells, N);
+        const T da = A::sub(C, p.Ca);
+        const T t1 = A::mul(p.neg_g, A::mul(da, da));
+        for (int j = 1; j < N; j++) {
+            const T* f = s + (long long)j * g.cells;
+            const T e = f[i];
+            T v = A::add(t1, A::mul(p.delta, cube(e)));
+            v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
+            v = A::sub(v, kappa_times(p.kappa, lap_at<T, DIM, UNIT>(f, i, n, p)));
+            out[(long long)j * g.cells + i] = A::sub(e, A::mul(p.dtL, v));
+        }
+    }
+}
+
+template <typename T, int DIM, bool UNIT>
+static void ost_fns(const void** mu, const void** up)
+{
+    *mu = (const void*)&ostwald_mu<T, DIM, UNIT>;
+    *up = (const void*)&ostwald_update<T, DIM, UNIT>;
+}
+
+template <typename T>
+static void ost_pick(int dim, bool unit, const void** mu, const void** up)
+{
+    if (dim == 3) unit ? ost_fns<T, 3, true>(mu, up) : ost_fns<T, 3, false>(mu, up);
+    else if (dim == 2) unit ? ost_fns<T, 2, true>(mu, up) : ost_fns<T, 2, false>(mu, up);
+    else unit ? ost_fns<T, 1, true>(mu, up) : ost_fns<T, 1, false>(mu, up);
+}
+
+cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
+{
+    const Coeffs c = make_coeffs(d);
+    const void* up = nullptr;
+    if (d.dtype == MMSP_GPU_F64) ost_pick<double>(g.dim, c.unit_w, &p->fn, &up);
+    else ost_pick<float>(g.dim, c.unit_w, &p->fn, &up);
+    long long blocks = (g.cells + 255) / 256;
+    const long long most = 8LL * sm_count();   // grid-stride beyond 8 blocks per SM
+    if (blocks > most) blocks = most;
+    p->grid = dim3((unsigned)blocks, 1, 1);
+    p->block = dim3(256, 1, 1);
+    p->smem = 0;
+    p->planes = 1;
+    p->fields = d.fields;
+    p->kind = 4;
+    p->ring = 0;
+    p->ok = true;
+    return cudaSuccess;
+}
+
+cudaError_t launch_ostwald(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
+                           const void* in, void* out, void* work, cudaStream_t s)
+{
+    const void* mu = nullptr;
+    const void* up = nullptr;
+    int n = d.fields;
+    Geom gg = g;
+    cudaError_t e;
+    if (d.dtype == MMSP_GPU_F64) {
+        ost_pick<double>(g.dim, c.unit_w, &mu, &up);
+        OstP<double> q = ost_narrow<double>(c, g.dim);
+        void* a1[] = {(void*)&in, (void*)&work, (void*)&gg, (void*)&q, (void*)&n};
+        if ((e = cudaLaunchKernel(mu, p.grid, p.block, a1, 0, s)) != cudaSuccess) return e;
+        void* a2[] = {(void*)&in, (void*)&work, (void*)&out, (void*)&gg, (void*)&q, (void*)&n};
+        return cudaLaunchKernel(up, p.grid, p.block, a2, 0, s);
+    }
+    ost_pick<float>(g.dim, c.unit_w, &mu, &up);
+    OstP<float> q = ost_narrow<float>(c, g.dim);
+    void* a1[] = {(void*)&in, (void*)&work, (void*)&gg, (void*)&q, (void*)&n};
+    if ((e = cudaLaunchKernel(mu, p.grid, p.block, a1, 0, s)) != cudaSuccess) return e;
+    void* a2[] = {(void*)&in, (void*)&work, (void*)&out, (void*)&gg, (void*)&q, (void*)&n};
+    return cudaLaunchKernel(up, p.grid, p.block, a2, 0, s);
+}
+
+}  // namespace pf

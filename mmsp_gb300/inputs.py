@@ -126,3 +126,20 @@ def zener_particles(shape, particles: int, seed: int) -> np.ndarray:
             p = tuple((xi + oi) % si for xi, oi, si in zip(x, o, shape))
             eta[p] = (1.0, 0.0, 0.0)
     return eta
+
+
+def ostwald_start(shape, fields: int, seed: int) -> np.ndarray:
+    """The shipped Ostwald-ripening start state
+    (examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:13-54),
+    with a seeded stream: composition r ~ U(0, 1) per cell and the first
+    order parameter 1 - r; further order parameters (beyond the example's
+    two fields) start at 0.1 * U(0, 1)."""
+    shape = tuple(int(s) for s in shape)
+    n = int(np.prod(shape))
+    eta = np.zeros(shape + (fields,), dtype=np.float64)
+    r = uniform(seed, n).reshape(shape)
+    eta[..., 0] = r
+    eta[..., 1] = 1.0 - r
+    for j in range(2, fields):
+        eta[..., j] = 0.1 * uniform(seed, n, start=j * n).reshape(shape)
+    return eta

@@ -17,10 +17,12 @@ OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED
     0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10
 BC_MIRROR, BC_NEUMANN, BC_PERIODIC, BC_PARALLEL, BC_DIRICHLET = 0, 1, 2, 3, 4
 F64, F32 = 0, 1
-CH, CH_POLY, AC, GG, AC_POLY, ZENER = 0, 1, 2, 3, 4, 5
+CH, CH_POLY, AC, GG, AC_POLY, ZENER, OSTWALD = 0, 1, 2, 3, 4, 5, 6
 CELL_MAJOR, FIELD_MAJOR = 0, 1
 
-MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY, "zener": ZENER}
+MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY, "zener": ZENER,
+          "ostwald": OSTWALD}
+OSTWALD_AUX = ("D", "Calpha", "Cbeta", "A", "delta", "epsilon")   # mmsp_gpu_desc.aux of MMSP_GPU_OSTWALD
 DTYPES = {np.dtype(np.float64): F64, np.dtype(np.float32): F32}
 
 # Every symbol include/MMSP.gpu.h declares (checked by the CPU test suite).
@@ -46,7 +48,7 @@ class Desc(ctypes.Structure):
                 ("dtype", ctypes.c_int), ("model", ctypes.c_int), ("bc", (ctypes.c_int * 2) * 3),
                 ("dx", ctypes.c_double * 3), ("dt", ctypes.c_double), ("kappa", ctypes.c_double),
                 ("mobility", ctypes.c_double), ("gamma", ctypes.c_double), ("r", ctypes.c_double),
-                ("u", ctypes.c_double)]
+                ("u", ctypes.c_double), ("aux", ctypes.c_double * 6)]
 
 
 class OutputOpts(ctypes.Structure):
@@ -169,8 +171,9 @@ def strerror(code: int) -> str:
 
 
 def make_desc(shape, fields=1, dtype=np.float64, model="ch", dx=None, bc=None, dt=None, kappa=None,
-              mobility=None, gamma=None, r=None, u=None) -> Desc:
-    """A descriptor with the model's defaults (mmsp_gpu_desc_init), then overrides."""
+              mobility=None, gamma=None, r=None, u=None, **aux) -> Desc:
+    """A descriptor with the model's defaults (mmsp_gpu_desc_init), then overrides.
+    Ostwald-ripening parameters go by name (D, Calpha, Cbeta, A, delta, epsilon)."""
     L = load()
     shape = tuple(int(s) for s in shape)
     d = Desc()
@@ -188,6 +191,10 @@ def make_desc(shape, fields=1, dtype=np.float64, model="ch", dx=None, bc=None, d
     for name, v in (("dt", dt), ("kappa", kappa), ("mobility", mobility), ("gamma", gamma), ("r", r), ("u", u)):
         if v is not None:
             setattr(d, name, float(v))
+    for name, v in aux.items():
+        if name not in OSTWALD_AUX:
+            raise TypeError("unknown model parameter %r" % name)
+        d.aux[OSTWALD_AUX.index(name)] = float(v)
     return d
 
 

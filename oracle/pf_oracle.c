@@ -290,6 +290,78 @@ int pfo_ac_scalar_shipped(const pfo_grid* g, double* phi, int steps,
     return ac_run(g, 1, phi, steps, 2, 0.0, K, M, r, u, dt, threads);
 }
 
+/* Isotropic phase-field Ostwald ripening, ostwald.cpp:84-121: field 0 the
+ * composition C, fields 1..N-1 the order parameters.  Pass 1 writes the
+ * chemical potential into a scalar work grid (:89-100); pass 2 updates C
+ * from its Laplacian and each order parameter from its own (:103-120).
+ * The derived constants follow :67-80 with the same pow calls. */
+int pfo_ostwald(const pfo_grid* g, int N, double* eta, int steps, double dt, double L, double D,
+                double Calpha, double Cbeta, double A, double delta, double epsilon, double kappa,
+                int threads)
+{
+    geo q;
+    if (N < 2 || N > 64 || geo_init(&q, g) || !eta || steps < 0) return -1;
+    const double Cmatrix = 0.5 * (Calpha + Cbeta);
+    const double B = A / pow(Cbeta - Cmatrix, 2);
+    const double gamma = 2.0 / pow(Cbeta - Calpha, 2);
+    const double Dalpha = gamma / pow(delta, 2);
+    const double Dbeta = gamma / pow(delta, 2);
+    double* nw = (double*)malloc(sizeof(double) * (size_t)q.cells * (size_t)N);
+    double* w = (double*)malloc(sizeof(double) * (size_t)q.cells);
+    if (!nw || !w) { free(nw); free(w); geo_free(&q); return -1; }
+    double* old = eta;
+    int nt = nthreads(threads);
+    (void)nt;
+    for (int step = 0; step < steps; step++) {
+        #pragma omp parallel for schedule(static) num_threads(nt)
+        for (int i0 = 0; i0 < q.n[0]; i0++)
+            for (int i1 = 0; i1 < q.n[1]; i1++)
+                for (int i2 = 0; i2 < q.n[2]; i2++) {
+                    int xc[3] = {i0, i1, i2};
+                    long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                    const double* phi = old + i * N;
+                    double sum = 0.0;
+                    for (int j = 1; j < N; j++) sum += pow(phi[j], 2);
+                    double C = phi[0];
+                    double lap = lap_at(&q, old, i, N, 0, xc);
+                    w[i] = -A * (C - Cmatrix) + B * pow(C - Cmatrix, 3)
+                           + Dalpha * pow(C - Calpha, 3) + Dbeta * pow(C - Cbeta, 3)
+                           - gamma * (C - Calpha) * sum - kappa * lap;
+                }
+        #pragma omp parallel for schedule(static) num_threads(nt)
+        for (int i0 = 0; i0 < q.n[0]; i0++)
+            for (int i1 = 0; i1 < q.n[1]; i1++)
+                for (int i2 = 0; i2 < q.n[2]; i2++) {
+                    int xc[3] = {i0, i1, i2};
+                    long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                    const double* phi = old + i * N;
+                    double* out = nw + i * N;
+                    double lap = lap_at(&q, w, i, 1, 0, xc);
+                    double C = phi[0];
+                    out[0] = C + dt * D * lap;
+                    double sum = 0.0;
+                    for (int j = 1; j < N; j++) sum += pow(phi[j], 2);
+                    for (int j = 1; j < N; j++) {
+                        double value = phi[j];
+                        double vlap = lap_at(&q, old, i, N, j, xc);
+                        out[j] = value - dt * L * (-gamma * pow(C - Calpha, 2) + delta * pow(value, 3)
+                                                   + epsilon * value * (sum - pow(value, 2)) - kappa * vlap);
+                    }
+                }
+        double* t = old;
+        old = nw;
+        nw = t;
+    }
+    if (old != eta) {
+        memcpy(eta, old, sizeof(double) * (size_t)q.cells * (size_t)N);
+        nw = old;
+    }
+    free(nw);
+    free(w);
+    geo_free(&q);
+    return 0;
+}
+
 /* Neumaier's improvement of Kahan summation. */
 typedef struct { double s, c; } nsum;
 static inline void nadd(nsum* a, double x)

@@ -80,6 +80,14 @@ int pfo_ac_graingrowth(const pfo_grid* g, int N, double* eta, int steps,
  * still runs over every field. */
 int pfo_ac_zener(const pfo_grid* g, int N, double* eta, int steps, double dt, int threads);
 
+/* Isotropic phase-field Ostwald ripening exactly as shipped
+ * (examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:84-121),
+ * with the constants of :66-80 as arguments.  eta is cell-major with N >= 2
+ * values per cell: the composition first, then the order parameters. */
+int pfo_ostwald(const pfo_grid* g, int N, double* eta, int steps, double dt, double L, double D,
+                double Calpha, double Cbeta, double A, double delta, double epsilon, double kappa,
+                int threads);
+
 /* Scalar Allen-Cahn exactly as shipped (allen-cahn.cpp:70):
  *   p' = p - dt*M*(-r*p + u*pow(p,3) - K*lap(p)). */
 int pfo_ac_scalar_shipped(const pfo_grid* g, double* phi, int steps,

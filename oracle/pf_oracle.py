@@ -46,6 +46,7 @@ def lib():
             ("pfo_ac_baseline", [gp, ctypes.c_int, dp, ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int]),
             ("pfo_ac_graingrowth", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
             ("pfo_ac_zener", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+            ("pfo_ostwald", [gp, ctypes.c_int, dp, ctypes.c_int] + [ctypes.c_double] * 9 + [ctypes.c_int]),
             ("pfo_ac_scalar_shipped", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int]),
             ("pfo_laplacian", [gp, dp, dp]),
             ("pfo_ch_mass_energy", [gp, dp, ctypes.c_double, dp, dp]),
@@ -117,6 +118,16 @@ def ac_zener(eta, steps, dt=0.01, dx=None, bc=None, threads=0):
     out = np.array(eta, dtype=np.float64, order="C", copy=True)
     g = _grid(out.shape[:-1], dx, bc)
     _check(lib().pfo_ac_zener(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps), dt, threads), "ac_zener")
+    return out
+
+
+def ostwald(eta, steps, dt=0.001, L=1.0, D=1.0, Calpha=0.05, Cbeta=0.95, A=2.0, delta=1.0, epsilon=3.0,
+            kappa=2.0, dx=None, bc=None, threads=0):
+    """Ostwald ripening as shipped; ``eta`` has shape grid_shape + (N,), field 0 the composition."""
+    out = np.array(eta, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape[:-1], dx, bc)
+    _check(lib().pfo_ostwald(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps), dt, L, D, Calpha, Cbeta, A,
+                             delta, epsilon, kappa, threads), "ostwald")
     return out
 
 

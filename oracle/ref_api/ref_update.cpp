@@ -9,6 +9,7 @@
 //   examples/coarsening/grain_growth/isotropic/phase_field/graingrowth.cpp:73-111
 //   examples/phase_transitions/allen-cahn/allen-cahn.cpp:47-75
 //   examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:103-143
+//   examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:56-123
 // The "shipped" models are those loops with the examples' own expressions;
 // the "baseline" models substitute f(c)=c^2(1-c)^2 for Cahn-Hilliard and
 // f = sum(-e^2/2+e^4/4) + gamma*sum_{i<j} e_i^2 e_j^2 for grain growth, with
@@ -20,6 +21,7 @@
 //   ac_baseline      gamma kappa L dt
 //   graingrowth      dt
 //   zener            dt
+//   ostwald          dt L D Calpha Cbeta A delta epsilon kappa
 //   ac_scalar        r u K M dt
 // Prints "update_seconds <t>" (std::chrono around update() only).
 #include "MMSP.hpp"
@@ -132,6 +134,55 @@ template <int dim> void zener_update(grid<dim, vector<double> >& oldGrid, int st
 	}
 }
 
+// examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:56-123
+// with dt, L, D, Calpha, Cbeta, A, delta, epsilon, kappa from the command line
+// (the example's :66-80 constants by default).
+template <int dim> void ostwald_update(grid<dim, vector<double> >& oldGrid, int steps,
+                                       const std::vector<double>& p)
+{
+	ghostswap(oldGrid);
+	grid<dim, vector<double> > newGrid(oldGrid);
+	grid<dim, double> wspace(oldGrid, 1);
+	double dt = p[0], L = p[1], D = p[2], Calpha = p[3], Cbeta = p[4], A = p[5], delta = p[6],
+	       epsilon = p[7], kappa = p[8];
+	double Cmatrix = 0.5 * (Calpha + Cbeta);
+	double B = A / pow(Cbeta - Cmatrix, 2);
+	double gamma = 2.0 / pow(Cbeta - Calpha, 2);
+	double Dalpha = gamma / pow(delta, 2);
+	double Dbeta = gamma / pow(delta, 2);
+	for (int step = 0; step < steps; step++) {
+		for (int n = 0; n < nodes(oldGrid); n++) {
+			vector<int> x = position(oldGrid, n);
+			double sum = 0.0;
+			for (int i = 1; i < fields(oldGrid); i++)
+				sum += pow(oldGrid(n)[i], 2);
+			double C = oldGrid(n)[0];
+			double lap = laplacian(oldGrid, x, 0);
+			wspace(x) = -A * (C - Cmatrix) + B * pow(C - Cmatrix, 3)
+			            + Dalpha * pow(C - Calpha, 3) + Dbeta * pow(C - Cbeta, 3)
+			            - gamma * (C - Calpha) * sum - kappa * lap;
+		}
+		ghostswap(wspace);
+		for (int n = 0; n < nodes(oldGrid); n++) {
+			vector<int> x = position(oldGrid, n);
+			double lap = laplacian(wspace, x);
+			double C = oldGrid(n)[0];
+			newGrid(n)[0] = C + dt * D * lap;
+			double sum = 0.0;
+			for (int i = 1; i < fields(oldGrid); i++)
+				sum += pow(oldGrid(n)[i], 2);
+			vector<double> vlap = laplacian(oldGrid, x);
+			for (int i = 1; i < fields(oldGrid); i++) {
+				double value = oldGrid(n)[i];
+				newGrid(n)[i] = value - dt * L * (-gamma * pow(C - Calpha, 2) + delta * pow(value, 3)
+				                                  + epsilon * value * (sum - pow(value, 2)) - kappa * vlap[i]);
+			}
+		}
+		swap(oldGrid, newGrid);
+		ghostswap(oldGrid);
+	}
+}
+
 } // namespace MMSP
 
 static double now_s()
@@ -163,6 +214,7 @@ template <int dim> int run_vector(const std::string& model, const char* in, cons
 	if (model == "ac_baseline") MMSP::gg_update(g, steps, false, p);
 	else if (model == "graingrowth") MMSP::gg_update(g, steps, true, p);
 	else if (model == "zener") MMSP::zener_update(g, steps, p);
+	else if (model == "ostwald") MMSP::ostwald_update(g, steps, p);
 	else return 2;
 	double t1 = now_s();
 	std::printf("update_seconds %.9f\n", t1 - t0);
@@ -181,7 +233,8 @@ int main(int argc, char* argv[])
 	std::vector<double> p;
 	for (int i = 5; i < argc; i++) p.push_back(std::atof(argv[i]));
 	size_t need = (model == "ch_baseline") ? 3 : (model == "ch_shipped" || model == "ac_scalar") ? 5
-	            : (model == "ac_baseline") ? 4 : (model == "graingrowth" || model == "zener") ? 1 : 0;
+	            : (model == "ac_baseline") ? 4 : (model == "graingrowth" || model == "zener") ? 1
+	            : (model == "ostwald") ? 9 : 0;
 	if (need == 0 || p.size() != need) {
 		std::cerr << "bad model or parameter count" << std::endl;
 		return 1;

@@ -56,6 +56,8 @@ SMALL = [
     ("gg3d_shipped", "graingrowth", (36, 36, 4), 2, ("circles",), (0.01,), 40, {}),
     ("zener2d_shipped", "zener", (64, 64), 3, ("zener", 40, 22), (0.01,), 100, {}),
     ("zener3d_shipped", "zener", (24, 24, 12), 3, ("zener", 30, 23), (0.01,), 40, {}),
+    ("ostwald2d_shipped", "ostwald", (64, 32), 2, ("ostwald", 24), (0.001, 1.0, 1.0, 0.05, 0.95, 2.0, 1.0, 3.0, 2.0), 60, {}),
+    ("ostwald3d_shipped", "ostwald", (16, 12, 8), 4, ("ostwald", 25), (0.001, 1.0, 1.0, 0.05, 0.95, 2.0, 1.0, 3.0, 2.0), 40, {}),
 ]
 
 
@@ -72,6 +74,8 @@ def start_state(shape, fields, spec):
     if kind == "zener":
         _, particles, seed = spec
         return inputs.zener_particles(shape, particles, seed)
+    if kind == "ostwald":
+        return inputs.ostwald_start(shape, fields, spec[1])
     raise ValueError(kind)
 
 

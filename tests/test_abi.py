@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_version_and_strerror(lib):
-    assert lib.mmsp_gpu_version() == 1
+    assert lib.mmsp_gpu_version() == 2
     assert lib.mmsp_gpu_strerror(0) == b"ok"
     assert lib.mmsp_gpu_strerror(-4) == b"unsupported configuration"
 
@@ -52,6 +52,26 @@ def test_desc_init_defaults(lib):
     assert d.dt == 0.005 and d.kappa == 1.0 and d.mobility == 1.0
     assert lib.mmsp_gpu_desc_init(ctypes.byref(d), 3, n, 2, native.F32, native.GG) == 0
     assert d.dt == 0.01 and d.kappa == 2.0
+    assert lib.mmsp_gpu_desc_init(ctypes.byref(d), 2, n, 3, native.F64, native.OSTWALD) == 0
+    assert (d.dt, d.kappa, d.mobility) == (0.001, 2.0, 1.0)              # ostwald.cpp:66-80
+    assert list(d.aux) == [1.0, 0.05, 0.95, 2.0, 1.0, 3.0]
+    assert ctypes.sizeof(native.Desc) == 4 * 13 + 4 + 8 * 15     # C layout: 13 ints, padding, 15 doubles
+
+
+def test_ostwald_validation_and_footprint(lib):
+    from mmsp_gb300 import native
+
+    d = native.make_desc((16, 16), fields=1, model="ostwald")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL          # needs an order parameter
+    d = native.make_desc((16, 16), fields=3, model="ostwald", Cbeta=0.05)
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL          # Calpha == Cbeta
+    d = native.make_desc((16, 16), fields=3, model="ostwald")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.OK
+    b = ctypes.c_size_t()
+    assert lib.mmsp_gpu_footprint(ctypes.byref(d), ctypes.byref(b)) == 0
+    assert b.value >= 2 * 3 * 256 * 8 + 256 * 8                              # two states and the work grid
+    x = np.zeros(16 * 16 * 3)
+    assert lib.mmsp_gpu_step_noalloc(ctypes.byref(d), x.ctypes.data, x.ctypes.data, 1, None) == native.EUNSUPPORTED
 
 
 def test_validation_without_device(lib):

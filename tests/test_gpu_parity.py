@@ -38,6 +38,9 @@ def desc_for(native, model, params, shape, fields, dtype, dx=None, bc=None):
         return native.make_desc(shape, fields, dtype, "gg", dt=p[0], **kw)
     if model == "zener":
         return native.make_desc(shape, fields, dtype, "zener", dt=p[0], **kw)
+    if model == "ostwald":
+        return native.make_desc(shape, fields, dtype, "ostwald", dt=p[0], mobility=p[1], D=p[2], Calpha=p[3],
+                                Cbeta=p[4], A=p[5], delta=p[6], epsilon=p[7], kappa=p[8], **kw)
     raise ValueError(model)
 
 
@@ -57,7 +60,7 @@ def test_fp64_matches_reference_fixture(gpu, path):
     z = np.load(path)
     model = str(z["model"])
     x = z["start"]
-    vector = model in ("ac_baseline", "graingrowth", "zener")
+    vector = model in ("ac_baseline", "graingrowth", "zener", "ostwald")
     shape = x.shape[:-1] if vector else x.shape
     fields = x.shape[-1] if vector else 1
     bc = z["bc"].tolist()
@@ -397,3 +400,69 @@ def test_zener_particles_do_not_move(gpu, oracle, dtype, shape):
     tol = TOL_SHIPPED if dtype == np.float64 else TOL_F32
     assert np.abs(got.astype(np.float64) - want).max() <= tol * max(1.0, np.abs(want).max())
     assert np.abs(want[..., 1:] - x[..., 1:]).max() > 1e-3
+
+
+OSTWALD = [((96, 64), 2), ((20, 16, 12), 3), ((7, 9, 13), 4), ((200,), 2)]
+
+
+@pytest.mark.parametrize("shape,fields", OSTWALD, ids=["%s-%d" % ("x".join(map(str, s)), f) for s, f in OSTWALD])
+def test_ostwald_fp32_and_fp64_against_oracle(gpu, oracle, shape, fields):
+    """Ostwald ripening (two kernels per step): FP64 within the shipped-form
+    tolerance of the oracle (pow(x,3) by the compensated cube), FP32 within
+    the precision-form tolerance."""
+    from mmsp_gb300 import inputs
+
+    x = inputs.ostwald_start(shape, fields, 50 + len(shape))
+    steps = 100
+    want = oracle.ostwald(x, steps)
+    d64 = gpu.make_desc(shape, fields, np.float64, "ostwald")
+    got64 = run_gpu(gpu, d64, x, steps)
+    assert np.abs(got64 - want).max() <= TOL_SHIPPED * np.abs(want).max()
+    d32 = gpu.make_desc(shape, fields, np.float32, "ostwald")
+    got32 = run_gpu(gpu, d32, x.astype(np.float32), steps).astype(np.float64)
+    assert np.abs(got32 - want).max() <= TOL_F32
+    assert np.abs(want - x).max() > 1e-3
+    # the composition is conserved: its sum moves by rounding only
+    assert abs(want[..., 0].sum() - x[..., 0].sum()) < 1e-9 * x[..., 0].size
+    assert abs(got64[..., 0].sum() - x[..., 0].sum()) < 1e-9 * x[..., 0].size
+
+
+def ostwald_energy(x, dx, Ca=0.05, Cb=0.95, A=2.0, delta=1.0, eps=3.0, kappa=2.0):
+    """The free energy the library reports for the Ostwald model, in numpy:
+    -A/2 (C-Cm)^2 + B/4 (C-Cm)^4 + Da/4 (C-Ca)^4 + Db/4 (C-Cb)^4 - g/2 (C-Ca)^2 sum e^2
+    + delta/4 sum e^4 + eps/2 sum_{i<j} e_i^2 e_j^2 + kappa/2 sum |grad|^2 (central differences)."""
+    Cm = 0.5 * (Ca + Cb)
+    B = A / (Cb - Cm) ** 2
+    g = 2.0 / (Cb - Ca) ** 2
+    Da = Db = g / delta ** 2
+    C = x[..., 0]
+    e = x[..., 1:]
+    e2 = e * e
+    sq = e2.sum(-1)
+    pair = 0.5 * (sq * sq - (e2 * e2).sum(-1))
+    f = (-0.5 * A * (C - Cm) ** 2 + 0.25 * B * (C - Cm) ** 4 + 0.25 * Da * (C - Ca) ** 4
+         + 0.25 * Db * (C - Cb) ** 4 - 0.5 * g * (C - Ca) ** 2 * sq + 0.25 * delta * (e2 * e2).sum(-1)
+         + 0.5 * eps * pair)
+    grad = np.zeros_like(C)
+    for j in range(x.shape[-1]):
+        for a in range(C.ndim):
+            gi = (np.roll(x[..., j], -1, a) - np.roll(x[..., j], 1, a)) / (2.0 * dx[a])
+            grad += gi * gi
+    dV = float(np.prod(dx))
+    return dV * x.sum(), dV * (f + 0.5 * kappa * grad).sum()
+
+
+def test_ostwald_reductions(gpu):
+    from mmsp_gb300 import inputs
+
+    shape, dx = (24, 20, 16), [1.0, 0.9, 1.1]
+    x = inputs.ostwald_start(shape, 3, 61)
+    d = gpu.make_desc(shape, 3, np.float64, "ostwald", dx=dx)
+    with gpu.Stepper(d) as s:
+        s.upload(x)
+        s.step(20)
+        st = s.reduce()
+        y = s.download()
+    m, e = ostwald_energy(y, dx)
+    assert abs(st.mass - m) <= 1e-12 * abs(m)
+    assert abs(st.energy - e) <= 1e-11 * abs(e)

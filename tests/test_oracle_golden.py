@@ -38,6 +38,8 @@ def run_oracle(o, z, x=None, steps=None):
         return o.ac_graingrowth(x, st, *p, dx=dx, bc=bc)
     if m == "zener":
         return o.ac_zener(x, st, *p, dx=dx, bc=bc)
+    if m == "ostwald":
+        return o.ostwald(x, st, *p, dx=dx, bc=bc)
     raise ValueError(m)
 
 
