@@ -234,7 +234,45 @@ def other_configs(native, inputs, stream):
                               "f64_value_updates_per_s": vals / (ms64 / 1e3),
                               "f32_roofline_frac": 2 * 4 * vals / (ms32 / 1e3) / 1e9 / peaks()[0],
                               "f32_max_err_vs_f64": float(np.abs(o32.astype(np.float64) - o64).max())}
+    res.update(other_models(native, inputs, timed))
     return res
+
+
+def other_models(native, inputs, timed):
+    """The further explicit models on the same device path: Zener pinning
+    (grain growth with the particle field fixed) on 128^3 x 3 fields and
+    Ostwald ripening (composition + order parameter, two kernels per step)
+    on 256 x 128 x 64 x 2 fields (the example's 128 x 64 x 16, doubled per
+    axis), 500 steps each in FP32 and FP64, beside the oracle (the
+    reference's loops restated in C, FP64, one thread) on 2 steps."""
+    from oracle import pf_oracle
+
+    peak = peaks()[0]
+    out = {}
+    cases = [
+        ("zener3d_128_n3_500", (128, 128, 128), 3, "zener", inputs.zener_particles((128, 128, 128), 400, 9),
+         lambda x, n: pf_oracle.ac_zener(x, n, 0.01, threads=1)),
+        ("ostwald3d_256x128x64_n2_500", (256, 128, 64), 2, "ostwald", inputs.ostwald_start((256, 128, 64), 2, 9),
+         lambda x, n: pf_oracle.ostwald(x, n, threads=1)),
+    ]
+    for name, shape, fields, model, x, cpu in cases:
+        steps = 500
+        d32 = native.make_desc(shape, fields, np.float32, model)
+        d64 = native.make_desc(shape, fields, np.float64, model)
+        ms32, o32 = timed(d32, x.astype(np.float32), steps)
+        ms64, o64 = timed(d64, x, steps)
+        vals = int(np.prod(shape)) * fields * steps
+        t0 = time.perf_counter()
+        cpu(x, 2)
+        cpu_s = (time.perf_counter() - t0) / 2
+        cpu_rate = int(np.prod(shape)) * fields / cpu_s
+        out[name] = {"f32_ms": ms32, "f64_ms": ms64, "f32_value_updates_per_s": vals / (ms32 / 1e3),
+                     "f64_value_updates_per_s": vals / (ms64 / 1e3),
+                     "f32_roofline_frac": 2 * 4 * vals / (ms32 / 1e3) / 1e9 / peak,
+                     "f32_max_err_vs_f64": float(np.abs(o32.astype(np.float64) - o64).max()),
+                     "cpu_oracle_value_updates_per_s": cpu_rate, "cpu_sample": "2 FP64 steps, 1 thread",
+                     "f64_speedup_vs_cpu": vals / (ms64 / 1e3) / cpu_rate}
+    return out
 
 
 def output_path(native, inputs):

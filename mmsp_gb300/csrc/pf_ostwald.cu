@@ -5,11 +5,11 @@
 // chemical potential of the composition C (field 0) into a scalar work grid
 // (:89-100), ghostswap, then the new composition from the Laplacian of that
 // grid and the new order parameters (fields 1..N-1) from their own
-// Laplacians (:103-120).  Here each pass is one kernel over all cells, the
-// work grid is a device buffer of the handle, and the periodic halo is index
-// arithmetic.  Neighbour values come through the L1/L2 caches: the state of
-// the shipped examples (a few fields of at most 128 x 64 x 16 cells) stays
-// in L2, so the passes are bound by FP64 arithmetic, not by DRAM.
+// Laplacians (:103-120).  Here each pass is one kernel over all cells (a
+// block walks rows along axis Z, one thread per cell of a row, so a cell's
+// coordinates need no division), the work grid is a device buffer of the
+// handle, and the periodic halo is index arithmetic.  Neighbour values come
+// through the L1/L2 caches.
 //
 // FP64 follows the reference's operation order with separately rounded
 // operations (pow(x,3) as the compensated cube of pf_device.cuh, pow(x,2)
@@ -50,25 +50,28 @@ static OstP<T> ost_narrow(const Coeffs& c, int dim)
     return p;
 }
 
-// Offsets of the six periodic neighbours of cell i (padded axes X, Y, Z).
+// Offsets of the six periodic neighbours of a cell (padded axes X, Y, Z).
+// The X and Y offsets are those of the cell's row; Z depends on the cell.
 struct Nb {
-    long long xh, xl, yh, yl, zh, zl;
+    long long xh, xl, yh, yl;
+    int zh, zl;
 };
 
-static __device__ __forceinline__ Nb neighbours(const Geom& g, long long i)
+static __device__ __forceinline__ Nb row_neighbours(const Geom& g, int x, int y)
 {
-    const int x = (int)(i / g.YZ);
-    const long long r = i - (long long)x * g.YZ;
-    const int y = (int)(r / g.Z);
-    const int z = (int)(r - (long long)y * g.Z);
     Nb n;
     n.xh = (x + 1 == g.X ? -(long long)x : 1LL) * g.YZ;
     n.xl = (x == 0 ? (long long)(g.X - 1) : -1LL) * g.YZ;
     n.yh = (y + 1 == g.Y ? -(long long)y : 1LL) * g.Z;
     n.yl = (y == 0 ? (long long)(g.Y - 1) : -1LL) * g.Z;
-    n.zh = z + 1 == g.Z ? -(long long)z : 1LL;
-    n.zl = z == 0 ? (long long)(g.Z - 1) : -1LL;
+    n.zh = n.zl = 0;
     return n;
+}
+
+static __device__ __forceinline__ void cell_z(Nb& n, const Geom& g, int z)
+{
+    n.zh = z + 1 == g.Z ? -z : 1;
+    n.zl = z == 0 ? g.Z - 1 : -1;
 }
 
 template <typename T, int DIM, bool UNIT>
@@ -98,19 +101,24 @@ __global__ void __launch_bounds__(256)
 ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
 {
     using A = Ar<T>;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g.cells;
-         i += (long long)gridDim.x * blockDim.x) {
-        const Nb n = neighbours(g, i);
-        const T sum = order_sum(s, i, g.cells, N);
-        const T C = s[i];
-        const T lap = lap_at<T, DIM, UNIT>(s, i, n, p);
-        const T dm = A::sub(C, p.Cm), da = A::sub(C, p.Ca), db = A::sub(C, p.Cb);
-        T v = A::mul(p.negA, dm);
-        v = A::add(v, A::mul(p.B, cube(dm)));
-        v = A::add(v, A::mul(p.Da, cube(da)));
-        v = A::add(v, A::mul(p.Db, cube(db)));
-        v = A::sub(v, A::mul(A::mul(p.g, da), sum));
-        w[i] = A::sub(v, kappa_times(p.kappa, lap));
+    const long long rows = (long long)g.X * g.Y;
+    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int x = (int)(row / g.Y), y = (int)(row - (long long)x * g.Y);
+        Nb n = row_neighbours(g, x, y);
+        for (int z = threadIdx.x; z < g.Z; z += blockDim.x) {
+            cell_z(n, g, z);
+            const long long i = row * g.Z + z;
+            const T sum = order_sum(s, i, g.cells, N);
+            const T C = s[i];
+            const T lap = lap_at<T, DIM, UNIT>(s, i, n, p);
+            const T dm = A::sub(C, p.Cm), da = A::sub(C, p.Ca), db = A::sub(C, p.Cb);
+            T v = A::mul(p.negA, dm);
+            v = A::add(v, A::mul(p.B, cube(dm)));
+            v = A::add(v, A::mul(p.Da, cube(da)));
+            v = A::add(v, A::mul(p.Db, cube(db)));
+            v = A::sub(v, A::mul(A::mul(p.g, da), sum));
+            w[i] = A::sub(v, kappa_times(p.kappa, lap));
+        }
     }
 }
 
@@ -122,21 +130,26 @@ __global__ void __launch_bounds__(256)
 ostwald_update(const T* __restrict__ s, const T* __restrict__ w, T* __restrict__ out, Geom g, OstP<T> p, int N)
 {
     using A = Ar<T>;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g.cells;
-         i += (long long)gridDim.x * blockDim.x) {
-        const Nb n = neighbours(g, i);
-        const T C = s[i];
-        out[i] = A::add(C, A::mul(p.dtD, lap_at<T, DIM, UNIT>(w, i, n, p)));
-        const T sum = order_sum(s, i, g.cells, N);
-        const T da = A::sub(C, p.Ca);
-        const T t1 = A::mul(p.neg_g, A::mul(da, da));
-        for (int j = 1; j < N; j++) {
-            const T* f = s + (long long)j * g.cells;
-            const T e = f[i];
-            T v = A::add(t1, A::mul(p.delta, cube(e)));
-            v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
-            v = A::sub(v, kappa_times(p.kappa, lap_at<T, DIM, UNIT>(f, i, n, p)));
-            out[(long long)j * g.cells + i] = A::sub(e, A::mul(p.dtL, v));
+    const long long rows = (long long)g.X * g.Y;
+    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int x = (int)(row / g.Y), y = (int)(row - (long long)x * g.Y);
+        Nb n = row_neighbours(g, x, y);
+        for (int z = threadIdx.x; z < g.Z; z += blockDim.x) {
+            cell_z(n, g, z);
+            const long long i = row * g.Z + z;
+            const T C = s[i];
+            out[i] = A::add(C, A::mul(p.dtD, lap_at<T, DIM, UNIT>(w, i, n, p)));
+            const T sum = order_sum(s, i, g.cells, N);
+            const T da = A::sub(C, p.Ca);
+            const T t1 = A::mul(p.neg_g, A::mul(da, da));
+            for (int j = 1; j < N; j++) {
+                const T* f = s + (long long)j * g.cells;
+                const T e = f[i];
+                T v = A::add(t1, A::mul(p.delta, cube(e)));
+                v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
+                v = A::sub(v, kappa_times(p.kappa, lap_at<T, DIM, UNIT>(f, i, n, p)));
+                out[(long long)j * g.cells + i] = A::sub(e, A::mul(p.dtL, v));
+            }
         }
     }
 }
@@ -162,11 +175,14 @@ cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     const void* up = nullptr;
     if (d.dtype == MMSP_GPU_F64) ost_pick<double>(g.dim, c.unit_w, &p->fn, &up);
     else ost_pick<float>(g.dim, c.unit_w, &p->fn, &up);
-    long long blocks = (g.cells + 255) / 256;
-    const long long most = 8LL * sm_count();   // grid-stride beyond 8 blocks per SM
+    // one row (axis Z) per block iteration, threads along the row; blocks
+    // stride over the rows beyond 16 resident blocks per SM
+    const int threads = g.Z >= 256 ? 256 : (g.Z + 31) / 32 * 32;
+    long long blocks = (long long)g.X * g.Y;
+    const long long most = 16LL * sm_count() * (256 / threads);
     if (blocks > most) blocks = most;
     p->grid = dim3((unsigned)blocks, 1, 1);
-    p->block = dim3(256, 1, 1);
+    p->block = dim3(threads, 1, 1);
     p->smem = 0;
     p->planes = 1;
     p->fields = d.fields;
