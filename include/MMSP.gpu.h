@@ -114,7 +114,15 @@ typedef struct mmsp_gpu_desc {
     double mobility;  /* M (Cahn-Hilliard) or L (Allen-Cahn) */
     double gamma;     /* grain-boundary coupling (MMSP_GPU_AC) */
     double r, u;      /* polynomial coefficients (MMSP_GPU_CH_POLY, MMSP_GPU_AC_POLY) */
-    double aux[6];    /* further model parameters: MMSP_GPU_OSTWALD takes D, Ca, Cb, A, delta, eps */
+    double aux[6];    /* further model parameters: MMSP_GPU_OSTWALD takes D, Ca, Cb, A, delta, eps;
+                         MMSP_GPU_CH_POLY and MMSP_GPU_AC_POLY take a thermal noise standard
+                         deviation (aux[0], 0: none) and stream seed (aux[1], an integer <= 2^53):
+                         the stochastic forms of model_A.cpp:99-100 (AC_POLY), model_B.cpp:100-106
+                         and spinodal.cpp:95-102 (CH_POLY) add gaussian(0, aux[0]) to mu.  The examples
+                         draw it from rand() in cell order; here deviate step*cells + cell of a
+                         SplitMix64 / Box-Muller stream, step counting from the last upload.
+                         Noisy grids are stepped without graph replay and are refused by batches
+                         and mmsp_gpu_step_noalloc (EUNSUPPORTED). */
 } mmsp_gpu_desc;
 
 typedef struct mmsp_gpu_stats {

@@ -37,6 +37,8 @@
 #include <iostream>
 #include <vector>
 
+#include <cmath>
+
 #include "MMSP.gpu.h"
 
 namespace MMSP {
@@ -86,6 +88,29 @@ inline Model ostwald_ripening_shipped(double dt = 0.001, double L = 1.0, double 
                                       double epsilon = 3.0, double kappa = 2.0)
 {
     Model m = {MMSP_GPU_OSTWALD, dt, kappa, L, 1.0, 0.0, 0.0, {D, Calpha, Cbeta, A, delta, epsilon}};
+    return m;
+}
+// examples/phase_transitions/model_A/model_A.cpp:74-107: scalar Allen-Cahn with thermal noise
+// of standard deviation sqrt(2 kT/(dt dV)) from stream `seed`
+inline Model model_A(double r = 1.0, double u = 1.0, double K = 1.0, double M = 1.0, double dt = 0.01,
+                     double kT = 0.01, double dV = 1.0, double seed = 0.0)
+{
+    Model m = {MMSP_GPU_AC_POLY, dt, K, M, 0.0, r, u, {std::sqrt(2.0 * kT / (dt * dV)), seed, 0.0, 0.0, 0.0, 0.0}};
+    return m;
+}
+// examples/phase_transitions/model_B/model_B.cpp:74-112: Cahn-Hilliard with thermal noise in mu
+inline Model model_B(double r = 1.0, double u = 1.0, double K = 1.0, double M = 1.0, double dt = 0.01,
+                     double kT = 0.01, double dV = 1.0, double seed = 0.0)
+{
+    Model m = {MMSP_GPU_CH_POLY, dt, K, M, 0.0, r, u, {std::sqrt(2.0 * kT / (dt * dV)), seed, 0.0, 0.0, 0.0, 0.0}};
+    return m;
+}
+// examples/phase_transitions/spinodal/spinodal.cpp:95-102: mu = -c + c^3 - lap c + noise of standard
+// deviation sqrt(epsilon dt/dV); c' = c + dt/(2 dV) lap mu
+inline Model spinodal(double dt = 0.01, double dV = 1.0, double epsilon = 0.05, double seed = 0.0)
+{
+    Model m = {MMSP_GPU_CH_POLY, dt, 1.0, 1.0 / (2.0 * dV), 0.0, 1.0, 1.0,
+               {std::sqrt(epsilon * dt / dV), seed, 0.0, 0.0, 0.0, 0.0}};
     return m;
 }
 // allen-cahn.cpp:57-70 as shipped (scalar grid)

@@ -118,6 +118,11 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     if (d->model == MMSP_GPU_OSTWALD && d->fields < 2)
         BAD(MMSP_GPU_EINVAL, "Ostwald ripening takes a composition and at least one order parameter, fields=%d",
             d->fields);
+    if ((d->model == MMSP_GPU_CH_POLY || d->model == MMSP_GPU_AC_POLY) &&
+        (!(d->aux[0] >= 0.0) || !isfinite(d->aux[0]) || !(d->aux[1] >= 0.0) || !(d->aux[1] <= 9007199254740992.0) ||
+         d->aux[1] != floor(d->aux[1])))
+        BAD(MMSP_GPU_EINVAL, "noise: aux[0] (standard deviation) must be finite and >= 0, aux[1] (seed) an integer "
+                             "in [0, 2^53]");
     if (d->model == MMSP_GPU_OSTWALD && (!(d->aux[2] != d->aux[1]) || !(d->aux[4] != 0.0)))
         BAD(MMSP_GPU_EINVAL, "Ostwald ripening needs Calpha != Cbeta and delta != 0");
     if (d->fields > 32) BAD(MMSP_GPU_EUNSUPPORTED, "fields=%d above 32", d->fields);
@@ -332,14 +337,18 @@ extern "C" int mmsp_gpu_download_device(mmsp_gpu_handle* h, void* dev, size_t by
     return download(h, dev, bytes, layout, cudaMemcpyDeviceToDevice, false);
 }
 
-static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s)
+// One step on `s`; `step` indexes the noise stream of the stochastic forms
+// (steps since the last upload) and is unused otherwise.
+static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s, long long step = 0)
 {
     bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
     const void* in = h->buf[h->cur];
     void* out = h->buf[h->cur ^ 1];
-    cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, h->c, in, out, h->work, s)
-                    : ch ? pf::launch_ch(h->plan, h->d, h->g, h->c, in, out, h->flags, s)
-                         : pf::launch_ac(h->plan, h->d, h->g, h->c, in, out, h->flags, s);
+    pf::Coeffs c = h->c;
+    c.step = step;
+    cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, c, in, out, h->work, s)
+                    : ch ? pf::launch_ch(h->plan, h->d, h->g, c, in, out, h->flags, s)
+                         : pf::launch_ac(h->plan, h->d, h->g, c, in, out, h->flags, s);
     h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913
     return e;
 }
@@ -384,7 +393,12 @@ extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
     cudaError_t e = cudaEventRecord(h->ev0, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "event");
     int left = steps;
-    if (steps >= kGraphMin) {
+    if (pf::noisy(h->d)) {
+        // the step index is a kernel argument, so no graph replay
+        for (int k = 0; k < steps; k++)
+            if ((e = one_step(h, h->stream, h->steps + k)) != cudaSuccess) return cuda_fail(h, e, "step");
+        left = 0;
+    } else if (steps >= kGraphMin) {
         int rc = build_graph(h);
         if (rc) return rc;
         if (h->cur == 1) {

@@ -64,7 +64,8 @@ extern "C" int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, 
     int rc = mmsp_gpu_validate(desc);
     if (rc) return rc;
     if (!in || !out || steps < 0) return MMSP_GPU_EINVAL;
-    if (desc->model == MMSP_GPU_OSTWALD) return MMSP_GPU_EUNSUPPORTED;   // needs a work grid of its own
+    // a work grid of its own, or a noise stream indexed by the handle's step count
+    if (desc->model == MMSP_GPU_OSTWALD || pf::noisy(*desc)) return MMSP_GPU_EUNSUPPORTED;
     mmsp_gpu_desc d = *desc;
     for (int a = d.dim; a < 3; a++) d.n[a] = 1;
     const size_t bytes = state_bytes(d);

@@ -78,6 +78,13 @@ ac_step_kernel(const T* __restrict__ ein, T* __restrict__ eout, Geom g, P<T> p, 
                 T y2 = twice(y);
                 T lap = lap_ref<T, UNIT_W, DIM>(y2, H[o], L[o], C[o + CW], C[o - CW], C[o + 1], C[o - 1], p.wx, p.wy,
                                                 p.wz);
+                if (MODEL == MMSP_GPU_AC_POLY && p.noise != 0.0) {
+                    // model_A.cpp:99-100: p - dt*M*(-r p + u pow(p,3) - K lap + noise)
+                    T e = A::sub(A::add(A::mul(p.neg_r, y), A::mul(p.u, cube(y))), kappa_times(p.kappa, lap));
+                    e = A::add(e, noise_at(p, cells, (long long)gx * g.YZ + (long long)gy * g.Z + gz));
+                    dst[f * cells] = A::sub(y, A::mul(p.dtm, e));
+                    continue;
+                }
                 // Zener pinning: the particles (field 0) have zero mobility (zener.cpp:134)
                 dst[f * cells] = (MODEL == MMSP_GPU_ZENER && f == 0) ? y : ac_new<T, MODEL>(y, sum, lap, p);
             }
@@ -135,7 +142,8 @@ static const void* ac_pick(int dim, int model, int ty, bool unit)
 
 cudaError_t plan_ac(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
-    if (ac3_stream_eligible(d, g)) return plan_ac3_stream(d, g, p);
+    // the stochastic form takes the tile kernel, which adds the noise term
+    if (!noisy(d) && ac3_stream_eligible(d, g)) return plan_ac3_stream(d, g, p);
     Coeffs c = make_coeffs(d);
     bool dbl = d.dtype == MMSP_GPU_F64;
     size_t es = dbl ? sizeof(double) : sizeof(float);

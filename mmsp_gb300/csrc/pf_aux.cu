@@ -64,6 +64,10 @@ Coeffs make_coeffs(const mmsp_gpu_desc& d)
     c.neg_r = -d.r;
     c.u = d.u;
     c.dtm = (d.model == MMSP_GPU_GG || d.model == MMSP_GPU_ZENER) ? d.dt : d.dt * d.mobility;
+    if (noisy(d)) {
+        c.noise = d.aux[0];
+        c.seed = (unsigned long long)d.aux[1];
+    }
     if (d.model == MMSP_GPU_OSTWALD) {
         // ostwald.cpp:67-80, with the same pow calls
         OstConst& o = c.ost;

@@ -67,7 +67,8 @@ ch_step_kernel(const T* __restrict__ cin, T* __restrict__ cout, Geom g, P<T> p, 
         }
     };
     // mu on the (TY+2) x (TZ+2) plane from c planes below / at / above it
-    auto mu_plane = [&](int mslot, int cl, int cc, int chh) {
+    auto mu_plane = [&](int mslot, int cl, int cc, int chh, int gx) {
+        const long long pbase = (long long)wrapi(gx, g.X) * g.YZ;
         const T* C = cs + cc * CP;
         const T* L = cs + cl * CP;
         const T* H = cs + chh * CP;
@@ -79,7 +80,10 @@ ch_step_kernel(const T* __restrict__ cin, T* __restrict__ cout, Geom g, P<T> p, 
             T y2 = twice(y);
             T lap = lap_ref<T, UNIT_W, DIM>(y2, H[ci], L[ci], C[ci + CW], C[ci - CW], C[ci + 1], C[ci - 1], p.wx,
                                             p.wy, p.wz);
-            M[e] = ch_mu<T, MODEL>(y, lap, p);
+            T mu = ch_mu<T, MODEL>(y, lap, p);
+            // thermal noise of the stochastic forms (model_B.cpp:100-101, spinodal.cpp:95-97): mu + noise
+            if (p.noise != 0.0) mu = A::add(mu, noise_at(p, g.cells, pbase + yoff[my + 1] + zoff[mz + 1]));
+            M[e] = mu;
         }
     };
     // c' = c + dt*M*lap(mu) on the TY x TZ tile of plane gx
@@ -106,7 +110,7 @@ ch_step_kernel(const T* __restrict__ cin, T* __restrict__ cout, Geom g, P<T> p, 
     if (DIM < 3) {
         load(0, 0);
         __syncthreads();
-        mu_plane(0, 0, 0, 0);
+        mu_plane(0, 0, 0, 0, 0);
         __syncthreads();
         out_plane(0, 0, 0, 0, 0);
         return;
@@ -120,13 +124,13 @@ ch_step_kernel(const T* __restrict__ cin, T* __restrict__ cout, Geom g, P<T> p, 
     auto msl = [&](int x) { return (x - xs + 1) % 3; };
     for (int x = xs - 2; x <= xs + 1; x++) load(csl(x), x);
     __syncthreads();
-    mu_plane(msl(xs - 1), csl(xs - 2), csl(xs - 1), csl(xs));
-    mu_plane(msl(xs), csl(xs - 1), csl(xs), csl(xs + 1));
+    mu_plane(msl(xs - 1), csl(xs - 2), csl(xs - 1), csl(xs), xs - 1);
+    mu_plane(msl(xs), csl(xs - 1), csl(xs), csl(xs + 1), xs);
     __syncthreads();
     for (int x = xs; x < xe; x++) {
         load(csl(x + 2), x + 2);  // overwrites c(x-2): its last readers were before the previous syncs
         __syncthreads();
-        mu_plane(msl(x + 1), csl(x), csl(x + 1), csl(x + 2));
+        mu_plane(msl(x + 1), csl(x), csl(x + 1), csl(x + 2), x + 1);
         __syncthreads();
         out_plane(x, csl(x), msl(x - 1), msl(x), msl(x + 1));
     }
@@ -164,8 +168,9 @@ static const void* ch_pick(int dim, int model, int ty, bool unit)
 
 cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
-    if (ch3_stream_eligible(d, g)) return plan_ch3_stream(d, g, p);
-    if (ch_rows_eligible(d, g)) return plan_ch_rows(d, g, p);
+    // the stochastic forms take the tile kernel, which adds the noise term
+    if (!noisy(d) && ch3_stream_eligible(d, g)) return plan_ch3_stream(d, g, p);
+    if (!noisy(d) && ch_rows_eligible(d, g)) return plan_ch_rows(d, g, p);
     p->kind = 0;
     Coeffs c = make_coeffs(d);
     int ty = g.Y >= 16 ? 16 : 8;

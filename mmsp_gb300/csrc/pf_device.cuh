@@ -46,7 +46,40 @@ static __device__ __forceinline__ float cube(float x) { return x * x * x; }
 template <typename T> struct P {
     T wx, wy, wz;      // Laplacian weights of padded axes X, Y, Z
     T kappa, dtm, gamma2, neg_r, u;
+    double noise;               // thermal noise standard deviation (0: none)
+    unsigned long long seed;    // noise stream
+    long long step;             // step index within the stream
 };
+
+// Value j of the SplitMix64 stream `seed` (Steele, Lea and Flood, OOPSLA
+// 2014): the same function as mmsp_gb300/inputs.py and the oracle use.
+static __device__ __forceinline__ unsigned long long splitmix64_at(unsigned long long seed, unsigned long long j)
+{
+    unsigned long long z = seed + (j + 1ULL) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+// Standard normal deviate k of stream `seed` by the Box-Muller transform of
+// uniforms 2k and 2k+1 (top 53 bits): sqrt(-2 log(1 - u1)) cos(2 pi u2).
+// Counter-based, so a cell's noise is the same wherever it is recomputed.
+static __device__ __forceinline__ double gauss_at(unsigned long long seed, unsigned long long k)
+{
+    const double u1 = (double)(splitmix64_at(seed, 2ULL * k) >> 11) * 0x1.0p-53;
+    const double u2 = (double)(splitmix64_at(seed, 2ULL * k + 1ULL) >> 11) * 0x1.0p-53;
+    return sqrt(-2.0 * log(1.0 - u1)) * cos(6.283185307179586 * u2);
+}
+
+// The noise term of cell `cell` in the current step, std * N(0,1), as the
+// examples' gaussian(0.0, std) returns it (model_A.cpp:13-40: ave + u*std),
+// narrowed to the state type.
+template <typename T>
+static __device__ __forceinline__ T noise_at(const P<T>& p, long long cells, long long cell)
+{
+    const unsigned long long k = (unsigned long long)p.step * (unsigned long long)cells + (unsigned long long)cell;
+    return (T)(0.0 + gauss_at(p.seed, k) * p.noise);
+}
 
 // 2.0*y, which is exact.  For FP64 a normal y whose double stays finite is
 // doubled by adding 1 to its exponent on the integer pipe; zeros,
@@ -169,6 +202,9 @@ static inline P<T> narrow(const Coeffs& c, int dim)
     p.gamma2 = (T)c.gamma2;
     p.neg_r = (T)c.neg_r;
     p.u = (T)c.u;
+    p.noise = c.noise;
+    p.seed = c.seed;
+    p.step = c.step;
     return p;
 }
 

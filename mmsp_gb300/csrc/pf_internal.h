@@ -38,7 +38,19 @@ struct Coeffs {
     double dV;         // cell volume
     bool unit_w;       // every w == 1.0 exactly
     OstConst ost;      // MMSP_GPU_OSTWALD
+    // Thermal noise of MMSP_GPU_CH_POLY / MMSP_GPU_AC_POLY (aux[0], aux[1]):
+    // standard deviation (0: none), stream seed, and the index of the step
+    // being launched (steps since the last upload).
+    double noise;
+    unsigned long long seed;
+    long long step;
 };
+
+// Noise on: the shipped polynomial models with a nonzero standard deviation.
+inline bool noisy(const mmsp_gpu_desc& d)
+{
+    return (d.model == MMSP_GPU_CH_POLY || d.model == MMSP_GPU_AC_POLY) && d.aux[0] != 0.0;
+}
 
 Geom make_geom(const mmsp_gpu_desc& d);
 int sm_count();                 // SMs of the current device

@@ -23,6 +23,7 @@ CELL_MAJOR, FIELD_MAJOR = 0, 1
 MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY, "zener": ZENER,
           "ostwald": OSTWALD}
 OSTWALD_AUX = ("D", "Calpha", "Cbeta", "A", "delta", "epsilon")   # mmsp_gpu_desc.aux of MMSP_GPU_OSTWALD
+NOISE_AUX = ("noise", "seed")   # mmsp_gpu_desc.aux of MMSP_GPU_CH_POLY / MMSP_GPU_AC_POLY
 DTYPES = {np.dtype(np.float64): F64, np.dtype(np.float32): F32}
 
 # Every symbol include/MMSP.gpu.h declares (checked by the CPU test suite).
@@ -173,7 +174,9 @@ def strerror(code: int) -> str:
 def make_desc(shape, fields=1, dtype=np.float64, model="ch", dx=None, bc=None, dt=None, kappa=None,
               mobility=None, gamma=None, r=None, u=None, **aux) -> Desc:
     """A descriptor with the model's defaults (mmsp_gpu_desc_init), then overrides.
-    Ostwald-ripening parameters go by name (D, Calpha, Cbeta, A, delta, epsilon)."""
+    Ostwald-ripening parameters go by name (D, Calpha, Cbeta, A, delta, epsilon);
+    the polynomial models take a thermal noise standard deviation and seed
+    (noise, seed)."""
     L = load()
     shape = tuple(int(s) for s in shape)
     d = Desc()
@@ -191,10 +194,11 @@ def make_desc(shape, fields=1, dtype=np.float64, model="ch", dx=None, bc=None, d
     for name, v in (("dt", dt), ("kappa", kappa), ("mobility", mobility), ("gamma", gamma), ("r", r), ("u", u)):
         if v is not None:
             setattr(d, name, float(v))
+    names = OSTWALD_AUX if m == OSTWALD else NOISE_AUX
     for name, v in aux.items():
-        if name not in OSTWALD_AUX:
+        if name not in names:
             raise TypeError("unknown model parameter %r" % name)
-        d.aux[OSTWALD_AUX.index(name)] = float(v)
+        d.aux[names.index(name)] = float(v)
     return d
 
 

@@ -146,8 +146,36 @@ int pfo_laplacian(const pfo_grid* g, const double* in, double* out)
 
 /* Two-pass explicit Cahn-Hilliard in the structure of cahn-hilliard.cpp:65-80.
  * form 0: BASELINE free energy, form 1: the shipped polynomial. */
+/* Value j of the SplitMix64 stream `seed` (Steele, Lea and Flood, OOPSLA
+ * 2014), as mmsp_gb300/inputs.py and the device compute it. */
+static uint64_t splitmix64_at(uint64_t seed, uint64_t j)
+{
+    uint64_t z = seed + (j + 1u) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+/* Standard normal deviate k of stream `seed`: Box-Muller on uniforms 2k and
+ * 2k+1 (top 53 bits).  Stands in for the examples' gaussian()
+ * (model_A.cpp:13-40), whose rand()-driven polar method depends on the
+ * serial visiting order of the cells. */
+double pfo_gaussian(uint64_t seed, uint64_t k)
+{
+    const double u1 = (double)(splitmix64_at(seed, 2u * k) >> 11) * 0x1.0p-53;
+    const double u2 = (double)(splitmix64_at(seed, 2u * k + 1u) >> 11) * 0x1.0p-53;
+    return sqrt(-2.0 * log(1.0 - u1)) * cos(6.283185307179586 * u2);
+}
+
+/* gaussian(0.0, std) of cell i in step `step`, as ave + u*std (model_A.cpp:31) */
+static inline double noise_at(double nstd, uint64_t seed, long long step, long cells, long i)
+{
+    return 0.0 + pfo_gaussian(seed, (uint64_t)step * (uint64_t)cells + (uint64_t)i) * nstd;
+}
+
 static int ch_run(const pfo_grid* g, double* c, int steps, int form,
-                  double r, double u, double K, double M, double dt, int threads)
+                  double r, double u, double K, double M, double dt, int threads,
+                  double nstd, uint64_t seed, long long step0)
 {
     geo q;
     if (geo_init(&q, g) || !c || steps < 0) return -1;
@@ -169,6 +197,8 @@ static int ch_run(const pfo_grid* g, double* c, int steps, int form,
                         temp[i] = 2.0 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) - K * lap_at(&q, old, i, 1, 0, xc);
                     else
                         temp[i] = -r * phi + u * pow(phi, 3) - K * lap_at(&q, old, i, 1, 0, xc);
+                    /* model_B.cpp:100-101, spinodal.cpp:95-97: the mu pass takes + noise */
+                    if (nstd != 0.0) temp[i] = temp[i] + noise_at(nstd, seed, step0 + step, q.cells, i);
                 }
         #pragma omp parallel for schedule(static) num_threads(nt)
         for (int i0 = 0; i0 < q.n[0]; i0++)
@@ -196,13 +226,19 @@ static int ch_run(const pfo_grid* g, double* c, int steps, int form,
 int pfo_ch_baseline(const pfo_grid* g, double* c, int steps,
                     double kappa, double M, double dt, int threads)
 {
-    return ch_run(g, c, steps, 0, 0.0, 0.0, kappa, M, dt, threads);
+    return ch_run(g, c, steps, 0, 0.0, 0.0, kappa, M, dt, threads, 0.0, 0, 0);
 }
 
 int pfo_ch_shipped(const pfo_grid* g, double* c, int steps,
                    double r, double u, double K, double M, double dt, int threads)
 {
-    return ch_run(g, c, steps, 1, r, u, K, M, dt, threads);
+    return ch_run(g, c, steps, 1, r, u, K, M, dt, threads, 0.0, 0, 0);
+}
+
+int pfo_ch_shipped_noise(const pfo_grid* g, double* c, int steps, double r, double u, double K, double M,
+                         double dt, double nstd, uint64_t seed, long long step0, int threads)
+{
+    return ch_run(g, c, steps, 1, r, u, K, M, dt, threads, nstd, seed, step0);
 }
 
 /* Single-pass multi-field Allen-Cahn in the structure of graingrowth.cpp:86-110.
@@ -213,7 +249,7 @@ int pfo_ch_shipped(const pfo_grid* g, double* c, int steps,
  * form 1 with field 0 (the particles) copied unchanged. */
 static int ac_run(const pfo_grid* g, int N, double* eta, int steps, int form,
                   double gamma, double kappa, double L, double r, double u,
-                  double dt, int threads)
+                  double dt, int threads, double nstd, uint64_t seed, long long step0)
 {
     geo q;
     if (N < 1 || N > 64 || geo_init(&q, g) || !eta || steps < 0) return -1;
@@ -236,7 +272,11 @@ static int ac_run(const pfo_grid* g, int N, double* eta, int steps, int form,
                     for (int j = 0; j < N; j++) lap[j] = lap_at(&q, old, i, N, j, xc);
                     if (form == 2) {
                         double p = phi[0];
-                        out[0] = p - dt * L * (-r * p + u * pow(p, 3) - kappa * lap[0]);
+                        if (nstd != 0.0) /* model_A.cpp:99-100 */
+                            out[0] = p - dt * L * (-r * p + u * pow(p, 3) - kappa * lap[0]
+                                                   + noise_at(nstd, seed, step0 + step, q.cells, i));
+                        else
+                            out[0] = p - dt * L * (-r * p + u * pow(p, 3) - kappa * lap[0]);
                         continue;
                     }
                     /* sum of squares, graingrowth.cpp:97-101 */
@@ -269,25 +309,31 @@ static int ac_run(const pfo_grid* g, int N, double* eta, int steps, int form,
 int pfo_ac_baseline(const pfo_grid* g, int N, double* eta, int steps,
                     double gamma, double kappa, double L, double dt, int threads)
 {
-    return ac_run(g, N, eta, steps, 0, gamma, kappa, L, 0.0, 0.0, dt, threads);
+    return ac_run(g, N, eta, steps, 0, gamma, kappa, L, 0.0, 0.0, dt, threads, 0.0, 0, 0);
 }
 
 int pfo_ac_graingrowth(const pfo_grid* g, int N, double* eta, int steps,
                        double dt, int threads)
 {
-    return ac_run(g, N, eta, steps, 1, 0.0, 0.0, 1.0, 0.0, 0.0, dt, threads);
+    return ac_run(g, N, eta, steps, 1, 0.0, 0.0, 1.0, 0.0, 0.0, dt, threads, 0.0, 0, 0);
 }
 
 int pfo_ac_zener(const pfo_grid* g, int N, double* eta, int steps, double dt, int threads)
 {
-    return ac_run(g, N, eta, steps, 3, 0.0, 0.0, 1.0, 0.0, 0.0, dt, threads);
+    return ac_run(g, N, eta, steps, 3, 0.0, 0.0, 1.0, 0.0, 0.0, dt, threads, 0.0, 0, 0);
 }
 
 int pfo_ac_scalar_shipped(const pfo_grid* g, double* phi, int steps,
                           double r, double u, double K, double M, double dt,
                           int threads)
 {
-    return ac_run(g, 1, phi, steps, 2, 0.0, K, M, r, u, dt, threads);
+    return ac_run(g, 1, phi, steps, 2, 0.0, K, M, r, u, dt, threads, 0.0, 0, 0);
+}
+
+int pfo_ac_scalar_noise(const pfo_grid* g, double* phi, int steps, double r, double u, double K, double M,
+                        double dt, double nstd, uint64_t seed, long long step0, int threads)
+{
+    return ac_run(g, 1, phi, steps, 2, 0.0, K, M, r, u, dt, threads, nstd, seed, step0);
 }
 
 /* Isotropic phase-field Ostwald ripening, ostwald.cpp:84-121: field 0 the

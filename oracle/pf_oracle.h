@@ -32,6 +32,8 @@
 #ifndef PF_ORACLE_H
 #define PF_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -87,6 +89,19 @@ int pfo_ac_zener(const pfo_grid* g, int N, double* eta, int steps, double dt, in
 int pfo_ostwald(const pfo_grid* g, int N, double* eta, int steps, double dt, double L, double D,
                 double Calpha, double Cbeta, double A, double delta, double epsilon, double kappa,
                 int threads);
+
+/* Stochastic forms.  The examples add gaussian(0.0, std) to the
+ * polynomial models' mu (model_A.cpp:99-100 on the scalar Allen-Cahn update,
+ * model_B.cpp:100-101 and spinodal.cpp:95-97 on the Cahn-Hilliard mu pass), drawn
+ * from rand() in cell order.  These restatements draw the same term from a
+ * counter-based stream instead: deviate (step0 + step) * cells + cell of
+ * pfo_gaussian(seed, .), times std.  std = 0 reproduces the deterministic
+ * functions bit for bit. */
+double pfo_gaussian(uint64_t seed, uint64_t k);
+int pfo_ch_shipped_noise(const pfo_grid* g, double* c, int steps, double r, double u, double K, double M,
+                         double dt, double nstd, uint64_t seed, long long step0, int threads);
+int pfo_ac_scalar_noise(const pfo_grid* g, double* phi, int steps, double r, double u, double K, double M,
+                        double dt, double nstd, uint64_t seed, long long step0, int threads);
 
 /* Scalar Allen-Cahn exactly as shipped (allen-cahn.cpp:70):
  *   p' = p - dt*M*(-r*p + u*pow(p,3) - K*lap(p)). */

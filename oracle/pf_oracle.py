@@ -47,6 +47,10 @@ def lib():
             ("pfo_ac_graingrowth", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
             ("pfo_ac_zener", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
             ("pfo_ostwald", [gp, ctypes.c_int, dp, ctypes.c_int] + [ctypes.c_double] * 9 + [ctypes.c_int]),
+            ("pfo_ch_shipped_noise", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 6
+             + [ctypes.c_uint64, ctypes.c_longlong, ctypes.c_int]),
+            ("pfo_ac_scalar_noise", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 6
+             + [ctypes.c_uint64, ctypes.c_longlong, ctypes.c_int]),
             ("pfo_ac_scalar_shipped", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int]),
             ("pfo_laplacian", [gp, dp, dp]),
             ("pfo_ch_mass_energy", [gp, dp, ctypes.c_double, dp, dp]),
@@ -57,6 +61,8 @@ def lib():
             f.restype = ctypes.c_int
         L.pfo_pow3.argtypes = [dp, dp, ctypes.c_long]
         L.pfo_pow3.restype = None
+        L.pfo_gaussian.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        L.pfo_gaussian.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -128,6 +134,31 @@ def ostwald(eta, steps, dt=0.001, L=1.0, D=1.0, Calpha=0.05, Cbeta=0.95, A=2.0, 
     g = _grid(out.shape[:-1], dx, bc)
     _check(lib().pfo_ostwald(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps), dt, L, D, Calpha, Cbeta, A,
                              delta, epsilon, kappa, threads), "ostwald")
+    return out
+
+
+def gaussian(seed, k):
+    """Deviate k of the counter-based normal stream `seed` (pfo_gaussian)."""
+    return lib().pfo_gaussian(int(seed), int(k))
+
+
+def ch_shipped_noise(c, steps, r=1.0, u=1.0, K=1.0, M=1.0, dt=0.01, noise=0.0, seed=0, step0=0, dx=None, bc=None,
+                     threads=0):
+    """Shipped Cahn-Hilliard with gaussian(0, noise) added to mu (model B, spinodal)."""
+    out = np.array(c, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape, dx, bc)
+    _check(lib().pfo_ch_shipped_noise(ctypes.byref(g), _ptr(out), int(steps), r, u, K, M, dt, noise, int(seed),
+                                      int(step0), threads), "ch_shipped_noise")
+    return out
+
+
+def ac_scalar_noise(phi, steps, r=1.0, u=1.0, K=1.0, M=1.0, dt=0.01, noise=0.0, seed=0, step0=0, dx=None, bc=None,
+                    threads=0):
+    """Shipped scalar Allen-Cahn with gaussian(0, noise) in the bracket (model A)."""
+    out = np.array(phi, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape, dx, bc)
+    _check(lib().pfo_ac_scalar_noise(ctypes.byref(g), _ptr(out), int(steps), r, u, K, M, dt, noise, int(seed),
+                                     int(step0), threads), "ac_scalar_noise")
     return out
 
 

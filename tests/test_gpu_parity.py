@@ -466,3 +466,82 @@ def test_ostwald_reductions(gpu):
     m, e = ostwald_energy(y, dx)
     assert abs(st.mass - m) <= 1e-12 * abs(m)
     assert abs(st.energy - e) <= 1e-11 * abs(e)
+
+
+# Stochastic forms: the shipped polynomial models plus thermal noise from a
+# counter-based stream (the oracle draws the same deviates).
+# (name, model, shape, dtype, params, steps)
+KT, DT, DV = 0.01, 0.01, 1.0
+SIGMA_AB = float(np.sqrt(2.0 * KT / (DT * DV)))      # model_A.cpp:99, model_B.cpp:100: sqrt(2 kT/(dt dV))
+SIGMA_SPIN = float(np.sqrt(0.05 * DT / DV))           # spinodal.cpp:95: sqrt(epsilon dt/dV)
+NOISY = [
+    ("modelA_2d", "ac_poly", (48, 40), dict(r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=DT, noise=SIGMA_AB), 60),
+    ("modelA_3d_graph_length", "ac_poly", (12, 10, 14), dict(r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=DT,
+                                                          noise=SIGMA_AB), 150),
+    ("modelB_2d", "ch_poly", (40, 36), dict(r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=DT, noise=SIGMA_AB), 60),
+    ("modelB_3d", "ch_poly", (10, 12, 9), dict(r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=DT, noise=SIGMA_AB), 40),
+    ("spinodal_2d", "ch_poly", (64, 48), dict(r=1.0, u=1.0, kappa=1.0, mobility=0.5 / DV, dt=DT, noise=SIGMA_SPIN),
+     80),
+]
+
+
+def noisy_oracle(oracle, model, x, steps, prm, seed, step0=0):
+    kw = dict(r=prm["r"], u=prm["u"], K=prm["kappa"], M=prm["mobility"], dt=prm["dt"], noise=prm["noise"],
+              seed=seed, step0=step0)
+    if model == "ac_poly":
+        return oracle.ac_scalar_noise(x, steps, **kw)
+    return oracle.ch_shipped_noise(x, steps, **kw)
+
+
+@pytest.mark.parametrize("name,model,shape,prm,steps", NOISY, ids=[n[0] for n in NOISY])
+def test_stochastic_forms_against_oracle(gpu, oracle, name, model, shape, prm, steps):
+    from mmsp_gb300 import inputs
+
+    seed = 1234 + len(name)
+    x = inputs.noisy_composition(shape, 0.0, 0.2, 77 + len(shape))
+    want = noisy_oracle(oracle, model, x, steps, prm, seed)
+    d64 = gpu.make_desc(shape, 1, np.float64, model, seed=seed, **prm)
+    got = run_gpu(gpu, d64, x, steps)
+    assert np.abs(got - want).max() <= TOL_SHIPPED * max(1.0, np.abs(want).max())
+    d32 = gpu.make_desc(shape, 1, np.float32, model, seed=seed, **prm)
+    got32 = run_gpu(gpu, d32, x.astype(np.float32), steps).astype(np.float64)
+    assert np.abs(got32 - want).max() <= TOL_F32
+    # the noise acts: the deterministic form ends elsewhere
+    plain = dict(prm, noise=0.0)
+    assert np.abs(noisy_oracle(oracle, model, x, steps, plain, seed) - want).max() > 1e-4
+
+
+def test_stochastic_stream_is_deterministic_and_continues(gpu, oracle):
+    from mmsp_gb300 import inputs
+
+    shape = (32, 24)
+    prm = dict(r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=DT, noise=SIGMA_AB)
+    x = inputs.noisy_composition(shape, 0.0, 0.2, 5)
+    d = gpu.make_desc(shape, 1, np.float64, "ch_poly", seed=9, **prm)
+    a = run_gpu(gpu, d, x, 30)
+    assert np.array_equal(a, run_gpu(gpu, d, x, 30))                  # same seed, same bits
+    with gpu.Stepper(d) as s:                                         # steps split over calls
+        s.upload(x)
+        s.step(12)
+        s.step(18)
+        assert np.array_equal(s.download(), a)
+    d2 = gpu.make_desc(shape, 1, np.float64, "ch_poly", seed=10, **prm)
+    assert not np.array_equal(run_gpu(gpu, d2, x, 30), a)             # another seed, another path
+    # a new upload restarts the stream at step 0
+    with gpu.Stepper(d) as s:
+        s.upload(x)
+        s.step(7)
+        s.upload(x)
+        s.step(30)
+        assert np.array_equal(s.download(), a)
+
+
+def test_stochastic_forms_are_refused_where_no_step_index_travels(gpu):
+    d = gpu.make_desc((64, 64), 1, np.float32, "ch_poly", noise=0.1, seed=1)
+    with pytest.raises(gpu.GpuError) as e:
+        gpu.Batch([d, d])
+    assert e.value.code == gpu.EUNSUPPORTED
+    bad = gpu.make_desc((8, 8), 1, np.float64, "ch_poly", noise=-1.0)
+    with pytest.raises(gpu.GpuError) as e:
+        gpu.Stepper(bad)
+    assert e.value.code == gpu.EINVAL
