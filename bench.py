@@ -240,25 +240,30 @@ def other_configs(native, inputs, stream):
 
 def other_models(native, inputs, timed):
     """The further explicit models on the same device path: Zener pinning
-    (grain growth with the particle field fixed) on 128^3 x 3 fields and
+    (grain growth with the particle field fixed) on 128^3 x 3 fields,
     Ostwald ripening (composition + order parameter, two kernels per step)
     on 256 x 128 x 64 x 2 fields (the example's 128 x 64 x 16, doubled per
-    axis), 500 steps each in FP32 and FP64, beside the oracle (the
-    reference's loops restated in C, FP64, one thread) on 2 steps."""
+    axis) and model B (Cahn-Hilliard with thermal noise) on 1024^2, 500
+    steps each in FP32 and FP64, beside the oracle (the reference's loops
+    restated in C, FP64, one thread) on 2 steps."""
     from oracle import pf_oracle
 
     peak = peaks()[0]
     out = {}
+    sigma = float(np.sqrt(2.0 * 0.01 / 0.01))   # model B: sqrt(2 kT/(dt dV)), kT = dt = 0.01, dV = 1
     cases = [
-        ("zener3d_128_n3_500", (128, 128, 128), 3, "zener", inputs.zener_particles((128, 128, 128), 400, 9),
+        ("zener3d_128_n3_500", (128, 128, 128), 3, "zener", {}, inputs.zener_particles((128, 128, 128), 400, 9),
          lambda x, n: pf_oracle.ac_zener(x, n, 0.01, threads=1)),
-        ("ostwald3d_256x128x64_n2_500", (256, 128, 64), 2, "ostwald", inputs.ostwald_start((256, 128, 64), 2, 9),
-         lambda x, n: pf_oracle.ostwald(x, n, threads=1)),
+        ("ostwald3d_256x128x64_n2_500", (256, 128, 64), 2, "ostwald", {},
+         inputs.ostwald_start((256, 128, 64), 2, 9), lambda x, n: pf_oracle.ostwald(x, n, threads=1)),
+        ("modelB2d_1024_noise_500", (1024, 1024), 1, "ch_poly", dict(dt=0.01, noise=sigma, seed=3),
+         inputs.noisy_composition((1024, 1024), 0.0, 0.1, 9),
+         lambda x, n: pf_oracle.ch_shipped_noise(x, n, dt=0.01, noise=sigma, seed=3, threads=1)),
     ]
-    for name, shape, fields, model, x, cpu in cases:
+    for name, shape, fields, model, kw, x, cpu in cases:
         steps = 500
-        d32 = native.make_desc(shape, fields, np.float32, model)
-        d64 = native.make_desc(shape, fields, np.float64, model)
+        d32 = native.make_desc(shape, fields, np.float32, model, **kw)
+        d64 = native.make_desc(shape, fields, np.float64, model, **kw)
         ms32, o32 = timed(d32, x.astype(np.float32), steps)
         ms64, o64 = timed(d64, x, steps)
         vals = int(np.prod(shape)) * fields * steps

@@ -71,14 +71,30 @@ static __device__ __forceinline__ double gauss_at(unsigned long long seed, unsig
     return sqrt(-2.0 * log(1.0 - u1)) * cos(6.283185307179586 * u2);
 }
 
+// The same deviate in single precision for the FP32 form, without FP64
+// arithmetic: 1 - u1 is formed exactly in the integers from the 53-bit u1
+// before it is rounded to float, so the logarithm keeps its accuracy as u1
+// approaches 1; u2 keeps its top 24 bits.  Within a few 1e-7 of gauss_at.
+static __device__ __forceinline__ float gauss_at_f(unsigned long long seed, unsigned long long k)
+{
+    const unsigned long long m1 = splitmix64_at(seed, 2ULL * k) >> 11;            // u1 = m1 * 2^-53
+    const float t = (float)((1ULL << 53) - m1) * 0x1.0p-53f;                        // 1 - u1, in (0, 1]
+    const float u2 = (float)(splitmix64_at(seed, 2ULL * k + 1ULL) >> 40) * 0x1.0p-24f;
+    return sqrtf(-2.0f * logf(t)) * cosf(6.28318530717958648f * u2);
+}
+
 // The noise term of cell `cell` in the current step, std * N(0,1), as the
 // examples' gaussian(0.0, std) returns it (model_A.cpp:13-40: ave + u*std),
-// narrowed to the state type.
-template <typename T>
-static __device__ __forceinline__ T noise_at(const P<T>& p, long long cells, long long cell)
+// in the state type.
+static __device__ __forceinline__ double noise_at(const P<double>& p, long long cells, long long cell)
 {
     const unsigned long long k = (unsigned long long)p.step * (unsigned long long)cells + (unsigned long long)cell;
-    return (T)(0.0 + gauss_at(p.seed, k) * p.noise);
+    return 0.0 + gauss_at(p.seed, k) * p.noise;
+}
+static __device__ __forceinline__ float noise_at(const P<float>& p, long long cells, long long cell)
+{
+    const unsigned long long k = (unsigned long long)p.step * (unsigned long long)cells + (unsigned long long)cell;
+    return gauss_at_f(p.seed, k) * (float)p.noise;
 }
 
 // 2.0*y, which is exact.  For FP64 a normal y whose double stays finite is
