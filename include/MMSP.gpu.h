@@ -57,6 +57,7 @@ extern "C" {
 #define MMSP_GPU_ECANCELED    -8  /* request cancelled (server) */
 #define MMSP_GPU_ESTOPPED     -9  /* server stopped */
 #define MMSP_GPU_EIO         -10  /* a grid file could not be opened or written */
+#define MMSP_GPU_ENOCONV     -11  /* an implicit solve reached its iteration limit (the reference aborts) */
 
 /* Boundary-condition codes, identical to include/MMSP.utility.h:23-29. */
 #define MMSP_GPU_BC_MIRROR    0
@@ -96,6 +97,15 @@ extern "C" {
                                 with Cm = (Ca+Cb)/2, B = A/(Cb-Cm)^2, g = 2/(Cb-Ca)^2,
                                 Da = Db = g/delta^2 (ostwald.cpp:67-80); L = mobility;
                                 D, Ca, Cb, A, delta, eps in aux[0..5]                         */
+#define MMSP_GPU_CH_CONVEX 7 /* semi-implicit convex-splitting Cahn-Hilliard as shipped
+                                (examples/phase_transitions/cahn-hilliard/convex_splitting/
+                                cahn-hilliard.cpp:273-463, parametric free energy), FP64, fields = 2
+                                (c, mu), even extents: each step solves the linearised system by
+                                red-black successive over-relaxation until the relative residual
+                                falls below the tolerance (checked after iterations 1-4 and every
+                                5th), starting from the state two steps back as the example does.
+                                mobility = D, kappa = K; aux = {C0, Ca, Cb, A, omega, tolerance};
+                                at most 10000 iterations per step (MMSP_GPU_ENOCONV beyond)    */
 
 /* Host/device layouts of vector-valued grids (fields > 1). */
 #define MMSP_GPU_CELL_MAJOR  0  /* value j of cell i at i*fields + j (grid<dim,vector<T>> order) */
@@ -130,6 +140,7 @@ typedef struct mmsp_gpu_stats {
     double energy;    /* dV * sum of the model's free-energy density + kappa/2 |grad|^2 */
     double gpu_ms;    /* device time of the last mmsp_gpu_step call, CUDA events on the handle's stream */
     int64_t steps;    /* steps advanced since the last upload */
+    int64_t solver_iterations;  /* MMSP_GPU_CH_CONVEX: red-black iterations of the last step's solve */
 } mmsp_gpu_stats;
 
 typedef struct mmsp_gpu_handle mmsp_gpu_handle;
@@ -246,8 +257,8 @@ int mmsp_gpu_output_wait(mmsp_gpu_handle* h);
  * advanced together.  The reference has no batched path (one update() per
  * grid, cahn-hilliard.cpp:47-81); this replaces a loop of those calls.
  *
- * MMSP_GPU_OSTWALD grids are not batched (EUNSUPPORTED); handles and the
- * server take them.
+ * MMSP_GPU_OSTWALD, MMSP_GPU_CH_CONVEX and noisy grids are not batched
+ * (EUNSUPPORTED); handles and the server take them.
  * 2D Cahn-Hilliard grids (MMSP_GPU_CH / MMSP_GPU_CH_POLY, fields=1) whose
  * rows hold a multiple of 32 cells up to 512 share one persistent kernel per
  * step: a work list of (grid, run of rows) items is drained by all warps of
@@ -374,8 +385,9 @@ int mmsp_gpu_server_stop(mmsp_gpu_server* s);
  * out.  The first call on a device looks up the array's device address
  * with that device current; make that first call before any stream capture.
  * Calls that overlap on the GPU (from several threads or streams) share the
- * scratch array and race: serialise them.  MMSP_GPU_OSTWALD, whose step
- * needs a work grid beside the state, returns MMSP_GPU_EUNSUPPORTED. */
+ * scratch array and race: serialise them.  MMSP_GPU_OSTWALD (its step needs a
+ * work grid beside the state), MMSP_GPU_CH_CONVEX (an iterative solve per
+ * step) and the noisy polynomial forms return MMSP_GPU_EUNSUPPORTED. */
 int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, void* out, int steps,
                           void* cuda_stream);
 

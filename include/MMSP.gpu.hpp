@@ -113,6 +113,15 @@ inline Model spinodal(double dt = 0.01, double dV = 1.0, double epsilon = 0.05, 
                {std::sqrt(epsilon * dt / dV), seed, 0.0, 0.0, 0.0, 0.0}};
     return m;
 }
+// examples/phase_transitions/cahn-hilliard/convex_splitting/cahn-hilliard.cpp:273-463 as shipped
+// (parametric energy), on grid<dim,vector<double> > with fields c and mu, FP64, even extents
+inline Model cahn_hilliard_convex_splitting(double C0 = 0.45, double Ca = 0.05, double Cb = 0.95, double A = 2.0,
+                                            double K = 2.0, double omega = 1.2, double tolerance = 1.0e-14)
+{
+    const double D = 2.0 / (Cb - Ca);
+    Model m = {MMSP_GPU_CH_CONVEX, 1.0 / (D * K), K, D, 1.0, 0.0, 0.0, {C0, Ca, Cb, A, omega, tolerance}};
+    return m;
+}
 // allen-cahn.cpp:57-70 as shipped (scalar grid)
 inline Model allen_cahn_shipped(double r, double u, double K, double M, double dt)
 {

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <new>
+#include <string>
 
 #include "MMSP.gpu.h"
 #include "pf_handle.h"
@@ -48,6 +49,7 @@ extern "C" const char* mmsp_gpu_strerror(int code)
     case MMSP_GPU_ECANCELED: return "cancelled";
     case MMSP_GPU_ESTOPPED: return "server stopped";
     case MMSP_GPU_EIO: return "grid file could not be written";
+    case MMSP_GPU_ENOCONV: return "implicit solver did not converge";
     default: return "unknown status";
     }
 }
@@ -77,6 +79,17 @@ extern "C" int mmsp_gpu_desc_init(mmsp_gpu_desc* d, int dim, const int* n, int f
     case MMSP_GPU_GG: d->dt = 0.01; d->kappa = 2.0; break;        // graingrowth.cpp:84
     case MMSP_GPU_AC_POLY: d->dt = 0.01; break;                   // allen-cahn.cpp:57-61
     case MMSP_GPU_ZENER: d->dt = 0.01; d->kappa = 2.0; break;     // zener.cpp:115
+    case MMSP_GPU_CH_CONVEX:   // convex_splitting/cahn-hilliard.cpp:38-67 (parametric energy)
+        d->mobility = 2.0 / (0.95 - 0.05);    // D = 2/(Cb-Ca)
+        d->kappa = 2.0;                       // K
+        d->dt = pow(1.0, 2.0) / (d->mobility * d->kappa);
+        d->aux[0] = 0.45;    // C0
+        d->aux[1] = 0.05;    // Ca
+        d->aux[2] = 0.95;    // Cb
+        d->aux[3] = 2.0;     // A
+        d->aux[4] = 1.2;     // omega
+        d->aux[5] = 1.0e-14; // tolerance
+        break;
     case MMSP_GPU_OSTWALD:                                        // ostwald.cpp:66-80
         d->dt = 0.001;
         d->kappa = 2.0;
@@ -98,7 +111,7 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     if (!d) BAD(MMSP_GPU_EINVAL, "NULL descriptor");
     if (d->dim < 1 || d->dim > 3) BAD(MMSP_GPU_EINVAL, "dim %d outside 1..3", d->dim);
     if (d->dtype != MMSP_GPU_F64 && d->dtype != MMSP_GPU_F32) BAD(MMSP_GPU_EINVAL, "dtype %d", d->dtype);
-    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_OSTWALD) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
+    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_CH_CONVEX) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
     long long cells = 1;
     for (int a = 0; a < d->dim; a++) {
         if (d->n[a] < 1) BAD(MMSP_GPU_EINVAL, "extent n[%d]=%d", a, d->n[a]);
@@ -115,6 +128,17 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     bool scalar_model = d->model == MMSP_GPU_CH || d->model == MMSP_GPU_CH_POLY || d->model == MMSP_GPU_AC_POLY;
     if (scalar_model && d->fields != 1) BAD(MMSP_GPU_EINVAL, "model %d takes fields=1, got %d", d->model, d->fields);
     if (d->fields < 1) BAD(MMSP_GPU_EINVAL, "fields=%d", d->fields);
+    if (d->model == MMSP_GPU_CH_CONVEX) {
+        if (d->fields != 2) BAD(MMSP_GPU_EINVAL, "convex splitting takes fields=2 (c, mu), got %d", d->fields);
+        if (d->dtype != MMSP_GPU_F64)
+            BAD(MMSP_GPU_EUNSUPPORTED, "convex splitting runs in FP64 (its residual tolerance is below FP32)");
+        for (int a = 0; a < d->dim; a++)
+            if (d->n[a] % 2)
+                BAD(MMSP_GPU_EUNSUPPORTED, "convex splitting needs even extents for an order-free red-black sweep, "
+                                           "n[%d]=%d", a, d->n[a]);
+        if (!(d->aux[4] > 0.0 && d->aux[4] < 2.0) || !(d->aux[5] > 0.0) || !(d->aux[1] != d->aux[0]))
+            BAD(MMSP_GPU_EINVAL, "convex splitting: omega in (0,2), tolerance > 0 and Ca != C0");
+    }
     if (d->model == MMSP_GPU_OSTWALD && d->fields < 2)
         BAD(MMSP_GPU_EINVAL, "Ostwald ripening takes a composition and at least one order parameter, fields=%d",
             d->fields);
@@ -149,9 +173,11 @@ static size_t state_bytes(const mmsp_gpu_desc* d)
 }
 
 // Device scratch of a model beyond the two state buffers: the Ostwald
-// model's chemical-potential grid (one value per cell).
+// model's chemical-potential grid (one value per cell); for convex
+// splitting, a staging copy of the state for cell-major downloads.
 static size_t work_bytes(const mmsp_gpu_desc* d)
 {
+    if (d->model == MMSP_GPU_CH_CONVEX) return state_bytes(d);   // download staging (the guess stays put)
     if (d->model != MMSP_GPU_OSTWALD) return 0;
     return state_bytes(d) / (size_t)d->fields;
 }
@@ -181,6 +207,11 @@ static void release(mmsp_gpu_handle* h)
 
 static int make_plan(mmsp_gpu_handle* h)
 {
+    if (h->d.model == MMSP_GPU_CH_CONVEX) {   // kernels are launched directly (pf_convex.cu)
+        h->plan.kind = 5;
+        h->plan.ok = true;
+        return MMSP_GPU_OK;
+    }
     bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
     cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::plan_ostwald(h->d, h->g, &h->plan)
                     : ch ? pf::plan_ch(h->d, h->g, &h->plan) : pf::plan_ac(h->d, h->g, &h->plan);
@@ -294,6 +325,11 @@ static int upload(mmsp_gpu_handle* h, const void* src, size_t bytes, int layout,
         e = pf::launch_transpose(h->d.dtype, h->buf[1], h->buf[0], h->g.cells, h->d.fields, true, h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, "upload transpose");
     }
+    if (h->d.model == MMSP_GPU_CH_CONVEX) {
+        // the solver's first guess is a copy of the state (newGrid.copy(oldGrid), cahn-hilliard.cpp:283)
+        e = cudaMemcpyAsync(h->buf[1], h->buf[0], h->bytes, cudaMemcpyDeviceToDevice, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "upload guess");
+    }
     h->steps = 0;
     h->timed = false;
     if (sync && (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(h, e, "upload sync");
@@ -308,11 +344,13 @@ static int download(mmsp_gpu_handle* h, void* dst, size_t bytes, int layout, cud
     const void* src = h->buf[h->cur];
     cudaError_t e;
     if (transpose) {
-        // the other state buffer is free between steps
-        e = pf::launch_transpose(h->d.dtype, h->buf[h->cur], h->buf[h->cur ^ 1], h->g.cells, h->d.fields, false,
-                                 h->stream);
+        // the other state buffer is free between steps, except for convex
+        // splitting, whose next solve starts from it: that model stages in its
+        // work buffer
+        void* staging = h->d.model == MMSP_GPU_CH_CONVEX ? h->work : h->buf[h->cur ^ 1];
+        e = pf::launch_transpose(h->d.dtype, h->buf[h->cur], staging, h->g.cells, h->d.fields, false, h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, "download transpose");
-        src = h->buf[h->cur ^ 1];
+        src = staging;
     }
     e = cudaMemcpyAsync(dst, src, bytes, kind, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "download");
@@ -386,6 +424,47 @@ static int build_graph(mmsp_gpu_handle* h)
     return MMSP_GPU_OK;
 }
 
+// Convex-splitting Cahn-Hilliard: each step iterates red-black sweeps of
+// the guess buf[cur^1] (which holds the state two steps back, as the
+// example's swap leaves it) until the relative residual is at most the
+// tolerance, checked after iterations 1-4 and every 5th
+// (cahn-hilliard.cpp:311-388); then the guess becomes the state.
+static const unsigned kCsMaxIter = 10000;    // max_iter, cahn-hilliard.cpp:55
+static const unsigned kCsResidualStep = 5;   // residual_step, cahn-hilliard.cpp:54
+static int convex_steps(mmsp_gpu_handle* h, int steps)
+{
+    cudaError_t e;
+    double host[2];
+    for (int k = 0; k < steps; k++) {
+        const void* old = h->buf[h->cur];
+        void* nw = h->buf[h->cur ^ 1];
+        double residual = 1.0;
+        unsigned iter = 0;
+        while (iter < kCsMaxIter && residual > h->c.cs.tol) {
+            if ((e = pf::launch_convex_sweeps(h->d, h->g, h->c, old, nw, h->stream)) != cudaSuccess)
+                return cuda_fail(h, e, "convex sweep");
+            iter++;
+            if (iter < kCsResidualStep || iter % kCsResidualStep == 0) {
+                if ((e = pf::launch_convex_residual(h->d, h->g, h->c, old, nw, h->partials, h->stream)) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(host, h->partials + 4 * pf::kReduceBlocks, sizeof(host), cudaMemcpyDeviceToHost,
+                                         h->stream)) != cudaSuccess ||
+                    (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+                    return cuda_fail(h, e, "convex residual");
+                residual = sqrt(host[0] / host[1]) / (2.0 * h->c.cs.cells);
+            }
+        }
+        h->last_iters = iter;
+        if (iter == kCsMaxIter) {
+            char msg[64];
+            snprintf(msg, sizeof(msg), "%u iterations, residual %.3g", iter, residual);
+            return fail(h, MMSP_GPU_ENOCONV, "convex splitting stagnated on step %s: %s",
+                        std::to_string(h->steps + k).c_str(), msg);
+        }
+        h->cur ^= 1;   // swap(oldGrid, newGrid), cahn-hilliard.cpp:409
+    }
+    return MMSP_GPU_OK;
+}
+
 extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
 {
     if (!h || steps < 0) return MMSP_GPU_EINVAL;
@@ -393,7 +472,11 @@ extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
     cudaError_t e = cudaEventRecord(h->ev0, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "event");
     int left = steps;
-    if (pf::noisy(h->d)) {
+    if (h->d.model == MMSP_GPU_CH_CONVEX) {
+        int rc = convex_steps(h, steps);
+        if (rc) return rc;
+        left = 0;
+    } else if (pf::noisy(h->d)) {
         // the step index is a kernel argument, so no graph replay
         for (int k = 0; k < steps; k++)
             if ((e = one_step(h, h->stream, h->steps + k)) != cudaSuccess) return cuda_fail(h, e, "step");
@@ -455,6 +538,7 @@ extern "C" int mmsp_gpu_reduce(mmsp_gpu_handle* h, mmsp_gpu_stats* st)
     st->mass = res[0];
     st->energy = res[1];
     st->steps = h->steps;
+    st->solver_iterations = h->last_iters;
     st->gpu_ms = 0.0;
     if (h->timed) {
         float ms = 0.f;

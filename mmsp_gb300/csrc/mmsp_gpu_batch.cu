@@ -109,7 +109,8 @@ extern "C" int mmsp_gpu_batch_create(mmsp_gpu_batch** out, int count, const mmsp
         if (rc) return rc;
         if (descs[i].dtype != descs[0].dtype) return MMSP_GPU_EINVAL;
         // serve these through handles: a work grid, or a per-step noise index
-        if (descs[i].model == MMSP_GPU_OSTWALD || pf::noisy(descs[i])) return MMSP_GPU_EUNSUPPORTED;
+        if (descs[i].model == MMSP_GPU_OSTWALD || descs[i].model == MMSP_GPU_CH_CONVEX || pf::noisy(descs[i]))
+            return MMSP_GPU_EUNSUPPORTED;
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {

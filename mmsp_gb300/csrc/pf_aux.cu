@@ -68,6 +68,35 @@ Coeffs make_coeffs(const mmsp_gpu_desc& d)
         c.noise = d.aux[0];
         c.seed = (unsigned long long)d.aux[1];
     }
+    if (d.model == MMSP_GPU_CH_CONVEX) {
+        // cahn-hilliard.cpp (convex splitting) :38-96 and :293-298, the same expressions
+        CsConst& q = c.cs;
+        const double D = d.mobility, K = d.kappa, dt = d.dt;
+        const double C0 = d.aux[0], Ca = d.aux[1], Cb = d.aux[2], A = d.aux[3];
+        const double B = A / pow(Ca - C0, 2.0);
+        double lapWeight = 0.0, gridSize = 1.0;
+        for (int a = 0; a < d.dim; a++) {
+            lapWeight += 2.0 / pow(d.dx[a], 2.0);
+            gridSize *= (double)d.n[a];
+        }
+        q.A12 = dt * D * lapWeight;
+        q.KL = K * lapWeight;
+        q.Ddt = D * dt;
+        q.K = K;
+        q.A = A;
+        q.C0 = C0;
+        q.B = B;
+        q.Ca = Ca;
+        q.Cb = Cb;
+        q.QA = B + Ca + Cb;
+        q.QB = 3.0 * (B * C0 + Ca * Ca + Cb * Cb);
+        q.QC = 3.0 * (B * C0 * C0 + pow(Ca, 3.0) + pow(Cb, 3.0));
+        q.QD = B * pow(C0, 3.0) + pow(Ca, 4.0) + pow(Cb, 4.0);
+        q.omega = d.aux[4];
+        q.om1 = 1.0 - d.aux[4];
+        q.tol = d.aux[5];
+        q.cells = gridSize;
+    }
     if (d.model == MMSP_GPU_OSTWALD) {
         // ostwald.cpp:67-80, with the same pow calls
         OstConst& o = c.ost;
@@ -117,6 +146,7 @@ struct RedArgs {
     double wg[3];          // gradient weights of padded axes X, Y, Z (0 for padding)
     double kappa, gamma, r, u;
     OstConst ost;
+    CsConst cs;
     int model;
 };
 
@@ -168,6 +198,16 @@ __global__ void __launch_bounds__(256) reduce_kernel(const T* __restrict__ st, G
                 f = -0.5 * a.r * c2 + 0.25 * a.u * c2 * c2;
             }
             nadd(e, f + 0.5 * a.kappa * gsq(st, g, a, x, y, z));
+            nadd(m, C);
+        } else if (a.model == MMSP_GPU_CH_CONVEX) {
+            // reportEnergy of the example (cahn-hilliard.cpp:172-200): energy_density(C)
+            // + K/2 |grad C|^2 and the mass of C (field 1, the chemical potential, is not summed)
+            const CsConst& q = a.cs;
+            const double C = (double)st[i];
+            const double d0 = C - q.C0, da = C - q.Ca, db = C - q.Cb;
+            const double f = -0.5 * q.A * d0 * d0 + 0.25 * q.B * d0 * d0 * d0 * d0 + 0.25 * q.Ca * da * da * da * da +
+                             0.25 * q.Cb * db * db * db * db;
+            nadd(e, f + 0.5 * q.K * gsq(st, g, a, x, y, z));
             nadd(m, C);
         } else if (a.model == MMSP_GPU_OSTWALD) {
             // f = -A/2 (C-Cm)^2 + B/4 (C-Cm)^4 + Da/4 (C-Ca)^4 + Db/4 (C-Cb)^4 - g/2 (C-Ca)^2 sum e^2
@@ -259,6 +299,7 @@ cudaError_t launch_reduce(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c
     a.u = d.u;
     a.model = d.model;
     a.ost = c.ost;
+    a.cs = c.cs;
     int N = d.fields;
     if (gg) a.kappa = 2.0;   // graingrowth.cpp:105, zener.cpp:135: lap enters as 2*lap
     if (d.dtype == MMSP_GPU_F64)

@@ -23,7 +23,8 @@ struct mmsp_gpu_handle {
     void* buf[2];
     int cur;                 // buf[cur] holds the state
     double* partials;        // reduction scratch
-    void* work;              // MMSP_GPU_OSTWALD: the chemical-potential grid (cells values)
+    void* work;              // MMSP_GPU_OSTWALD: the chemical-potential grid (cells values);
+                             // MMSP_GPU_CH_CONVEX: download staging (state size)
     int* flags;              // device error word: a kernel's bounded wait ran out
     cudaStream_t own;        // private stream
     cudaStream_t stream;     // stream in use
@@ -33,5 +34,6 @@ struct mmsp_gpu_handle {
     // CUDA graph of kGraphSteps steps starting from buf[0] (an even count ends in buf[0])
     cudaGraphExec_t graph;
     pf::OutputState* out;    // snapshot writer (mmsp_gpu_output), created on first use
+    unsigned last_iters;     // MMSP_GPU_CH_CONVEX: solver iterations of the last step
     char err[512];
 };

@@ -26,6 +26,19 @@ struct OstConst {
     double dtD, dtL;   // dt*D and dt*L, as the update multiplies them (ostwald.cpp:108,117)
 };
 
+// Constants of the convex-splitting Cahn-Hilliard solve, as the example
+// defines them (cahn-hilliard.cpp:38-96, :293-298, :316-318).
+struct CsConst {
+    double A12;         // dt*D*lapWeight
+    double KL;          // K*lapWeight
+    double Ddt;         // D*dt
+    double K, A, C0, B, Ca, Cb;
+    double QA, QB, QC, QD;
+    double omega, om1;  // omega and 1 - omega
+    double tol;         // residual tolerance
+    double cells;       // gridSize
+};
+
 // Model constants in double; the launchers narrow them to the state type.
 struct Coeffs {
     double w[3];       // 1/(dx*dx) per real axis, MMSP axis order (grid.cpp:2062)
@@ -38,6 +51,7 @@ struct Coeffs {
     double dV;         // cell volume
     bool unit_w;       // every w == 1.0 exactly
     OstConst ost;      // MMSP_GPU_OSTWALD
+    CsConst cs;        // MMSP_GPU_CH_CONVEX
     // Thermal noise of MMSP_GPU_CH_POLY / MMSP_GPU_AC_POLY (aux[0], aux[1]):
     // standard deviation (0: none), stream seed, and the index of the step
     // being launched (steps since the last upload).
@@ -107,6 +121,15 @@ cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, 
 cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ostwald(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
                            const void* in, void* out, void* work, cudaStream_t s);
+
+// Convex-splitting Cahn-Hilliard (pf_convex.cu).  One red-black sweep
+// (color 1, then color 0 as the example orders them) of the guess `nw`
+// given the old state; and the residual reduction into partials
+// (result[0..1] = residual sum, norm of B, as launch_reduce leaves them).
+cudaError_t launch_convex_sweeps(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* old,
+                                 void* nw, cudaStream_t s);
+cudaError_t launch_convex_residual(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* old,
+                                   const void* nw, double* partials, cudaStream_t s);
 
 // Reductions: partial sums of (mass, energy) per block into `partials`
 // (4 doubles per block: mass sum, mass compensation, energy sum, energy

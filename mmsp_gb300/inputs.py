@@ -143,3 +143,28 @@ def ostwald_start(shape, fields: int, seed: int) -> np.ndarray:
     for j in range(2, fields):
         eta[..., j] = 0.1 * uniform(seed, n, start=j * n).reshape(shape)
     return eta
+
+
+def convex_start(shape, seed=None, C0: float = 0.45, K: float = 2.0, Ca: float = 0.05, Cb: float = 0.95,
+                 A: float = 2.0) -> np.ndarray:
+    """Start state of the convex-splitting Cahn-Hilliard example
+    (examples/phase_transitions/cahn-hilliard/convex_splitting/cahn-hilliard.cpp:
+    229-250): c = C0 (1 + 0.1 cos(q . x)) with q = 0.1 (sqrt 2, sqrt 3, sqrt 5)
+    (the 2D benchmark stripes) or, with a seed, c = C0 + 0.25 U(0,1) - 0.125;
+    then mu = f'(c) - K lap c with the parametric f of :57-96 (periodic,
+    dx = 1).  Shape grid_shape + (2,), cell-major (c, mu)."""
+    shape = tuple(int(s) for s in shape)
+    if seed is None:
+        q = (0.1 * np.sqrt(2.0), 0.1 * np.sqrt(3.0), 0.1 * np.sqrt(5.0))
+        x = np.indices(shape).astype(np.float64)
+        wave = sum(x[a] * q[a] for a in range(len(shape)))
+        c = C0 * (1.0 + 0.1 * np.cos(wave))
+    else:
+        c = C0 + 0.25 * uniform(seed, int(np.prod(shape))).reshape(shape) - 0.125
+    B = A / (Ca - C0) ** 2
+    dfdc = -A * (c - C0) + B * (c - C0) ** 3 + Ca * (c - Ca) ** 3 + Cb * (c - Cb) ** 3
+    lap = sum(np.roll(c, 1, a) + np.roll(c, -1, a) - 2.0 * c for a in range(len(shape)))
+    out = np.empty(shape + (2,))
+    out[..., 0] = c
+    out[..., 1] = dfdc - K * lap
+    return out

@@ -13,17 +13,18 @@ import numpy as np
 
 from . import build as _build
 
-OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED, ESTOPPED, EIO = \
-    0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10
+OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED, ESTOPPED, EIO, ENOCONV = \
+    0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10, -11
 BC_MIRROR, BC_NEUMANN, BC_PERIODIC, BC_PARALLEL, BC_DIRICHLET = 0, 1, 2, 3, 4
 F64, F32 = 0, 1
-CH, CH_POLY, AC, GG, AC_POLY, ZENER, OSTWALD = 0, 1, 2, 3, 4, 5, 6
+CH, CH_POLY, AC, GG, AC_POLY, ZENER, OSTWALD, CH_CONVEX = 0, 1, 2, 3, 4, 5, 6, 7
 CELL_MAJOR, FIELD_MAJOR = 0, 1
 
 MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY, "zener": ZENER,
-          "ostwald": OSTWALD}
+          "ostwald": OSTWALD, "ch_convex": CH_CONVEX}
 OSTWALD_AUX = ("D", "Calpha", "Cbeta", "A", "delta", "epsilon")   # mmsp_gpu_desc.aux of MMSP_GPU_OSTWALD
 NOISE_AUX = ("noise", "seed")   # mmsp_gpu_desc.aux of MMSP_GPU_CH_POLY / MMSP_GPU_AC_POLY
+CONVEX_AUX = ("C0", "Ca", "Cb", "A", "omega", "tolerance")   # mmsp_gpu_desc.aux of MMSP_GPU_CH_CONVEX
 DTYPES = {np.dtype(np.float64): F64, np.dtype(np.float32): F32}
 
 # Every symbol include/MMSP.gpu.h declares (checked by the CPU test suite).
@@ -59,7 +60,7 @@ class OutputOpts(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("mass", ctypes.c_double), ("energy", ctypes.c_double), ("gpu_ms", ctypes.c_double),
-                ("steps", ctypes.c_int64)]
+                ("steps", ctypes.c_int64), ("solver_iterations", ctypes.c_int64)]
 
 
 class BatchInfo(ctypes.Structure):
@@ -194,7 +195,7 @@ def make_desc(shape, fields=1, dtype=np.float64, model="ch", dx=None, bc=None, d
     for name, v in (("dt", dt), ("kappa", kappa), ("mobility", mobility), ("gamma", gamma), ("r", r), ("u", u)):
         if v is not None:
             setattr(d, name, float(v))
-    names = OSTWALD_AUX if m == OSTWALD else NOISE_AUX
+    names = OSTWALD_AUX if m == OSTWALD else CONVEX_AUX if m == CH_CONVEX else NOISE_AUX
     for name, v in aux.items():
         if name not in names:
             raise TypeError("unknown model parameter %r" % name)

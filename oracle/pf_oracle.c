@@ -408,6 +408,106 @@ int pfo_ostwald(const pfo_grid* g, int N, double* eta, int steps, double dt, dou
     return 0;
 }
 
+/* Convex-splitting Cahn-Hilliard, update() of
+ * examples/phase_transitions/cahn-hilliard/convex_splitting/cahn-hilliard.cpp:273-463
+ * with the parametric free energy (:38-96) and the constants as arguments.
+ * cm is cell-major (c, mu).  Serial red-black sweeps in cell order, the
+ * residual of :353-388 after iterations 1-4 and every 5th, the guess of the
+ * next step being the state two steps back (newGrid after swap).  Returns
+ * -2 when a step reaches max_iter; *iters receives the iterations of the
+ * last step. */
+int pfo_ch_convex(const pfo_grid* g, double* cm, int steps, double dt, double D, double K, double C0,
+                  double Ca, double Cb, double A, double omega, double tolerance, int* iters)
+{
+    geo q;
+    if (geo_init(&q, g) || !cm || steps < 0) return -1;
+    const double B = A / pow(Ca - C0, 2.0);
+    const double QA = B + Ca + Cb;
+    const double QB = 3.0 * (B * C0 + Ca * Ca + Cb * Cb);
+    const double QC = 3.0 * (B * C0 * C0 + pow(Ca, 3.0) + pow(Cb, 3.0));
+    const double QD = B * pow(C0, 3.0) + pow(Ca, 4.0) + pow(Cb, 4.0);
+    const unsigned residual_step = 5, max_iter = 10000;
+    double lapWeight = 0.0;
+    for (int a = 0; a < q.dim; a++) lapWeight += 2.0 / pow(g->dx[a], 2.0);
+    const double gridSize = (double)q.cells;
+    double* nw = (double*)malloc(sizeof(double) * 2 * (size_t)q.cells);
+    if (!nw) { geo_free(&q); return -1; }
+    memcpy(nw, cm, sizeof(double) * 2 * (size_t)q.cells);   /* newGrid.copy(oldGrid) */
+    double* old = cm;
+    int rc = 0;
+    for (int step = 0; step < steps && rc == 0; step++) {
+        double residual = 1.0;
+        unsigned iter = 0;
+        while (iter < max_iter && residual > tolerance) {
+            for (int color = 1; color > -1; color--)
+                for (int i0 = 0; i0 < q.n[0]; i0++)
+                    for (int i1 = 0; i1 < q.n[1]; i1++)
+                        for (int i2 = 0; i2 < q.n[2]; i2++) {
+                            if ((i0 + i1 + i2) % 2 == color) continue;
+                            int xc[3] = {i0, i1, i2};
+                            long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                            double cOld = old[2 * i];
+                            double cGuess = nw[2 * i];
+                            double uGuess = nw[2 * i + 1];
+                            double A12 = dt * D * lapWeight;
+                            double A21 = -(QA * pow(nw[2 * i], 2.0) + QC) - K * lapWeight;
+                            double detA = 1.0 - (A12 * A21);
+                            /* fringe_laplacian (:155-170) of fields 1 and 0 */
+                            double f1 = 0.0, f0 = 0.0;
+                            int off = 3 - q.dim;
+                            for (int ra = 0; ra < q.dim; ra++) {
+                                int a = off + ra;
+                                double weight = 1.0 / pow(g->dx[ra], 2.0);
+                                long hi = i + NB_HI(&q, a, xc[a]), lo = i + NB_LO(&q, a, xc[a]);
+                                f1 += weight * (nw[2 * hi + 1] + nw[2 * lo + 1]);
+                                f0 += weight * (nw[2 * hi] + nw[2 * lo]);
+                            }
+                            double B1 = cOld + D * dt * f1;
+                            double B2 = (-A * (cOld - C0) - QB * pow(cOld, 2.0) - QD) - K * f0;
+                            double cNew = (B1 - B2 * A12) / detA;
+                            double uNew = (B2 - B1 * A21) / detA;
+                            nw[2 * i] = omega * cNew + (1.0 - omega) * cGuess;
+                            nw[2 * i + 1] = omega * uNew + (1.0 - omega) * uGuess;
+                        }
+            iter++;
+            if (iter < residual_step || iter % residual_step == 0) {
+                double normB = 0.0;
+                residual = 0.0;
+                for (int i0 = 0; i0 < q.n[0]; i0++)
+                    for (int i1 = 0; i1 < q.n[1]; i1++)
+                        for (int i2 = 0; i2 < q.n[2]; i2++) {
+                            int xc[3] = {i0, i1, i2};
+                            long i = i0 * q.st[0] + i1 * q.st[1] + i2;
+                            double lapC = lap_at(&q, nw, i, 2, 0, xc);
+                            double lapU = lap_at(&q, nw, i, 2, 1, xc);
+                            double cOld = old[2 * i], cNew = nw[2 * i], uNew = nw[2 * i + 1];
+                            double B1 = cOld;
+                            double B2 = -A * (cOld - C0) - QB * pow(cOld, 2.0) - QD;
+                            double AX1 = cNew - D * dt * lapU;
+                            double AX2 = uNew - (QA * pow(cNew, 3.0) + QC * cNew) + K * lapC;
+                            double R1 = B1 - AX1;
+                            double R2 = B2 - AX2;
+                            residual += R1 * R1 + R2 * R2;
+                            normB += B1 * B1 + B2 * B2;
+                        }
+                residual = sqrt(residual / normB) / (2.0 * gridSize);
+            }
+        }
+        if (iters) *iters = (int)iter;
+        if (iter == max_iter) rc = -2;
+        double* t = old;   /* swap(oldGrid,newGrid) */
+        old = nw;
+        nw = t;
+    }
+    if (old != cm) {
+        memcpy(cm, old, sizeof(double) * 2 * (size_t)q.cells);
+        nw = old;
+    }
+    free(nw);
+    geo_free(&q);
+    return rc;
+}
+
 /* Neumaier's improvement of Kahan summation. */
 typedef struct { double s, c; } nsum;
 static inline void nadd(nsum* a, double x)

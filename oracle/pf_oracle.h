@@ -103,6 +103,13 @@ int pfo_ch_shipped_noise(const pfo_grid* g, double* c, int steps, double r, doub
 int pfo_ac_scalar_noise(const pfo_grid* g, double* phi, int steps, double r, double u, double K, double M,
                         double dt, double nstd, uint64_t seed, long long step0, int threads);
 
+/* Convex-splitting Cahn-Hilliard exactly as shipped
+ * (examples/phase_transitions/cahn-hilliard/convex_splitting/cahn-hilliard.cpp:273-463,
+ * parametric free energy), serial; cm cell-major (c, mu).  Returns -2 when a
+ * step reaches 10000 iterations; *iters gets the last step's iterations. */
+int pfo_ch_convex(const pfo_grid* g, double* cm, int steps, double dt, double D, double K, double C0,
+                  double Ca, double Cb, double A, double omega, double tolerance, int* iters);
+
 /* Scalar Allen-Cahn exactly as shipped (allen-cahn.cpp:70):
  *   p' = p - dt*M*(-r*p + u*pow(p,3) - K*lap(p)). */
 int pfo_ac_scalar_shipped(const pfo_grid* g, double* phi, int steps,

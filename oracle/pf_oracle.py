@@ -47,6 +47,7 @@ def lib():
             ("pfo_ac_graingrowth", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
             ("pfo_ac_zener", [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
             ("pfo_ostwald", [gp, ctypes.c_int, dp, ctypes.c_int] + [ctypes.c_double] * 9 + [ctypes.c_int]),
+            ("pfo_ch_convex", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 9 + [ctypes.POINTER(ctypes.c_int)]),
             ("pfo_ch_shipped_noise", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 6
              + [ctypes.c_uint64, ctypes.c_longlong, ctypes.c_int]),
             ("pfo_ac_scalar_noise", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 6
@@ -135,6 +136,25 @@ def ostwald(eta, steps, dt=0.001, L=1.0, D=1.0, Calpha=0.05, Cbeta=0.95, A=2.0, 
     _check(lib().pfo_ostwald(ctypes.byref(g), out.shape[-1], _ptr(out), int(steps), dt, L, D, Calpha, Cbeta, A,
                              delta, epsilon, kappa, threads), "ostwald")
     return out
+
+
+def ch_convex(cm, steps, dt=None, D=None, K=2.0, C0=0.45, Ca=0.05, Cb=0.95, A=2.0, omega=1.2, tolerance=1e-14,
+              dx=None, bc=None, return_iters=False):
+    """Convex-splitting Cahn-Hilliard as shipped; ``cm`` has shape grid_shape + (2,) (c, mu).
+    Defaults are the example's: D = 2/(Cb-Ca), dt = 1/(D*K)."""
+    if D is None:
+        D = 2.0 / (Cb - Ca)
+    if dt is None:
+        dt = 1.0 / (D * K)
+    out = np.array(cm, dtype=np.float64, order="C", copy=True)
+    g = _grid(out.shape[:-1], dx, bc)
+    it = ctypes.c_int(0)
+    rc = lib().pfo_ch_convex(ctypes.byref(g), _ptr(out), int(steps), dt, D, K, C0, Ca, Cb, A, omega, tolerance,
+                             ctypes.byref(it))
+    if rc == -2:
+        raise RuntimeError("convex splitting stagnated (10000 iterations)")
+    _check(rc, "ch_convex")
+    return (out, it.value) if return_iters else out
 
 
 def gaussian(seed, k):

@@ -10,6 +10,7 @@
 //   examples/phase_transitions/allen-cahn/allen-cahn.cpp:47-75
 //   examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:103-143
 //   examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:56-123
+//   examples/phase_transitions/cahn-hilliard/convex_splitting/cahn-hilliard.cpp:273-463
 // The "shipped" models are those loops with the examples' own expressions;
 // the "baseline" models substitute f(c)=c^2(1-c)^2 for Cahn-Hilliard and
 // f = sum(-e^2/2+e^4/4) + gamma*sum_{i<j} e_i^2 e_j^2 for grain growth, with
@@ -22,6 +23,7 @@
 //   graingrowth      dt
 //   zener            dt
 //   ostwald          dt L D Calpha Cbeta A delta epsilon kappa
+//   ch_convex        dt D K C0 Ca Cb A omega tolerance   (prints "iterations <n>" of the last step)
 //   ac_scalar        r u K M dt
 // Prints "update_seconds <t>" (std::chrono around update() only).
 #include "MMSP.hpp"
@@ -183,6 +185,122 @@ template <int dim> void ostwald_update(grid<dim, vector<double> >& oldGrid, int 
 	}
 }
 
+// examples/phase_transitions/cahn-hilliard/convex_splitting/cahn-hilliard.cpp:273-463
+// (parametric free energy :38-96), constants from the command line; the two
+// Laplacian helpers of that file (:135-170) restated.
+template <int dim> double cs_field_laplacian(const grid<dim, vector<double> >& GRID, const vector<int>& x, int field)
+{
+	double laplacian = 0.0;
+	vector<int> s = x;
+	const double& y = GRID(x)[field];
+	for (int i = 0; i < dim; i++) {
+		s[i] += 1;
+		const double& yh = GRID(s)[field];
+		s[i] -= 2;
+		const double& yl = GRID(s)[field];
+		s[i] += 1;
+		double weight = 1.0 / pow(dx(GRID, i), 2.0);
+		laplacian += weight * (yh - 2.0 * y + yl);
+	}
+	return laplacian;
+}
+
+template <int dim> double cs_fringe_laplacian(const grid<dim, vector<double> >& GRID, const vector<int>& x, int field)
+{
+	double laplacian = 0.0;
+	vector<int> s = x;
+	for (int i = 0; i < dim; i++) {
+		s[i] += 1;
+		const double& yh = GRID(s)[field];
+		s[i] -= 2;
+		const double& yl = GRID(s)[field];
+		s[i] += 1;
+		double weight = 1.0 / pow(dx(GRID, i), 2.0);
+		laplacian += weight * (yh + yl);
+	}
+	return laplacian;
+}
+
+template <int dim> void convex_update(grid<dim, vector<double> >& oldGrid, int steps, const std::vector<double>& p)
+{
+	double dt = p[0], D = p[1], K = p[2], C0 = p[3], Ca = p[4], Cb = p[5], A = p[6], omega = p[7],
+	       tolerance = p[8];
+	double B = A / pow(Ca - C0, 2.0);
+	double QA = B + Ca + Cb;
+	double QB = 3.0 * (B * C0 + Ca * Ca + Cb * Cb);
+	double QC = 3.0 * (B * C0 * C0 + pow(Ca, 3.0) + pow(Cb, 3.0));
+	double QD = B * pow(C0, 3.0) + pow(Ca, 4.0) + pow(Cb, 4.0);
+	unsigned int residual_step = 5, max_iter = 10000;
+	ghostswap(oldGrid);
+	grid<dim, vector<double> > newGrid(oldGrid);
+	newGrid.copy(oldGrid);
+	double gridSize = static_cast<double>(nodes(oldGrid));
+	double lapWeight = 0.0;
+	for (int d = 0; d < dim; d++)
+		lapWeight += 2.0 / pow(dx(oldGrid, d), 2.0);
+	unsigned int iter = 0;
+	for (int step = 0; step < steps; step++) {
+		double residual = 1.0;
+		iter = 0;
+		ghostswap(oldGrid);
+		ghostswap(newGrid);
+		while (iter < max_iter && residual > tolerance) {
+			for (int color = 1; color > -1; color--) {
+				for (int n = 0; n < nodes(oldGrid); n++) {
+					vector<int> x = position(oldGrid, n);
+					int x_sum = 0;
+					for (int d = 0; d < dim; d++)
+						x_sum += x[d];
+					if (x_sum % 2 == color)
+						continue;
+					double cOld = oldGrid(n)[0];
+					double cGuess = newGrid(n)[0];
+					double uGuess = newGrid(n)[1];
+					double A12 = dt * D * lapWeight;
+					double A21 = -(QA * pow(newGrid(n)[0], 2.0) + QC) - K * lapWeight;
+					double detA = 1.0 - (A12 * A21);
+					double B1 = cOld + D * dt * cs_fringe_laplacian(newGrid, x, 1);
+					double B2 = (-A * (cOld - C0) - QB * pow(cOld, 2.0) - QD) - K * cs_fringe_laplacian(newGrid, x, 0);
+					double cNew = (B1 - B2 * A12) / detA;
+					double uNew = (B2 - B1 * A21) / detA;
+					newGrid(n)[0] = omega * cNew + (1.0 - omega) * cGuess;
+					newGrid(n)[1] = omega * uNew + (1.0 - omega) * uGuess;
+				}
+				ghostswap(newGrid);
+			}
+			iter++;
+			if (iter < residual_step || iter % residual_step == 0) {
+				double normB = 0.0;
+				residual = 0.0;
+				for (int n = 0; n < nodes(oldGrid); n++) {
+					vector<int> x = position(oldGrid, n);
+					double lapC = cs_field_laplacian(newGrid, x, 0);
+					double lapU = cs_field_laplacian(newGrid, x, 1);
+					double cOld = oldGrid(n)[0];
+					double cNew = newGrid(n)[0];
+					double uNew = newGrid(n)[1];
+					double B1 = cOld;
+					double B2 = -A * (cOld - C0) - QB * pow(cOld, 2.0) - QD;
+					double AX1 = cNew - D * dt * lapU;
+					double AX2 = uNew - (QA * pow(cNew, 3.0) + QC * cNew) + K * lapC;
+					double R1 = B1 - AX1;
+					double R2 = B2 - AX2;
+					double error = R1 * R1 + R2 * R2;
+					residual += error;
+					normB += B1 * B1 + B2 * B2;
+				}
+				residual = sqrt(residual / normB) / (2.0 * gridSize);
+			}
+		}
+		if (iter == max_iter) {
+			std::cerr << "solver stagnated on step " << step << std::endl;
+			std::exit(3);
+		}
+		swap(oldGrid, newGrid);
+	}
+	std::printf("iterations %u\n", iter);
+}
+
 } // namespace MMSP
 
 static double now_s()
@@ -215,6 +333,7 @@ template <int dim> int run_vector(const std::string& model, const char* in, cons
 	else if (model == "graingrowth") MMSP::gg_update(g, steps, true, p);
 	else if (model == "zener") MMSP::zener_update(g, steps, p);
 	else if (model == "ostwald") MMSP::ostwald_update(g, steps, p);
+	else if (model == "ch_convex") MMSP::convex_update(g, steps, p);
 	else return 2;
 	double t1 = now_s();
 	std::printf("update_seconds %.9f\n", t1 - t0);
@@ -234,7 +353,7 @@ int main(int argc, char* argv[])
 	for (int i = 5; i < argc; i++) p.push_back(std::atof(argv[i]));
 	size_t need = (model == "ch_baseline") ? 3 : (model == "ch_shipped" || model == "ac_scalar") ? 5
 	            : (model == "ac_baseline") ? 4 : (model == "graingrowth" || model == "zener") ? 1
-	            : (model == "ostwald") ? 9 : 0;
+	            : (model == "ostwald" || model == "ch_convex") ? 9 : 0;
 	if (need == 0 || p.size() != need) {
 		std::cerr << "bad model or parameter count" << std::endl;
 		return 1;

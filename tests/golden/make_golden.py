@@ -58,6 +58,8 @@ SMALL = [
     ("zener3d_shipped", "zener", (24, 24, 12), 3, ("zener", 30, 23), (0.01,), 40, {}),
     ("ostwald2d_shipped", "ostwald", (64, 32), 2, ("ostwald", 24), (0.001, 1.0, 1.0, 0.05, 0.95, 2.0, 1.0, 3.0, 2.0), 60, {}),
     ("ostwald3d_shipped", "ostwald", (16, 12, 8), 4, ("ostwald", 25), (0.001, 1.0, 1.0, 0.05, 0.95, 2.0, 1.0, 3.0, 2.0), 40, {}),
+    ("convex2d_shipped", "ch_convex", (40, 20), 2, ("convex", None), (0.225, 2.0 / 0.9, 2.0, 0.45, 0.05, 0.95, 2.0, 1.2, 1e-14), 4, {}),
+    ("convex3d_shipped", "ch_convex", (12, 10, 8), 2, ("convex", 31), (0.225, 2.0 / 0.9, 2.0, 0.45, 0.05, 0.95, 2.0, 1.2, 1e-14), 3, {}),
 ]
 
 
@@ -76,10 +78,12 @@ def start_state(shape, fields, spec):
         return inputs.zener_particles(shape, particles, seed)
     if kind == "ostwald":
         return inputs.ostwald_start(shape, fields, spec[1])
+    if kind == "convex":
+        return inputs.convex_start(shape, spec[1])
     raise ValueError(kind)
 
 
-def run_ref(model, data, vector, fields, steps, params, dx=None, bc=None):
+def run_ref(model, data, vector, fields, steps, params, dx=None, bc=None, want_stdout=False):
     dim = data.ndim - (1 if vector else 0)
     shape = data.shape[:dim]
     g = gridfile.GridData(dim=dim, g0=[0] * dim, g1=list(shape),
@@ -95,6 +99,8 @@ def run_ref(model, data, vector, fields, steps, params, dx=None, bc=None):
                              check=True, capture_output=True, text=True)
         secs = float(res.stdout.split()[-1])
         out = gridfile.read(fout)
+    if want_stdout:
+        return out.data, secs, res.stdout
     return out.data, secs
 
 
@@ -108,11 +114,15 @@ def make_small(only=None):
             continue
         x0 = start_state(shape, fields, spec)
         vector = fields > 0
-        out, secs = run_ref(model, x0, vector, fields, steps, params, extra.get("dx"), extra.get("bc"))
+        out, secs, text = run_ref(model, x0, vector, fields, steps, params, extra.get("dx"), extra.get("bc"),
+                                  want_stdout=True)
+        more = {}
+        if "iterations" in text:   # the implicit solve reports the last step's iterations
+            more["iterations"] = int(text.split("iterations")[1].split()[0])
         np.savez_compressed(os.path.join(HERE, name + ".npz"), start=x0, result=out, model=model,
                             params=np.asarray(params, dtype=np.float64), steps=steps,
                             dx=np.asarray(extra.get("dx", [1.0] * len(shape))),
-                            bc=np.asarray(extra.get("bc", [[2, 2]] * len(shape))))
+                            bc=np.asarray(extra.get("bc", [[2, 2]] * len(shape))), **more)
         print("%-24s %s steps=%d ref %.3fs" % (name, shape, steps, secs))
 
 

@@ -41,6 +41,9 @@ def desc_for(native, model, params, shape, fields, dtype, dx=None, bc=None):
     if model == "ostwald":
         return native.make_desc(shape, fields, dtype, "ostwald", dt=p[0], mobility=p[1], D=p[2], Calpha=p[3],
                                 Cbeta=p[4], A=p[5], delta=p[6], epsilon=p[7], kappa=p[8], **kw)
+    if model == "ch_convex":
+        return native.make_desc(shape, fields, dtype, "ch_convex", dt=p[0], mobility=p[1], kappa=p[2], C0=p[3],
+                                Ca=p[4], Cb=p[5], A=p[6], omega=p[7], tolerance=p[8], **kw)
     raise ValueError(model)
 
 
@@ -60,7 +63,7 @@ def test_fp64_matches_reference_fixture(gpu, path):
     z = np.load(path)
     model = str(z["model"])
     x = z["start"]
-    vector = model in ("ac_baseline", "graingrowth", "zener", "ostwald")
+    vector = model in ("ac_baseline", "graingrowth", "zener", "ostwald", "ch_convex")
     shape = x.shape[:-1] if vector else x.shape
     fields = x.shape[-1] if vector else 1
     bc = z["bc"].tolist()
@@ -545,3 +548,59 @@ def test_stochastic_forms_are_refused_where_no_step_index_travels(gpu):
     with pytest.raises(gpu.GpuError) as e:
         gpu.Stepper(bad)
     assert e.value.code == gpu.EINVAL
+
+
+# Convex-splitting Cahn-Hilliard: an implicit solve per step (red-black SOR to
+# a 1e-14 relative residual).  FP64 is compared with the oracle, which matches
+# the reference program bit for bit including its iteration counts.
+CONVEX = [((40, 20), None, 4), ((64, 48), 5, 6), ((12, 10, 8), 31, 3), ((128,), 7, 10)]
+
+
+@pytest.mark.parametrize("shape,seed,steps", CONVEX, ids=["x".join(map(str, s)) for s, _, _ in CONVEX])
+def test_convex_splitting_against_oracle(gpu, oracle, shape, seed, steps):
+    from mmsp_gb300 import inputs
+
+    x = inputs.convex_start(shape, seed)
+    want, iters = oracle.ch_convex(x, steps, return_iters=True)
+    d = gpu.make_desc(shape, 2, np.float64, "ch_convex")
+    with gpu.Stepper(d) as s:
+        s.upload(x)
+        states = [x]
+        for k in range(steps):
+            s.step(1)
+            states.append(s.download())
+        st = s.reduce()
+        got = states[-1]
+    assert abs(st.solver_iterations - iters) <= 5           # residual sums differ only in rounding
+    assert np.abs(got - want).max() <= 1e-10 * max(1.0, np.abs(want).max())
+    # convex splitting (Eyre) is energy-stable for the discrete energy of its
+    # Laplacian, the one with forward-difference gradients
+    fd = [convex_energy(y[..., 0], forward=True) for y in states]
+    assert all(b <= a + 1e-10 * abs(a) for a, b in zip(fd, fd[1:])), fd
+    # the reduction reports the example's reportEnergy (central differences) and the mass of c
+    assert abs(st.energy - convex_energy(got[..., 0])) <= 1e-11 * abs(st.energy)
+    assert abs(st.mass - x[..., 0].sum()) <= 1e-9 * abs(x[..., 0].sum())   # c is conserved
+
+
+def convex_energy(c, forward=False, C0=0.45, Ca=0.05, Cb=0.95, A=2.0, K=2.0):
+    """sum of energy_density(c) + K/2 |grad c|^2 (cahn-hilliard.cpp:57-80, 172-200), dx = 1:
+    central differences as reportEnergy's grad, or forward differences."""
+    B = A / (Ca - C0) ** 2
+    f = -0.5 * A * (c - C0) ** 2 + 0.25 * B * (c - C0) ** 4 + 0.25 * Ca * (c - Ca) ** 4 + 0.25 * Cb * (c - Cb) ** 4
+    g2 = np.zeros_like(c)
+    for a in range(c.ndim):
+        g = np.roll(c, -1, a) - c if forward else 0.5 * (np.roll(c, -1, a) - np.roll(c, 1, a))
+        g2 += g * g
+    return float((f + 0.5 * K * g2).sum())
+
+
+def test_convex_splitting_refusals(gpu):
+    with pytest.raises(gpu.GpuError) as e:
+        gpu.Stepper(gpu.make_desc((40, 20), 2, np.float32, "ch_convex"))
+    assert e.value.code == gpu.EUNSUPPORTED                   # FP64 only
+    with pytest.raises(gpu.GpuError) as e:
+        gpu.Stepper(gpu.make_desc((41, 20), 2, np.float64, "ch_convex"))
+    assert e.value.code == gpu.EUNSUPPORTED                   # odd extent
+    with pytest.raises(gpu.GpuError) as e:
+        gpu.Stepper(gpu.make_desc((40, 20), 1, np.float64, "ch_convex"))
+    assert e.value.code == gpu.EINVAL                         # c and mu

@@ -40,6 +40,12 @@ def run_oracle(o, z, x=None, steps=None):
         return o.ac_zener(x, st, *p, dx=dx, bc=bc)
     if m == "ostwald":
         return o.ostwald(x, st, *p, dx=dx, bc=bc)
+    if m == "ch_convex":
+        keys = ("dt", "D", "K", "C0", "Ca", "Cb", "A", "omega", "tolerance")
+        out, iters = o.ch_convex(x, st, dx=dx, bc=bc, return_iters=True, **dict(zip(keys, p)))
+        if "iterations" in z.files and steps is None:
+            assert iters == int(z["iterations"]), (iters, int(z["iterations"]))
+        return out
     raise ValueError(m)
 
 
