@@ -277,7 +277,34 @@ def other_models(native, inputs, timed):
                      "f32_max_err_vs_f64": float(np.abs(o32.astype(np.float64) - o64).max()),
                      "cpu_oracle_value_updates_per_s": cpu_rate, "cpu_sample": "2 FP64 steps, 1 thread",
                      "f64_speedup_vs_cpu": vals / (ms64 / 1e3) / cpu_rate}
+    out.update(convex_splitting(native, inputs, timed))
     return out
+
+
+def convex_splitting(native, inputs, timed):
+    """Convex-splitting Cahn-Hilliard on the example's 400 x 200 grid (stripes
+    start, parametric energy, dt = 1/(D K)): 20 semi-implicit steps in FP64,
+    each a red-black SOR solve to a 1e-14 residual, beside the oracle (the
+    example's loops restated in C, one thread) on 2 steps."""
+    from oracle import pf_oracle
+
+    shape = (400, 200)
+    x = inputs.convex_start(shape)
+    d = native.make_desc(shape, 2, np.float64, "ch_convex")
+    steps = 20
+    ms, _ = timed(d, x, steps)
+    with native.Stepper(d) as s:
+        s.upload(x)
+        s.step(steps)
+        iters = s.reduce().solver_iterations
+    t0 = time.perf_counter()
+    _, cpu_iters = pf_oracle.ch_convex(x, 2, return_iters=True)
+    cpu_s = (time.perf_counter() - t0) / 2
+    return {"convex2d_400x200_f64_20": {"ms_per_step": ms / steps, "iterations_last_step": iters,
+                                        "cpu_oracle_ms_per_step": cpu_s * 1e3,
+                                        "cpu_oracle_iterations_step2": cpu_iters,
+                                        "speedup_vs_cpu": cpu_s * 1e3 / (ms / steps),
+                                        "cpu_sample": "2 steps, 1 thread, FP64"}}
 
 
 def output_path(native, inputs):
