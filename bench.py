@@ -707,6 +707,8 @@ CASES = {
     "ch2d_f64": ((256, 256), 1, np.float64, "ch", dict(dt=0.005, kappa=1.0, mobility=1.0)),
     "ac3d_f32": ((128, 128, 128), 8, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
+    "ostwald3d_f32": ((256, 128, 64), 2, np.float32, "ostwald", {}),
+    "convex2d_f64": ((400, 200), 2, np.float64, "ch_convex", {}),
 }
 
 
@@ -730,6 +732,10 @@ def run_case(name: str, steps: int):
     shape, fields, dtype, model, params = CASES[name]
     if fields == 1:
         x = inputs.noisy_composition(shape, MEAN, AMP, SEED)
+    elif model == "ostwald":
+        x = inputs.ostwald_start(shape, fields, 9)
+    elif model == "ch_convex":
+        x = inputs.convex_start(shape)
     else:
         x = inputs.voronoi_grains(shape, 200, fields, 3)
     d = native.make_desc(shape, fields, dtype, model, **params)
