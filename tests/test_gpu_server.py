@@ -50,6 +50,32 @@ def test_results_same_alone_and_in_the_mix(gpu):
         assert np.array_equal(got, want)
 
 
+def test_further_models_same_alone_and_in_the_mix(gpu):
+    """Zener pinning, Ostwald ripening (two kernels and a work grid per step),
+    a noisy model-B grid (step-indexed noise, no graph replay) and a
+    convex-splitting grid (an implicit solve per step) run through the server
+    in chunks and must equal the same solves run alone in one call."""
+    from mmsp_gb300 import inputs
+
+    reqs = [
+        (gpu.make_desc((24, 20, 16), 3, np.float32, "zener", dt=0.01), inputs.zener_particles((24, 20, 16), 8, 11), 230),
+        (gpu.make_desc((32, 24, 16), 2, np.float64, "ostwald"), inputs.ostwald_start((32, 24, 16), 2, 12), 150),
+        (gpu.make_desc((48, 40), 1, np.float64, "ch_poly", dt=0.01, noise=1.4, seed=77),
+         inputs.noisy_composition((48, 40), 0.0, 0.2, 13), 260),
+        (gpu.make_desc((40, 20), 2, np.float64, "ch_convex"), inputs.convex_start((40, 20)), 3),
+        (gpu.make_desc((96, 80), 1, np.float32, "ch", dt=0.005), inputs.noisy_composition((96, 80), 0.5, 0.02, 14), 300),
+    ]
+    with gpu.Server(chunk_steps=100) as srv:
+        ids = [srv.submit(d, x, n) for d, x, n in reqs]
+        for rid in ids:
+            st = srv.wait(rid, 120.0)
+            assert st.state == gpu.REQ_DONE, (st.state, st.message)
+        outs = [srv.fetch(rid) for rid in ids]
+    for (d, x, n), got in zip(reqs, outs):
+        want, _ = alone(gpu, d, x, n)
+        assert np.array_equal(got, want)
+
+
 def test_budget_admission_and_memory_release(gpu):
     from mmsp_gb300 import inputs
     import ctypes
