@@ -35,6 +35,7 @@
 #define MMSP_GPU_HPP
 
 #include <iostream>
+#include <string>
 #include <vector>
 
 #include <cmath>
@@ -207,6 +208,93 @@ template <class G>
 void update(G& g, int steps, const Model& m)
 {
     int rc = try_update(g, steps, m);
+    if (rc) MMSP::Abort(rc);
+}
+
+// The run loop of MMSP.main.hpp with the state kept on the device.  The
+// reference's main() (include/MMSP.main.hpp:277-300, repeated for 2D and 3D)
+// calls update(grid, increment) and then output(grid, name) for
+// i = start, start + increment, ... < steps, the name being base, then
+// i + increment zero-padded to the digits of `steps`, then suffix.  Through
+// gpu::update every increment would copy the grid in and out; here the grid
+// goes to the device once, each snapshot is written by mmsp_gpu_output while
+// the next increment runs, and the host grid holds the final state at the end.
+// Files are the reference's format (grid::output, one block, zlib level 9).
+inline int run_buffer(const mmsp_gpu_desc& d, void* buf, size_t bytes, mmsp_gpu_output_opts& o, int start, int steps,
+                      int increment, const std::string& base, const std::string& suffix, mmsp_gpu_stats* stats)
+{
+    if (increment < 1) return MMSP_GPU_EINVAL;
+    mmsp_gpu_handle* h = 0;
+    int rc = mmsp_gpu_create(&h, &d);
+    if (rc) return report(rc, "create");
+    rc = mmsp_gpu_upload(h, buf, bytes, MMSP_GPU_CELL_MAJOR);
+    const size_t width = std::to_string(steps).size();
+    for (int i = start; rc == MMSP_GPU_OK && i < steps; i += increment) {
+        rc = mmsp_gpu_step(h, increment);
+        std::string num = std::to_string(i + increment);
+        if (num.size() < width) num = std::string(width - num.size(), '0') + num;
+        if (rc == MMSP_GPU_OK) rc = mmsp_gpu_output(h, (base + num + suffix).c_str(), &o);
+    }
+    int wrc = mmsp_gpu_output_wait(h);
+    if (rc == MMSP_GPU_OK) rc = wrc;
+    if (rc == MMSP_GPU_OK) rc = mmsp_gpu_download(h, buf, bytes, MMSP_GPU_CELL_MAJOR);
+    if (rc == MMSP_GPU_OK && stats) rc = mmsp_gpu_reduce(h, stats);
+    if (rc) std::cerr << "MMSP::gpu::run: " << mmsp_gpu_last_error(h) << std::endl;
+    mmsp_gpu_destroy(h);
+    return report(rc, "run");
+}
+
+template <template <int, typename> class Grid, int dim, typename T>
+int try_run(Grid<dim, T>& g, int start, int steps, int increment, const std::string& base, const std::string& suffix,
+            const Model& m, mmsp_gpu_stats* stats = 0)
+{
+    mmsp_gpu_desc d;
+    int rc = describe(g, dim, 1, dtype_of<T>::value, m, &d);
+    if (rc) return report(rc, "descriptor");
+    const int n = nodes(g);
+    std::vector<T> buf((size_t)n);
+    for (int i = 0; i < n; i++) buf[i] = g(i);
+    mmsp_gpu_output_opts o;
+    mmsp_gpu_output_opts_init(&o);
+    o.vector = 0;
+    o.fields_line = fields(g);
+    for (int a = 0; a < dim; a++) o.g0[a] = g0(g, a);
+    rc = run_buffer(d, &buf[0], buf.size() * sizeof(T), o, start, steps, increment, base, suffix, stats);
+    if (rc) return rc;
+    for (int i = 0; i < n; i++) g(i) = buf[i];
+    return MMSP_GPU_OK;
+}
+
+template <template <int, typename> class Grid, template <typename> class Vec, int dim, typename T>
+int try_run(Grid<dim, Vec<T> >& g, int start, int steps, int increment, const std::string& base,
+            const std::string& suffix, const Model& m, mmsp_gpu_stats* stats = 0)
+{
+    const int N = fields(g);
+    mmsp_gpu_desc d;
+    int rc = describe(g, dim, N, dtype_of<T>::value, m, &d);
+    if (rc) return report(rc, "descriptor");
+    const int n = nodes(g);
+    std::vector<T> buf((size_t)n * N);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < N; j++) buf[(size_t)i * N + j] = g(i)[j];
+    mmsp_gpu_output_opts o;
+    mmsp_gpu_output_opts_init(&o);
+    o.vector = 1;
+    o.fields_line = N;
+    for (int a = 0; a < dim; a++) o.g0[a] = g0(g, a);
+    rc = run_buffer(d, &buf[0], buf.size() * sizeof(T), o, start, steps, increment, base, suffix, stats);
+    if (rc) return rc;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < N; j++) g(i)[j] = buf[(size_t)i * N + j];
+    return MMSP_GPU_OK;
+}
+
+// The main()-facing call: aborts like the reference on failure.
+template <class G>
+void run(G& g, int start, int steps, int increment, const std::string& base, const std::string& suffix,
+         const Model& m)
+{
+    int rc = try_run(g, start, steps, increment, base, suffix, m);
     if (rc) MMSP::Abort(rc);
 }
 

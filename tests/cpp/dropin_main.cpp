@@ -72,8 +72,44 @@ template <typename T> static int vector_case(const char* in, const char* out, in
     return write_raw(out, v) ? 0 : 3;
 }
 
+// MMSP.main.hpp's loop through MMSP::gpu::run: snapshots BASE.<step>.dat
+// every `inc` steps, and the final values as raw data in OUT.
+template <typename T> static int run_scalar(const char* in, const char* base, const char* out, int steps, int inc,
+                                            int n0, int n1, int n2)
+{
+    MMSP::grid<3, T> g(0, 0, n0, 0, n1, 0, n2);
+    std::vector<T> v((size_t)n0 * n1 * n2);
+    if (!read_raw(in, v)) return 2;
+    for (int i = 0; i < nodes(g); i++) g(i) = v[i];
+    MMSP::gpu::run(g, 0, steps, inc, std::string(base) + ".", ".dat", MMSP::gpu::cahn_hilliard(1.0, 1.0, 0.002));
+    for (int i = 0; i < nodes(g); i++) v[i] = g(i);
+    return write_raw(out, v) ? 0 : 3;
+}
+
+template <typename T> static int run_vector(const char* in, const char* base, const char* out, int steps, int inc,
+                                            int n0, int n1, int n2, int N)
+{
+    MMSP::grid<3, MMSP::vector<T> > g(N, 0, n0, 0, n1, 0, n2);
+    std::vector<T> v((size_t)n0 * n1 * n2 * N);
+    if (!read_raw(in, v)) return 2;
+    for (int i = 0; i < nodes(g); i++)
+        for (int j = 0; j < N; j++) g(i)[j] = v[(size_t)i * N + j];
+    MMSP::gpu::run(g, 0, steps, inc, std::string(base) + ".", ".dat", MMSP::gpu::grain_growth_shipped(0.01));
+    for (int i = 0; i < nodes(g); i++)
+        for (int j = 0; j < N; j++) v[(size_t)i * N + j] = g(i)[j];
+    return write_raw(out, v) ? 0 : 3;
+}
+
 int main(int argc, char* argv[])
 {
+    // usage: dropin_main run_ch|run_gg IN BASE OUT STEPS INC n0 n1 n2 [fields]
+    if (argc >= 10 && (std::string(argv[1]) == "run_ch" || std::string(argv[1]) == "run_gg")) {
+        int steps = std::atoi(argv[5]), inc = std::atoi(argv[6]);
+        int n0 = std::atoi(argv[7]), n1 = std::atoi(argv[8]), n2 = std::atoi(argv[9]);
+        if (std::string(argv[1]) == "run_ch") return run_scalar<double>(argv[2], argv[3], argv[4], steps, inc, n0, n1, n2);
+        int N = argc > 10 ? std::atoi(argv[10]) : 2;
+        return run_vector<double>(argv[2], argv[3], argv[4], steps, inc, n0, n1, n2, N);
+    }
     if (argc < 8) {
         std::fprintf(stderr, "usage: dropin_main ch|ch_f32|gg|gg_f32 IN OUT STEPS n0 n1 n2 [fields]\n");
         return 1;

@@ -90,3 +90,31 @@ def test_dropin_scalar_and_vector_grids_on_device(gpu, oracle, tmp_path):
     assert r.returncode == 0, r.stderr
     want = oracle.ac_graingrowth(e0, 30, 0.01)
     assert np.abs(out - want).max() <= 1e-12 * np.abs(want).max()
+
+
+@pytest.mark.gpu
+def test_run_loop_writes_the_snapshots_of_main(gpu, oracle, tmp_path):
+    """MMSP::gpu::run replaces MMSP.main.hpp's update/output loop with the state
+    on the device: one file per increment, named base.<step zero-padded to the
+    digits of the step count>.dat, holding the state after that many steps."""
+    from mmsp_gb300 import gridfile, inputs
+
+    exe = build_mini(str(tmp_path))
+    c0 = inputs.noisy_composition((12, 14, 16), 0.4, 0.02, 42)
+    fi, fo, base = str(tmp_path / "in.raw"), str(tmp_path / "out.raw"), str(tmp_path / "ch")
+    c0.tofile(fi)
+    r = subprocess.run([exe, "run_ch", fi, base, fo, "120", "40", "12", "14", "16"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for k in (40, 80, 120):
+        g = gridfile.read(base + ".%03d.dat" % k)
+        assert g.type_name == "grid:double" and g.shape == (12, 14, 16)
+        assert np.array_equal(g.data, oracle.ch_baseline(c0, k, 1.0, 1.0, 0.002))
+    assert np.array_equal(np.fromfile(fo).reshape(c0.shape), oracle.ch_baseline(c0, 120, 1.0, 1.0, 0.002))
+    e0 = inputs.graingrowth_circles((20, 20, 4), 2)
+    e0.tofile(fi)
+    r = subprocess.run([exe, "run_gg", fi, str(tmp_path / "gg"), fo, "30", "10", "20", "20", "4", "2"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    g = gridfile.read(str(tmp_path / "gg") + ".30.dat")
+    want = oracle.ac_graingrowth(e0, 30, 0.01)
+    assert g.vector and g.fields == 2 and np.abs(g.data - want).max() <= 1e-12 * np.abs(want).max()
