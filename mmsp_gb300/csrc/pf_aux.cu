@@ -275,16 +275,29 @@ __global__ void __launch_bounds__(256) reduce_kernel(const T* __restrict__ st, G
     }
 }
 
+// One warp: lane l combines partials l, l+32, ... (its loads run in
+// parallel with the other lanes'), then lane 0 combines the 32 lane sums in
+// lane order.  The assignment is fixed, so the result is deterministic.
 __global__ void reduce_final(double* partials, int nblocks, double dV)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
     NS m{0.0, 0.0}, e{0.0, 0.0};
-    for (int b = 0; b < nblocks; b++) {
+    for (int b = lane; b < nblocks; b += 32) {
         m = ncombine(m, NS{partials[b * 4 + 0], partials[b * 4 + 1]});
         e = ncombine(e, NS{partials[b * 4 + 2], partials[b * 4 + 3]});
     }
-    partials[nblocks * 4 + 0] = dV * (m.s + m.c);
-    partials[nblocks * 4 + 1] = dV * (e.s + e.c);
+    NS tm{0.0, 0.0}, te{0.0, 0.0};
+    for (int w = 0; w < 32; w++) {
+        const NS om{__shfl_sync(0xffffffffu, m.s, w), __shfl_sync(0xffffffffu, m.c, w)};
+        const NS oe{__shfl_sync(0xffffffffu, e.s, w), __shfl_sync(0xffffffffu, e.c, w)};
+        tm = ncombine(tm, om);
+        te = ncombine(te, oe);
+    }
+    if (lane == 0) {
+        partials[nblocks * 4 + 0] = dV * (tm.s + tm.c);
+        partials[nblocks * 4 + 1] = dV * (te.s + te.c);
+    }
 }
 
 cudaError_t launch_reduce(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,

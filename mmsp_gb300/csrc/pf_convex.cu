@@ -181,18 +181,30 @@ cs_residual(const double* __restrict__ old, const double* __restrict__ nw, Geom 
     }
 }
 
+// One warp: lane l combines partials l, l+32, ..., then lane 0 the lane
+// sums in lane order (a fixed assignment: deterministic).
 __global__ void cs_residual_final(double* partials, int nblocks)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
     CsNS r{0.0, 0.0}, b{0.0, 0.0};
-    for (int k = 0; k < nblocks; k++) {
+    for (int k = lane; k < nblocks; k += 32) {
         cs_add(r, partials[k * 4 + 0]);
         r.c += partials[k * 4 + 1];
         cs_add(b, partials[k * 4 + 2]);
         b.c += partials[k * 4 + 3];
     }
-    partials[nblocks * 4 + 0] = r.s + r.c;
-    partials[nblocks * 4 + 1] = b.s + b.c;
+    CsNS tr{0.0, 0.0}, tb{0.0, 0.0};
+    for (int w = 0; w < 32; w++) {
+        cs_add(tr, __shfl_sync(0xffffffffu, r.s, w));
+        tr.c += __shfl_sync(0xffffffffu, r.c, w);
+        cs_add(tb, __shfl_sync(0xffffffffu, b.s, w));
+        tb.c += __shfl_sync(0xffffffffu, b.c, w);
+    }
+    if (lane == 0) {
+        partials[nblocks * 4 + 0] = tr.s + tr.c;
+        partials[nblocks * 4 + 1] = tb.s + tb.c;
+    }
 }
 
 static CsArgs cs_args(const Coeffs& c, const Geom& g)
