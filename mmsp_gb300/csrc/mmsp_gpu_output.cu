@@ -103,7 +103,7 @@ struct OutputState {
             cudaError_t e = cudaEventSynchronize(copied[j.slot]);
             if (e != cudaSuccess)
                 rc = MMSP_GPU_ECUDA, w = std::string("output copy: ") + cudaGetErrorString(e);
-            else
+            else   // write_grid_file throws nothing: failures come back as codes
                 rc = write_grid_file(j.filename.c_str(), j.fi, host[j.slot], j.bytes, j.level, j.threads, &w);
             {
                 std::lock_guard<std::mutex> lk(m);
@@ -350,8 +350,7 @@ extern "C" int mmsp_gpu_output(mmsp_gpu_handle* h, const char* filename, const m
         (e = cudaEventRecord(s->drained, s->copy)) != cudaSuccess)
         return out_cuda(h, e, "output copy");
     // stage 3 (writer thread)
-    {
-        std::lock_guard<std::mutex> lk(s->m);
+    try {
         pf::OutputJob j;
         j.filename = filename;
         j.fi = fi;
@@ -359,9 +358,13 @@ extern "C" int mmsp_gpu_output(mmsp_gpu_handle* h, const char* filename, const m
         j.level = o->level;
         j.threads = o->threads;
         j.slot = slot;
+        std::lock_guard<std::mutex> lk(s->m);
+        s->queue.push_back(j);
         s->busy[slot] = true;
         s->pending++;
-        s->queue.push_back(j);
+    } catch (...) {
+        cudaStreamSynchronize(s->copy);   // the copy into the slot must end before the slot is reused
+        return out_fail(h, MMSP_GPU_ENOMEM, "output: out of host memory");
     }
     s->cv.notify_all();
     return MMSP_GPU_OK;

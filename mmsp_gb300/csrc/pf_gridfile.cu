@@ -60,6 +60,8 @@ struct Piece {
 };
 
 // Raw deflate of base[off, off+len), primed with the preceding 32 KB.
+// Leaves p->ok false on any failure, allocation included (it runs on
+// worker threads, which must not throw).
 void deflate_piece(const unsigned char* base, size_t off, size_t len, bool last, int level, Piece* p)
 {
     z_stream s;
@@ -70,7 +72,12 @@ void deflate_piece(const unsigned char* base, size_t off, size_t len, bool last,
         deflateEnd(&s);
         return;
     }
-    p->out.resize(deflateBound(&s, (uLong)len) + 64);   // room for the sync-flush marker too
+    try {
+        p->out.resize(deflateBound(&s, (uLong)len) + 64);   // room for the sync-flush marker too
+    } catch (...) {
+        deflateEnd(&s);
+        return;
+    }
     s.next_in = const_cast<Bytef*>(base + off);
     s.avail_in = (uInt)len;
     s.next_out = p->out.data();
@@ -117,8 +124,24 @@ struct File {
 
 }  // namespace
 
+static int write_grid_file_impl(const char* filename, const GridFileInfo& fi, const void* payload,
+                                size_t size_in_mem, int level, int threads, std::string* why);
+
+// No exception leaves: allocation failures (buffers, threads) become
+// MMSP_GPU_ENOMEM.
 int write_grid_file(const char* filename, const GridFileInfo& fi, const void* payload, size_t size_in_mem, int level,
                     int threads, std::string* why)
+{
+    try {
+        return write_grid_file_impl(filename, fi, payload, size_in_mem, level, threads, why);
+    } catch (...) {
+        if (why) *why = "out of host memory or threads while writing the grid file";
+        return MMSP_GPU_ENOMEM;
+    }
+}
+
+static int write_grid_file_impl(const char* filename, const GridFileInfo& fi, const void* payload,
+                                size_t size_in_mem, int level, int threads, std::string* why)
 {
     if (!filename || !payload || level < 0 || level > 9) {
         if (why) *why = "write_grid_file: bad argument";
@@ -154,7 +177,14 @@ int write_grid_file(const char* filename, const GridFileInfo& fi, const void* pa
             }
         };
         std::vector<std::thread> pool;
-        for (int t = 1; t < nt; t++) pool.emplace_back(work);
+        pool.reserve(nt);
+        for (int t = 1; t < nt; t++) {
+            try {
+                pool.emplace_back(work);
+            } catch (...) {
+                break;   // fewer threads: the pieces left are taken by those running
+            }
+        }
         work();
         for (auto& t : pool) t.join();
         uLong adler = 1;
