@@ -81,13 +81,18 @@ static __device__ __forceinline__ T lap_at(const T* __restrict__ f, long long i,
                                  f[i + n.zl], p.wx, p.wy, p.wz);
 }
 
-// sum_{j>=1} pow(e_j,2), ostwald.cpp:91-93 (0.0 + x == x for x >= 0)
-template <typename T>
+// sum_{j>=1} pow(e_j,2), ostwald.cpp:91-93 (0.0 + x == x for x >= 0).
+// NF: the field count when it is a compile-time constant (loops unroll), 0
+// when it is taken from N.
+template <typename T, int NF>
 static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long i, long long cells, int N)
 {
     using A = Ar<T>;
+    const int n = NF ? NF : N;
     T sum = T(0);
-    for (int j = 1; j < N; j++) {
+#pragma unroll(NF ? NF : 1)
+    for (int j = 1; j < (NF ? NF : 64); j++) {
+        if (!NF && j >= n) break;
         const T e = s[(long long)j * cells + i];
         sum = j == 1 ? A::mul(e, e) : A::add(sum, A::mul(e, e));
     }
@@ -96,7 +101,7 @@ static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long
 
 // Pass 1, ostwald.cpp:95-99:
 //   w = -A*(C-Cm) + B*pow(C-Cm,3) + Da*pow(C-Ca,3) + Db*pow(C-Cb,3) - g*(C-Ca)*sum - kappa*lap C
-template <typename T, int DIM, bool UNIT>
+template <typename T, int DIM, bool UNIT, int NF>
 __global__ void __launch_bounds__(256)
 ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
 {
@@ -108,7 +113,7 @@ ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
         for (int z = threadIdx.x; z < g.Z; z += blockDim.x) {
             cell_z(n, g, z);
             const long long i = row * g.Z + z;
-            const T sum = order_sum(s, i, g.cells, N);
+            const T sum = order_sum<T, NF>(s, i, g.cells, N);
             const T C = s[i];
             const T lap = lap_at<T, DIM, UNIT>(s, i, n, p);
             const T dm = A::sub(C, p.Cm), da = A::sub(C, p.Ca), db = A::sub(C, p.Cb);
@@ -125,7 +130,7 @@ ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
 // Pass 2, ostwald.cpp:103-120:
 //   C'   = C + dt*D*lap w
 //   e_j' = e_j - dt*L*(-g*pow(C-Ca,2) + delta*pow(e_j,3) + eps*e_j*(sum - pow(e_j,2)) - kappa*lap e_j)
-template <typename T, int DIM, bool UNIT>
+template <typename T, int DIM, bool UNIT, int NF>
 __global__ void __launch_bounds__(256)
 ostwald_update(const T* __restrict__ s, const T* __restrict__ w, T* __restrict__ out, Geom g, OstP<T> p, int N)
 {
@@ -139,10 +144,12 @@ ostwald_update(const T* __restrict__ s, const T* __restrict__ w, T* __restrict__
             const long long i = row * g.Z + z;
             const T C = s[i];
             out[i] = A::add(C, A::mul(p.dtD, lap_at<T, DIM, UNIT>(w, i, n, p)));
-            const T sum = order_sum(s, i, g.cells, N);
+            const T sum = order_sum<T, NF>(s, i, g.cells, N);
             const T da = A::sub(C, p.Ca);
             const T t1 = A::mul(p.neg_g, A::mul(da, da));
-            for (int j = 1; j < N; j++) {
+#pragma unroll(NF ? NF : 1)
+            for (int j = 1; j < (NF ? NF : 64); j++) {
+                if (!NF && j >= N) break;
                 const T* f = s + (long long)j * g.cells;
                 const T e = f[i];
                 T v = A::add(t1, A::mul(p.delta, cube(e)));
@@ -154,27 +161,36 @@ ostwald_update(const T* __restrict__ s, const T* __restrict__ w, T* __restrict__
     }
 }
 
-template <typename T, int DIM, bool UNIT>
+template <typename T, int DIM, bool UNIT, int NF>
 static void ost_fns(const void** mu, const void** up)
 {
-    *mu = (const void*)&ostwald_mu<T, DIM, UNIT>;
-    *up = (const void*)&ostwald_update<T, DIM, UNIT>;
+    *mu = (const void*)&ostwald_mu<T, DIM, UNIT, NF>;
+    *up = (const void*)&ostwald_update<T, DIM, UNIT, NF>;
+}
+
+template <typename T, int DIM, bool UNIT>
+static void ost_pick_n(int N, const void** mu, const void** up)
+{
+    if (N == 2) ost_fns<T, DIM, UNIT, 2>(mu, up);
+    else if (N == 3) ost_fns<T, DIM, UNIT, 3>(mu, up);
+    else if (N == 4) ost_fns<T, DIM, UNIT, 4>(mu, up);
+    else ost_fns<T, DIM, UNIT, 0>(mu, up);
 }
 
 template <typename T>
-static void ost_pick(int dim, bool unit, const void** mu, const void** up)
+static void ost_pick(int dim, bool unit, int N, const void** mu, const void** up)
 {
-    if (dim == 3) unit ? ost_fns<T, 3, true>(mu, up) : ost_fns<T, 3, false>(mu, up);
-    else if (dim == 2) unit ? ost_fns<T, 2, true>(mu, up) : ost_fns<T, 2, false>(mu, up);
-    else unit ? ost_fns<T, 1, true>(mu, up) : ost_fns<T, 1, false>(mu, up);
+    if (dim == 3) unit ? ost_pick_n<T, 3, true>(N, mu, up) : ost_pick_n<T, 3, false>(N, mu, up);
+    else if (dim == 2) unit ? ost_pick_n<T, 2, true>(N, mu, up) : ost_pick_n<T, 2, false>(N, mu, up);
+    else unit ? ost_pick_n<T, 1, true>(N, mu, up) : ost_pick_n<T, 1, false>(N, mu, up);
 }
 
 cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     const Coeffs c = make_coeffs(d);
     const void* up = nullptr;
-    if (d.dtype == MMSP_GPU_F64) ost_pick<double>(g.dim, c.unit_w, &p->fn, &up);
-    else ost_pick<float>(g.dim, c.unit_w, &p->fn, &up);
+    if (d.dtype == MMSP_GPU_F64) ost_pick<double>(g.dim, c.unit_w, d.fields, &p->fn, &up);
+    else ost_pick<float>(g.dim, c.unit_w, d.fields, &p->fn, &up);
     // one row (axis Z) per block iteration, threads along the row; blocks
     // stride over the rows beyond 16 resident blocks per SM
     const int threads = g.Z >= 256 ? 256 : (g.Z + 31) / 32 * 32;
@@ -201,14 +217,14 @@ cudaError_t launch_ostwald(const StepPlan& p, const mmsp_gpu_desc& d, const Geom
     Geom gg = g;
     cudaError_t e;
     if (d.dtype == MMSP_GPU_F64) {
-        ost_pick<double>(g.dim, c.unit_w, &mu, &up);
+        ost_pick<double>(g.dim, c.unit_w, d.fields, &mu, &up);
         OstP<double> q = ost_narrow<double>(c, g.dim);
         void* a1[] = {(void*)&in, (void*)&work, (void*)&gg, (void*)&q, (void*)&n};
         if ((e = cudaLaunchKernel(mu, p.grid, p.block, a1, 0, s)) != cudaSuccess) return e;
         void* a2[] = {(void*)&in, (void*)&work, (void*)&out, (void*)&gg, (void*)&q, (void*)&n};
         return cudaLaunchKernel(up, p.grid, p.block, a2, 0, s);
     }
-    ost_pick<float>(g.dim, c.unit_w, &mu, &up);
+    ost_pick<float>(g.dim, c.unit_w, d.fields, &mu, &up);
     OstP<float> q = ost_narrow<float>(c, g.dim);
     void* a1[] = {(void*)&in, (void*)&work, (void*)&gg, (void*)&q, (void*)&n};
     if ((e = cudaLaunchKernel(mu, p.grid, p.block, a1, 0, s)) != cudaSuccess) return e;
