@@ -195,6 +195,9 @@ static void release(mmsp_gpu_handle* h)
 {
     if (h->out) pf::output_release(h);   // waits for snapshots still being written
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (int p = 0; p < 2; p++)
+        if (h->cs_graph[p]) cudaGraphExecDestroy(h->cs_graph[p]);
+    if (h->cs_host) cudaFreeHost(h->cs_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->buf[0]) cudaFree(h->buf[0]);
@@ -431,6 +434,46 @@ static int build_graph(mmsp_gpu_handle* h)
 // (cahn-hilliard.cpp:311-388); then the guess becomes the state.
 static const unsigned kCsMaxIter = 10000;    // max_iter, cahn-hilliard.cpp:55
 static const unsigned kCsResidualStep = 5;   // residual_step, cahn-hilliard.cpp:54
+// After iteration kCsResidualStep the checks fall every kCsResidualStep
+// iterations: those chunks (sweeps, residual, read-back into pinned memory)
+// replay one CUDA graph per state buffer, built on first use.
+static int convex_chunk_graph(mmsp_gpu_handle* h, int p)
+{
+    if (h->cs_graph[p]) return MMSP_GPU_OK;
+    cudaError_t e;
+    if (!h->cs_host && (e = cudaHostAlloc((void**)&h->cs_host, 2 * sizeof(double), cudaHostAllocDefault)) != cudaSuccess)
+        return cuda_fail(h, e, "convex pinned buffer");
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(h, e, "graph stream");
+    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return cuda_fail(h, e, "begin capture");
+    }
+    const void* old = h->buf[p];
+    void* nw = h->buf[p ^ 1];
+    cudaError_t le = cudaSuccess;
+    for (unsigned k = 0; k < kCsResidualStep && le == cudaSuccess; k++)
+        le = pf::launch_convex_sweeps(h->d, h->g, h->c, old, nw, cs);
+    if (le == cudaSuccess) le = pf::launch_convex_residual(h->d, h->g, h->c, old, nw, h->partials, cs);
+    if (le == cudaSuccess)
+        le = cudaMemcpyAsync(h->cs_host, h->partials + 4 * pf::kReduceBlocks, 2 * sizeof(double),
+                             cudaMemcpyDeviceToHost, cs);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(cs, &graph);
+    cudaStreamDestroy(cs);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(h, le != cudaSuccess ? le : e, "convex capture");
+    }
+    e = cudaGraphInstantiate(&h->cs_graph[p], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        h->cs_graph[p] = nullptr;
+        return cuda_fail(h, e, "convex instantiate");
+    }
+    return MMSP_GPU_OK;
+}
+
 static int convex_steps(mmsp_gpu_handle* h, int steps)
 {
     cudaError_t e;
@@ -441,6 +484,16 @@ static int convex_steps(mmsp_gpu_handle* h, int steps)
         double residual = 1.0;
         unsigned iter = 0;
         while (iter < kCsMaxIter && residual > h->c.cs.tol) {
+            if (iter >= kCsResidualStep) {   // a whole chunk: iterations iter+1 .. iter+5, check at iter+5
+                int rc = convex_chunk_graph(h, h->cur);
+                if (rc) return rc;
+                if ((e = cudaGraphLaunch(h->cs_graph[h->cur], h->stream)) != cudaSuccess ||
+                    (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+                    return cuda_fail(h, e, "convex chunk");
+                iter += kCsResidualStep;
+                residual = sqrt(h->cs_host[0] / h->cs_host[1]) / (2.0 * h->c.cs.cells);
+                continue;
+            }
             if ((e = pf::launch_convex_sweeps(h->d, h->g, h->c, old, nw, h->stream)) != cudaSuccess)
                 return cuda_fail(h, e, "convex sweep");
             iter++;
