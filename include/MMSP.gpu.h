@@ -375,8 +375,11 @@ int mmsp_gpu_server_stop(mmsp_gpu_server* s);
  * cudaMalloc/cudaFree, which may synchronise the whole device.
  *
  * `in` and `out` are device pointers to field-major state of
- * desc->fields * cells values of the descriptor's type; `out` may equal
- * `in`.  The intermediate steps live in one file-scope device array of
+ * desc->fields * cells values of the descriptor's type (there is no layout
+ * argument: vector grids must already be field-major), both 16-byte
+ * aligned; `out` may equal `in` but must not otherwise overlap it.  A
+ * misaligned or partly overlapping pointer returns MMSP_GPU_EINVAL before
+ * any device work is queued.  The intermediate steps live in one file-scope device array of
  * MMSP_GPU_NOALLOC_MAX_BYTES shared by every call in the process; a state
  * larger than that returns MMSP_GPU_ENOMEM when steps > 1 or out == in
  * (one step from in to a distinct out needs no scratch).  Work is queued on
@@ -384,6 +387,8 @@ int mmsp_gpu_server_stop(mmsp_gpu_server* s);
  * it has finished, with MMSP_GPU_ETIMEDOUT if a kernel's bounded wait ran
  * out.  The first call on a device looks up the array's device address
  * with that device current; make that first call before any stream capture.
+ * The address is kept for the life of the process: after cudaDeviceReset on
+ * a device, do not call this entry point on that device again.
  * Calls that overlap on the GPU (from several threads or streams) share the
  * scratch array and race: serialise them.  MMSP_GPU_OSTWALD (its step needs a
  * work grid beside the state), MMSP_GPU_CH_CONVEX (an iterative solve per

@@ -12,8 +12,21 @@
 // call's kernels; the state part needs no clearing because every step
 // overwrites all of it before it is read.  Calls that overlap on the GPU
 // race on the array.
+//
+// The caller's buffers reach the FP32 3D kernels, which stage planes with
+// bulk asynchronous copies that need 16-byte-aligned global addresses, so
+// both pointers must be 16-byte aligned; a pointer that is not, or an
+// output that partly overlaps the input, is refused before anything is
+// queued on the device.
+//
+// The device address of the array is looked up once per device and kept
+// for the life of the process.  cudaDeviceReset (or anything else that
+// unloads the library's module from the device's primary context) leaves
+// the kept address stale: a process that resets a device must not call this
+// entry point on that device again.
 #include <mutex>
 
+#include <stdint.h>
 #include <string.h>
 
 #include "MMSP.gpu.h"
@@ -70,14 +83,20 @@ extern "C" int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, 
     mmsp_gpu_desc d = *desc;
     for (int a = d.dim; a < 3; a++) d.n[a] = 1;
     const size_t bytes = state_bytes(d);
+    // 16-byte alignment for the bulk-copy kernels; an output that overlaps
+    // the input without being it would be written while still being read
+    const uintptr_t pi = reinterpret_cast<uintptr_t>(in), po = reinterpret_cast<uintptr_t>(out);
+    if ((pi | po) & 15u) return MMSP_GPU_EINVAL;
+    const bool in_place = pi == po;
+    if (!in_place && pi < po + bytes && po < pi + bytes) return MMSP_GPU_EINVAL;
     cudaStream_t s = (cudaStream_t)cuda_stream;
     if (steps == 0) {
-        if (in == out) return MMSP_GPU_OK;
+        if (in_place) return MMSP_GPU_OK;
         cudaError_t e = cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) cudaGetLastError();
         return e == cudaSuccess ? MMSP_GPU_OK : MMSP_GPU_ECUDA;
     }
-    const bool in_place = in == out;
     if ((steps > 1 || in_place) && bytes > MMSP_GPU_NOALLOC_MAX_BYTES) return MMSP_GPU_ENOMEM;
 
     int dev = 0;
@@ -114,13 +133,12 @@ extern "C" int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, 
         src = dst;
     }
     if (e == cudaSuccess && src != out) e = cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToDevice, s);
+    // the error word comes back on the same stream, so one synchronisation
+    // of that stream (not of the device) covers the steps and the read
+    int f = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&f, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
-        cudaGetLastError();
-        return MMSP_GPU_ECUDA;
-    }
-    int f = 0;
-    if (cudaMemcpy(&f, flag, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
         cudaGetLastError();
         return MMSP_GPU_ECUDA;
     }

@@ -137,3 +137,26 @@ def test_batch_and_server_refuse_without_a_device(lib):
     cfg = native.ServerConfig(0, 0, 0)
     assert lib.mmsp_gpu_server_start(ctypes.byref(s), ctypes.byref(cfg)) == native.ENODEV
     assert lib.mmsp_gpu_batch_create(ctypes.byref(b), 0, arr) == native.EINVAL
+
+
+def test_noalloc_refuses_misaligned_and_overlapping_pointers(lib):
+    """mmsp_gpu_step_noalloc checks the caller's pointers on the host, before
+    it touches a device: the FP32 3D kernels stage planes with bulk copies
+    that need 16-byte-aligned addresses, and an output that partly overlaps
+    the input would be written while it is still read.  The addresses below
+    are never dereferenced (no device work is queued for a refused call),
+    so the test runs without a GPU."""
+    from mmsp_gb300 import native
+
+    d = native.make_desc((40, 24, 64), 1, np.float32, "ch", dt=0.002)
+    nbytes = 40 * 24 * 64 * 4
+    base = 1 << 32
+    call = lambda i, o, steps=1: lib.mmsp_gpu_step_noalloc(ctypes.byref(d), ctypes.c_void_p(i),
+                                                           ctypes.c_void_p(o), steps, None)
+    assert call(base + 4, base + nbytes + 256) == native.EINVAL        # input 4 bytes off a 16-byte boundary
+    assert call(base, base + nbytes + 260) == native.EINVAL            # output misaligned
+    assert call(base + 8, base + 8) == native.EINVAL                   # in place, misaligned
+    assert call(base, base + nbytes - 16) == native.EINVAL             # output overlaps the input's tail
+    assert call(base + 4096, base) == native.EINVAL                    # input overlaps the output's tail
+    assert call(base, base + 16, 0) == native.EINVAL                   # a zero-step copy checks too
+    assert call(0, base) == native.EINVAL                              # NULL
