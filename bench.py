@@ -1,12 +1,24 @@
 """Benchmark of the explicit phase-field step (one JSON line on stdout).
 
 Default workload: 3D Cahn-Hilliard, f=c^2(1-c)^2, 256^3 cells, dt=0.002,
-kappa=M=1, periodic, 1000 explicit steps per bench step, FP32 precision form
-(FP64 compensated reductions).  ``value`` is cell-updates/s with the state
-resident in HBM; ``e2e`` is the same metric through the C ABI call a user's
-update(grid&, steps) makes (mmsp_gpu_update: pinned host buffer in, device
-steps, host buffer out, all inside the timed region).  The FP64 plain form is
-measured on the same grid and reported under ``forms``.
+kappa=M=1, periodic, 1000 explicit steps per bench step, in FP64 -- the
+arithmetic of the reference's own update() -- with fused multiply-adds
+(MMSP_GPU_FLAG_CONTRACT: within 1e-12 relative of the reference).  ``value``
+is cell-updates/s with the state resident in HBM; ``e2e`` is the same metric
+through the C ABI call a user's update(grid&, steps) makes (mmsp_gpu_update:
+pinned host buffer in, device steps, host buffer out, all inside the timed
+region).  The FP64 step is bound by the FP64 pipe, so ``roofline`` compares
+its FP64 operations per second with the device's measured FP64 rate
+(mmsp_gpu_fp64_rate).
+
+Beside the headline the line carries, measured in the same run:
+``forms``    the bit-identical FP64 form and the FP32 precision form (HBM
+             roofline, e2e, error and mass drift against FP64);
+``batched``  256 2D Cahn-Hilliard grids of sides 64..512 in FP32, against
+             the same 256 solves one at a time in FP64;
+``serving``  a Poisson stream of mixed requests through the request loop,
+             p50/p99 latency, against the same requests one at a time in FP64;
+``configs``  the other single-grid configurations and models.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -31,12 +43,16 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "cell-updates/s (3D Cahn-Hilliard 256^3, 1000 explicit steps)"
+METRIC = "cell-updates/s (3D Cahn-Hilliard 256^3, 1000 explicit steps, FP64)"
 SHAPE = (256, 256, 256)
 SOLVE_STEPS = 1000
 DT, KAPPA, MOB = 0.002, 1.0, 1.0
 MEAN, AMP, SEED = 0.4, 0.02, 2
-WORKLOAD = "ch3d_256_f32"
+WORKLOAD = "ch3d_256_f64"
+# FP64 pipe operations (add, multiply or fused multiply-add) per cell-step of
+# the two FP64 forms (pf_ch64.cu: 9 + 7 contracted, 13 + 10 exact)
+F64_OPS_CONTRACT = 16
+F64_OPS_EXACT = 23
 
 
 def dist_env():
@@ -187,7 +203,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "ch3d_256_f64_cpu", "grid": list(SHAPE), "steps_per_solve": SOLVE_STEPS,
+        "config": {"workload": WORKLOAD, "grid": list(SHAPE), "steps_per_solve": SOLVE_STEPS,
                    "dt": DT, "kappa": KAPPA, "M": MOB, "parallelism": "host threads"},
         "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
                          "sample": sample},
@@ -224,7 +240,9 @@ def other_configs(native, inputs, stream):
     res = {}
     c2 = inputs.noisy_composition((256, 256), 0.5, 0.01, 1)
     ms, _ = timed(native.make_desc((256, 256), 1, np.float64, "ch", dt=0.005), c2, 2000)
-    res["ch2d_256_f64_2000"] = {"ms": ms, "cell_updates_per_s": 256 * 256 * 2000 / (ms / 1e3)}
+    msc, _ = timed(native.make_desc((256, 256), 1, np.float64, "ch", dt=0.005, contract=True), c2, 2000)
+    res["ch2d_256_f64_2000"] = {"ms": ms, "cell_updates_per_s": 256 * 256 * 2000 / (ms / 1e3),
+                                "contracted_ms": msc, "contracted_cell_updates_per_s": 256 * 256 * 2000 / (msc / 1e3)}
     e = inputs.voronoi_grains((128, 128, 128), 200, 8, 3)
     ms32, o32 = timed(native.make_desc((128, 128, 128), 8, np.float32, "ac", gamma=1.5, kappa=2.0, dt=0.05),
                       e.astype(np.float32), 500)
@@ -345,6 +363,54 @@ def output_path(native, inputs):
             "speedup_vs_reference_write": ref / (wall / 3)}
 
 
+def timed_solver(native, stream, flush):
+    """One bench step on `stream`: reset the state from a device copy
+    (untimed), flush L2 (untimed), then `steps` steps between CUDA events on
+    the same stream."""
+    import torch
+
+    def solve(s, init, nbytes, steps=SOLVE_STEPS):
+        with torch.cuda.stream(stream):
+            s.upload_device(init.data_ptr(), nbytes, native.FIELD_MAJOR)
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.step(steps)
+            e1.record(stream)
+        return e0, e1
+
+    return solve
+
+
+def e2e_update(native, desc, host, reps, warmup, flush):
+    """mmsp_gpu_update (create, upload from the pinned host buffer, 1000
+    steps, reduction, download into it, destroy), timed on the host around
+    the call; the host buffer is refilled (untimed) before every call."""
+    import ctypes
+
+    import torch
+
+    L = native.load()
+    stats = native.Stats()
+    hv, c0 = host
+    nbytes = hv.nbytes
+    times = []
+    for i in range(warmup + reps):
+        hv[:] = c0
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        rc = L.mmsp_gpu_update(ctypes.byref(desc), hv.ctypes.data, nbytes, native.CELL_MAJOR, SOLVE_STEPS,
+                               ctypes.byref(stats))
+        t2 = time.perf_counter()
+        if rc != 0:
+            raise native.GpuError(rc, "mmsp_gpu_update")
+        if i >= warmup:
+            times.append(t2 - t1)
+    return float(np.mean(times)), nbytes
+
+
 def run_gpu(args):
     import torch
 
@@ -367,32 +433,20 @@ def run_gpu(args):
     c0_32 = c0.astype(np.float32)
     stream = torch.cuda.Stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    solve = timed_solver(native, stream, flush)
 
-    def make(dtype):
-        d = native.make_desc(SHAPE, 1, dtype, "ch", kappa=KAPPA, mobility=MOB, dt=DT)
+    def make(dtype, contract=False):
+        d = native.make_desc(SHAPE, 1, dtype, "ch", kappa=KAPPA, mobility=MOB, dt=DT, contract=contract)
         s = native.Stepper(d)
         s.set_stream(stream.cuda_stream)
-        return s
+        return d, s
 
-    s32 = make(np.float32)
-    init32 = torch.from_numpy(c0_32).cuda()
-    nbytes32 = init32.numel() * 4
-
-    def timed_solve(s, init, nbytes):
-        """One bench step on `stream`: reset the state (untimed), flush L2
-        (untimed), then 1000 steps between CUDA events on the same stream."""
-        with torch.cuda.stream(stream):
-            s.upload_device(init.data_ptr(), nbytes, native.FIELD_MAJOR)
-            flush.zero_()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            s.step(SOLVE_STEPS)
-            e1.record(stream)
-        return e0, e1
-
+    # ---- headline: FP64 (contracted) on the device -------------------------------------------
+    d64, s64 = make(np.float64, contract=True)
+    init64 = torch.from_numpy(c0).cuda()
+    nbytes64 = init64.numel() * 8
     for _ in range(args.warmup):
-        timed_solve(s32, init32, nbytes32)
+        solve(s64, init64, nbytes64)
     stream.synchronize()
     torch.cuda.synchronize()
     barrier()
@@ -401,7 +455,7 @@ def run_gpu(args):
     evs = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        evs.append(timed_solve(s32, init32, nbytes32))
+        evs.append(solve(s64, init64, nbytes64))
     stream.synchronize()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -410,72 +464,89 @@ def run_gpu(args):
     ms = [a.elapsed_time(b) for a, b in evs]
     ms_step = max_over_ranks(float(np.mean(ms)), "cuda")
     value = job_throughput(cells * SOLVE_STEPS, ms_step / 1e3, ws)
-    # accuracy of the timed form: FP32 result vs the FP64 plain form, mass drift
-    st32 = s32.reduce()
-    out32 = s32.download().astype(np.float64)
-
-    # FP64 plain form on the same grid (reported beside the headline)
-    s64 = make(np.float64)
-    init64 = torch.from_numpy(c0).cuda()
-    timed_solve(s64, init64, init64.numel() * 8)
-    stream.synchronize()
-    a, b = timed_solve(s64, init64, init64.numel() * 8)
-    stream.synchronize()
-    ms64 = a.elapsed_time(b)
     st64 = s64.reduce()
-    out64 = s64.download()
-    err = np.abs(out32 - out64)
-    m0 = float(np.sum(c0))
+    out64c = s64.download()
     s64.close()
+    m0 = float(np.sum(c0))
 
-    # end to end through the C ABI with pinned host buffers
-    d32 = native.make_desc(SHAPE, 1, np.float32, "ch", kappa=KAPPA, mobility=MOB, dt=DT)
-    host = torch.empty(cells, dtype=torch.float32, pin_memory=True)
-    hv = host.numpy()
-    L = native.load()
-    import ctypes
-    stats = native.Stats()
-    e2e_t = []
-    for i in range(args.warmup + args.steps):
-        hv[:] = c0_32.ravel()
-        flush.zero_()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        rc = L.mmsp_gpu_update(ctypes.byref(d32), host.data_ptr(), nbytes32, native.CELL_MAJOR, SOLVE_STEPS,
-                               ctypes.byref(stats))
-        t2 = time.perf_counter()
-        if rc != 0:
-            raise native.GpuError(rc, "mmsp_gpu_update")
-        if i >= args.warmup:
-            e2e_t.append(t2 - t1)
-    e2e_s = max_over_ranks(float(np.mean(e2e_t)), "cuda")
+    # FP64 roofline: FP64 pipe operations per step over the measured FP64 rate
+    fp64_peak = native.fp64_rate(stream.cuda_stream)
+    step_s = ms_step / 1e3 / SOLVE_STEPS
+    fp64_achieved = F64_OPS_CONTRACT * cells / step_s
+    hbm_peak, peak_kind = peaks()
+
+    # ---- bit-identical FP64 form (the reference's operation order) ----------------------------
+    dx64, sx64 = make(np.float64, contract=False)
+    solve(sx64, init64, nbytes64)
+    a, b = solve(sx64, init64, nbytes64)
+    stream.synchronize()
+    ms_exact = a.elapsed_time(b)
+    stx = sx64.reduce()
+    out64 = sx64.download()
+    sx64.close()
+    rel_contract = float(np.abs(out64c - out64).max() / np.abs(out64).max())
+
+    # ---- e2e FP64 through mmsp_gpu_update with pinned host buffers ----------------------------
+    host64 = torch.empty(cells, dtype=torch.float64, pin_memory=True)
+    e2e_s, _ = e2e_update(native, d64, (host64.numpy(), c0.ravel()), args.steps, 1, flush)
+    e2e_s = max_over_ranks(e2e_s, "cuda")
     e2e_val = job_throughput(cells * SOLVE_STEPS, e2e_s, ws)
 
-    peak, peak_kind = peaks()
-    alg_bytes = cells * 2 * 4                     # one read + one write of the FP32 state per step
-    launch_s = ms_step / 1e3 / SOLVE_STEPS
-    achieved = alg_bytes / launch_s / 1e9
-    traffic = profile_traffic("ch3_stream_f32_256")
+    # ---- FP32 precision form -------------------------------------------------------------------
+    d32, s32 = make(np.float32)
+    init32 = torch.from_numpy(c0_32).cuda()
+    nbytes32 = init32.numel() * 4
+    for _ in range(args.warmup):
+        solve(s32, init32, nbytes32)
+    ev32 = [solve(s32, init32, nbytes32) for _ in range(args.steps)]
+    stream.synchronize()
+    ms32 = float(np.mean([a.elapsed_time(b) for a, b in ev32]))
+    st32 = s32.reduce()
+    out32 = s32.download().astype(np.float64)
+    s32.close()
+    err = np.abs(out32 - out64)
+    host32 = torch.empty(cells, dtype=torch.float32, pin_memory=True)
+    e2e32_s, _ = e2e_update(native, d32, (host32.numpy(), c0_32.ravel()), min(args.steps, 5), 1, flush)
+    alg32 = cells * 2 * 4                      # one read + one write of the FP32 state per step
+    ach32 = alg32 / (ms32 / 1e3 / SOLVE_STEPS) / 1e9
+
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64, c=0.4+0.02*U(-1,1))",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64, c=0.4+0.02*U(-1,1))",
         "config": {"workload": WORKLOAD, "grid": list(SHAPE), "steps_per_solve": SOLVE_STEPS, "dt": DT,
                    "kappa": KAPPA, "M": MOB, "bc": "periodic", "parallelism": "replicas" if ws > 1 else "1 GPU",
-                   "l2": "flushed (256 MiB write) before every timed solve; FP32 working set 134 MB"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "ch3_stream_f32<8,256,2,CH,unit>", "peak_source": peak_kind,
-                     "alg_bytes_per_launch": alg_bytes},
-        "e2e": {"value": e2e_val, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes32,
-                "d2h_bytes_per_step": nbytes32 + 16, "ms_per_step": e2e_s * 1e3},
-        "gpu_launches": args.steps * SOLVE_STEPS,
+                   "form": "FP64, fused multiply-adds (MMSP_GPU_FLAG_CONTRACT), <= 1e-12 relative of the reference",
+                   "l2": "flushed (256 MiB write) before every timed solve; FP64 working set 403 MB (state, "
+                         "newGrid, temp)"},
+        "roofline": {"bound": "fp64", "achieved": fp64_achieved / 1e12, "peak": fp64_peak / 1e12,
+                     "unit": "T FP64 ops/s", "frac": fp64_achieved / fp64_peak,
+                     "traffic": profile_traffic("ch64_step_f64_256"),
+                     "kernel": "ch64_mu + ch64_update (one step: two launches)",
+                     "peak_source": "measured live: mmsp_gpu_fp64_rate (independent FP64 FMA chains, all SMs)",
+                     "ops_per_launch": F64_OPS_CONTRACT * cells, "ops_per_cell": F64_OPS_CONTRACT,
+                     "hbm": {"alg_bytes_per_step": cells * 40,
+                             "achieved_gbs": cells * 40 / step_s / 1e9, "peak_gbs": hbm_peak,
+                             "note": "read c, write mu; read mu and c, write c' (40 B per cell)"}},
+        "e2e": {"value": e2e_val, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes64,
+                "d2h_bytes_per_step": nbytes64 + 16, "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": args.steps * SOLVE_STEPS * 2,
         "forms": {
-            "f32_precision": {"cell_updates_per_s": value, "ms_per_solve": ms_step,
+            "f64_contracted": {"cell_updates_per_s": value, "ms_per_solve": ms_step,
+                               "max_rel_err_vs_exact": rel_contract, "mass_drift": (st64.mass - m0) / m0},
+            "f64_exact": {"cell_updates_per_s": cells * SOLVE_STEPS / (ms_exact / 1e3), "ms_per_solve": ms_exact,
+                          "mass_drift": (stx.mass - m0) / m0,
+                          "fp64_frac": F64_OPS_EXACT * cells / (ms_exact / 1e3 / SOLVE_STEPS) / fp64_peak,
+                          "note": "bit-identical to the reference's update()"},
+            "f32_precision": {"cell_updates_per_s": cells * SOLVE_STEPS / (ms32 / 1e3), "ms_per_solve": ms32,
                               "max_err_vs_f64": float(err.max()), "l2_err_vs_f64": float(np.sqrt(np.mean(err ** 2))),
-                              "mass_drift": (st32.mass - m0) / m0},
-            "f64_plain": {"cell_updates_per_s": cells * SOLVE_STEPS / (ms64 / 1e3), "ms_per_solve": ms64,
-                          "mass_drift": (st64.mass - m0) / m0},
+                              "mass_drift": (st32.mass - m0) / m0,
+                              "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm_peak, "unit": "GB/s",
+                                           "frac": ach32 / hbm_peak, "traffic": profile_traffic("ch3_stream_f32_256"),
+                                           "kernel": "ch3_stream_f32<8,256,2,CH,unit>", "peak_source": peak_kind,
+                                           "alg_bytes_per_launch": alg32},
+                              "e2e": {"value": cells * SOLVE_STEPS / e2e32_s, "unit": "cell-updates/s",
+                                      "h2d_bytes_per_step": nbytes32, "d2h_bytes_per_step": nbytes32 + 16}},
         },
         "clocks": clk,
         "wall_s_timed_region": wall,
@@ -483,11 +554,12 @@ def run_gpu(args):
     line["configs"] = other_configs(native, inputs, stream)
     if rank == 0:
         line["output"] = output_path(native, inputs)
+        line["batched"] = batched(native, inputs, stream, max(3, args.steps // 4), flush)
+        line["serving"] = serving(native, args.serve_requests, 200.0, 5, sequential=True)
     if rank == 0 and args.cpu_baseline:
         v, n, el = cpu_sample(1)
         line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
                                 "sample": "%d explicit FP64 steps of the 256^3 grid (%.1f s), serial C oracle" % (n, el)}
-    s32.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -496,10 +568,102 @@ def run_gpu(args):
     return 0
 
 
+BATCH_STEPS = 1000
+
+
+def batched(native, inputs, stream, reps, flush):
+    """Batched 2D Cahn-Hilliard (256 grids, sides 64..512, own kappa and mean
+    composition, dt 0.005, 1000 steps each) in FP32 through mmsp_gpu_batch_*,
+    against the same 256 solves one at a time in FP64 (contracted form) on
+    the same GPU: the device time with the states resident, and end to end
+    with host buffers in and out (mmsp_gpu_update per grid for the sequential
+    side).  The FP32 results' largest deviation from FP64 is the accuracy."""
+    import torch
+
+    work = inputs.batched_cahn_hilliard(count=256, seed=4)
+    cells = sum(c0.size for c0, _ in work)
+    host = [c0.astype(np.float32) for c0, _ in work]
+    descs = [native.make_desc(c0.shape, 1, np.float32, "ch", kappa=k, mobility=1.0, dt=0.005) for c0, k in work]
+    b = native.Batch(descs)
+    b.set_stream(stream.cuda_stream)
+    for i, h in enumerate(host):
+        b.upload(i, h)
+    b.tune()
+    info = b.info()
+    times = []
+    for it in range(1 + reps):
+        for i, h in enumerate(host):          # reset (untimed)
+            b.upload(i, h)
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            b.step(BATCH_STEPS)
+            e1.record(stream)
+        stream.synchronize()
+        if it >= 1:
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    out32 = [b.download(i).astype(np.float64) for i in range(len(work))]
+    e2e = []
+    for _ in range(max(2, reps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i, h in enumerate(host):
+            b.upload(i, h)
+        b.step(BATCH_STEPS)
+        res = [b.download(i) for i in range(len(work))]
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e))
+    b.close()
+    del res
+    # one at a time, FP64: resident (device time of the steps) and end to end (mmsp_gpu_update)
+    seq_dev = 0.0
+    seq_e2e = 0.0
+    err = 0.0
+    for i, (c0, k) in enumerate(work):
+        d = native.make_desc(c0.shape, 1, np.float64, "ch", kappa=k, mobility=1.0, dt=0.005, contract=True)
+        with native.Stepper(d) as s:
+            s.upload(c0)
+            s.synchronize()
+            t1 = time.perf_counter()
+            s.step(BATCH_STEPS)
+            s.synchronize()
+            seq_dev += time.perf_counter() - t1
+        t1 = time.perf_counter()
+        o64, _ = native.update(c0, BATCH_STEPS, d)
+        seq_e2e += time.perf_counter() - t1
+        err = max(err, float(np.abs(o64 - out32[i]).max()))
+    solves = len(work) / (ms / 1e3)
+    achieved = cells * 8 * BATCH_STEPS / (ms / 1e3) / 1e9      # FP32 read + write per cell-step
+    peak, peak_kind = peaks()
+    return {
+        "metric": "solves/s (256 x 2D Cahn-Hilliard, sides 64-512, 1000 steps, FP32)", "value": solves,
+        "unit": "solves/s", "ms_per_batch": ms, "reps": reps, "dtype": "f32",
+        "config": {"workload": "ch2d_batch256_f32", "grids": len(work), "cells": cells,
+                   "steps_per_solve": BATCH_STEPS, "dt": 0.005,
+                   "data": "synthetic (seeded; kappa~U(0.5,2), mean~U(0.3,0.7), c=mean+0.01*U(-1,1))",
+                   "tuning": {"rows_per_item": info.rows_per_item, "threads_per_block": info.threads_per_block,
+                              "blocks": info.blocks, "items": info.items, "tune_ms": info.tune_ms}},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profile_traffic("ch2_batch_f32_256grids"), "kernel": "ch2_batch_kernel<float,CH>",
+                     "peak_source": peak_kind, "alg_bytes_per_step": cells * 8},
+        "e2e": {"value": len(work) / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": cells * 4,
+                "d2h_bytes_per_step": cells * 4},
+        "sequential_f64": {"solves_per_s": len(work) / seq_dev, "seconds": seq_dev,
+                           "e2e_solves_per_s": len(work) / seq_e2e, "e2e_seconds": seq_e2e,
+                           "how": "256 solves one at a time, FP64 contracted form: device-resident step time, and "
+                                  "mmsp_gpu_update per grid (host buffers)"},
+        "speedup_vs_sequential_f64": solves / (len(work) / seq_dev),
+        "e2e_speedup_vs_sequential_f64": (len(work) / e2e_s) / (len(work) / seq_e2e),
+        "max_err_vs_f64": err,
+        "gpu_launches_per_batch": BATCH_STEPS,
+    }
+
+
 def run_batch(args):
-    """Batched 2D Cahn-Hilliard: 256 grids, sides 64..512, own kappa and mean,
-    FP32, 1000 steps each, one persistent launch per step replayed from CUDA
-    graphs; against 256 one-at-a-time FP64 plain solves on the same GPU."""
+    """`--workload batch`: the batched form alone as a bench line."""
     import torch
 
     from mmsp_gb300 import inputs, native
@@ -507,80 +671,13 @@ def run_batch(args):
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     native.load()
-    steps = 1000
-    work = inputs.batched_cahn_hilliard(count=256, seed=4)
-    cells = sum(c0.size for c0, _ in work)
-    descs = [native.make_desc(c0.shape, 1, np.float32, "ch", kappa=k, mobility=1.0, dt=0.005) for c0, k in work]
     stream = torch.cuda.Stream()
-    b = native.Batch(descs)
-    b.set_stream(stream.cuda_stream)
-    for i, (c0, _) in enumerate(work):
-        b.upload(i, c0.astype(np.float32))
-    b.tune()
-    info = b.info()
-
-    def reset():
-        for i, (c0, _) in enumerate(work):
-            b.upload(i, c0.astype(np.float32))
-
-    times = []
-    for it in range(args.warmup + args.steps):
-        reset()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            e0.record(stream)
-            b.step(steps)
-            e1.record(stream)
-        stream.synchronize()
-        if it >= args.warmup:
-            times.append(e0.elapsed_time(e1))
-    ms = float(np.mean(times))
-    out32 = [b.download(i).astype(np.float64) for i in range(len(work))]
-    # end to end: host buffers in, all grids advanced, host buffers out
-    host = [c0.astype(np.float32) for c0, _ in work]
-    t0 = time.perf_counter()
-    for i, h in enumerate(host):
-        b.upload(i, h)
-    b.step(steps)
-    res = [b.download(i) for i in range(len(work))]
-    e2e_s = time.perf_counter() - t0
-    b.close()
-    # one at a time, FP64 plain form, state resident, each solve synchronised
-    seq = 0.0
-    err = 0.0
-    for i, (c0, k) in enumerate(work):
-        d = native.make_desc(c0.shape, 1, np.float64, "ch", kappa=k, mobility=1.0, dt=0.005)
-        with native.Stepper(d) as s:
-            s.upload(c0)
-            s.synchronize()
-            t1 = time.perf_counter()
-            s.step(steps)
-            s.synchronize()
-            seq += time.perf_counter() - t1
-            err = max(err, float(np.abs(s.download() - out32[i]).max()))
-    solves = len(work) / (ms / 1e3)
-    alg_bytes = cells * 8                       # FP32 read + write per cell-step
-    achieved = alg_bytes * steps / (ms / 1e3) / 1e9
-    peak, peak_kind = peaks()
-    line = {
-        "metric": "batched solves/s (256 x 2D Cahn-Hilliard, sides 64-512, 1000 steps)", "value": solves,
-        "unit": "solves/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded; kappa~U(0.5,2), mean~U(0.3,0.7), c=mean+0.01*U(-1,1))",
-        "config": {"workload": "ch2d_batch256_f32", "grids": len(work), "cells": cells, "steps_per_solve": steps,
-                   "dt": 0.005, "tuning": {"rows_per_item": info.rows_per_item,
-                                           "threads_per_block": info.threads_per_block, "blocks": info.blocks,
-                                           "items": info.items, "tune_ms": info.tune_ms}},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "ch2_batch_kernel<float,CH>", "peak_source": peak_kind},
-        "e2e": {"value": len(work) / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": cells * 4,
-                "d2h_bytes_per_step": cells * 4},
-        "sequential_f64": {"solves_per_s": len(work) / seq, "seconds": seq},
-        "speedup_vs_sequential_f64": solves / (len(work) / seq),
-        "max_err_vs_f64": err,
-        "gpu_launches": args.steps * steps,
-    }
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    r = batched(native, inputs, stream, args.steps, flush)
+    line = dict(r)
+    line.update({"n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_batch"],
+                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                 "data": r["config"]["data"], "gpu_launches": args.steps * BATCH_STEPS})
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -620,82 +717,88 @@ def make_state(shape, fields, seed):
     return e
 
 
-def run_serve(args):
-    """Poisson arrivals of mixed solves into the request loop; p50/p99 latency
-    and solves/s, at the offered rate and at a sustainable one; one-at-a-time
-    FP64 plain solves/s estimated from per-kind FP64 rates measured here."""
+def serving(native, n, rate, seed, sequential=True):
+    """Poisson arrivals (`rate` per second) of `n` mixed FP32 requests into the
+    request loop (mmsp_gpu_server_*): host buffers in at submit, results
+    fetched to the host; p50/p99 latency from submit to finish and solves/s
+    over the span from the first submit to the last finish.  With
+    `sequential`, the same requests are then solved one at a time in FP64
+    (contracted form) through mmsp_gpu_update on the same GPU, which gives
+    the measured one-at-a-time baseline and the FP32 results' accuracy."""
     import threading
 
+    reqs = serve_requests(n, seed)
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    states = [make_state(sh, f, s) for sh, f, _, _, _, s in reqs]
+    descs = [native.make_desc(sh, f, np.float32, m, **p) for sh, f, m, p, _, _ in reqs]
+    srv = native.Server()
+    ids = [None] * n
+
+    def feeder():
+        t0 = time.perf_counter()
+        for i in range(n):
+            dt = arrivals[i] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids[i] = srv.submit(descs[i], states[i], reqs[i][4])
+
+    th = threading.Thread(target=feeder)
+    th.start()
+    th.join()
+    lat, fin, sub, results = [], [], [], []
+    for i in range(n):
+        st = srv.wait(ids[i], 3600.0)
+        assert st.state == native.REQ_DONE, (st.state, st.message, reqs[i])
+        lat.append(st.finish_s - st.submit_s)
+        fin.append(st.finish_s)
+        sub.append(st.submit_s)
+        results.append(srv.fetch(ids[i]) if sequential else None)
+    stats = srv.stats()
+    srv.stop()
+    span = max(fin) - min(sub)
+    work = sum(int(np.prod(sh)) * f * st for sh, f, _, _, st, _ in reqs)
+    out = {"metric": "served solves/s, p50/p99 latency (mixed CH/AC requests, Poisson arrivals, FP32)",
+           "value": n / span, "unit": "solves/s", "dtype": "f32", "rate_offered": rate, "requests": n,
+           "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)), "span_s": span,
+           "value_updates_per_s": work / span, "rounds": int(stats.rounds),
+           "arrival_window_s": float(arrivals[-1]),
+           "config": {"workload": "serve_mix_f32", "mix": "50% 2D CH sides 64-1024, 30% 3D CH sides 32-256, "
+                      "20% 3D AC N=4-16 sides 32-128; steps log-uniform 100-10000", "seed": seed},
+           "e2e": {"value": n / span, "unit": "solves/s",
+                   "h2d_bytes_per_step": int(sum(x.nbytes for x in states)),
+                   "d2h_bytes_per_step": int(sum(x.nbytes for x in states)),
+                   "note": "requests submitted from host buffers and fetched to host buffers"}}
+    if sequential:
+        seq = 0.0
+        err = 0.0
+        for (sh, f, m, p, st, _), x, r in zip(reqs, states, results):
+            d = native.make_desc(sh, f, np.float64, m, contract=True, **p)
+            t0 = time.perf_counter()
+            o64, _ = native.update(x.astype(np.float64), st, d)
+            seq += time.perf_counter() - t0
+            err = max(err, float(np.abs(o64 - r.astype(np.float64)).max()))
+        out["sequential_f64"] = {"solves_per_s": n / seq, "seconds": seq,
+                                 "how": "the same requests one at a time in FP64 (contracted form) through "
+                                        "mmsp_gpu_update: host buffer in, steps, host buffer out"}
+        out["speedup_vs_sequential_f64"] = (n / span) / (n / seq)
+        out["max_err_vs_f64"] = err
+    return out
+
+
+def run_serve(args):
+    """`--workload serve`: the serving form at the offered rate (with the
+    measured sequential FP64 baseline) and at a sustainable rate."""
     from mmsp_gb300 import native
 
     native.load()
-
-    def one_run(rate, n, seed):
-        reqs = serve_requests(n, seed)
-        rng = np.random.default_rng(seed + 1)
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
-        states = [make_state(sh, f, s) for sh, f, _, _, _, s in reqs]
-        descs = [native.make_desc(sh, f, np.float32, m, **p) for sh, f, m, p, _, _ in reqs]
-        srv = native.Server()
-        ids = [None] * n
-
-        def feeder():
-            t0 = time.perf_counter()
-            for i in range(n):
-                dt = arrivals[i] - (time.perf_counter() - t0)
-                if dt > 0:
-                    time.sleep(dt)
-                ids[i] = srv.submit(descs[i], states[i], reqs[i][4])
-
-        th = threading.Thread(target=feeder)
-        th.start()
-        th.join()
-        lat, fin, sub = [], [], []
-        for i in range(n):
-            st = srv.wait(ids[i], 3600.0)
-            assert st.state == native.REQ_DONE, (st.state, st.message, reqs[i])
-            lat.append(st.finish_s - st.submit_s)
-            fin.append(st.finish_s)
-            sub.append(st.submit_s)
-        stats = srv.stats()
-        srv.stop()
-        span = max(fin) - min(sub)
-        work = sum(int(np.prod(sh)) * f * st for sh, f, _, _, st, _ in reqs)
-        return {"rate_offered": rate, "requests": n, "solves_per_s": n / span, "p50_s": float(np.percentile(lat, 50)),
-                "p99_s": float(np.percentile(lat, 99)), "span_s": span, "value_updates_per_s": work / span,
-                "rounds": int(stats.rounds), "arrival_window_s": float(arrivals[-1])}, reqs
-
-    offered, reqs = one_run(200.0, args.serve_requests, 5)
-    sustained, _ = one_run(max(1.0, 0.7 * offered["solves_per_s"]), max(50, args.serve_requests // 2), 6)
-    # one-at-a-time FP64 plain: per-kind FP64 value-update rates, measured on representative grids
-    kinds = {"ch2": ((512, 512), 1, "ch", dict(dt=0.005)), "ch3": ((144, 144, 144), 1, "ch", dict(dt=0.002)),
-             "ac": ((80, 80, 80), 10, "ac", dict(dt=0.05, kappa=2.0, gamma=1.5))}
-    rate64 = {}
-    for k, (sh, f, m, p) in kinds.items():
-        d = native.make_desc(sh, f, np.float64, m, **p)
-        with native.Stepper(d) as s:
-            s.upload(make_state(sh, f, 1).astype(np.float64))
-            s.step(10)
-            s.synchronize()
-            t0 = time.perf_counter()
-            s.step(50)
-            s.synchronize()
-            rate64[k] = int(np.prod(sh)) * f * 50 / (time.perf_counter() - t0)
-    t64 = 0.0
-    for sh, f, m, p, st, _ in reqs:
-        k = "ac" if m == "ac" else ("ch3" if len(sh) == 3 else "ch2")
-        t64 += int(np.prod(sh)) * f * st / rate64[k]
-    seq64 = len(reqs) / t64
-    line = {
-        "metric": "served solves/s and p50/p99 latency (mixed CH/AC requests, Poisson arrivals)",
-        "value": offered["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 0,
-        "ms_per_step": offered["span_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded request mix and states)",
-        "config": {"workload": "serve_mix_f32", "offered_rate": 200.0, "requests": args.serve_requests},
-        "offered": offered, "sustainable": sustained,
-        "sequential_f64_estimate": {"solves_per_s": seq64, "value_updates_per_s_by_kind": rate64},
-        "speedup_vs_sequential_f64": offered["solves_per_s"] / seq64,
-    }
+    offered = serving(native, args.serve_requests, 200.0, 5, sequential=True)
+    sustained = serving(native, max(50, args.serve_requests // 2), max(1.0, 0.7 * offered["value"]), 6,
+                        sequential=False)
+    line = dict(offered)
+    line.update({"n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": offered["span_s"] * 1e3,
+                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                 "data": "synthetic (seeded request mix and states)", "sustainable": sustained})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -704,6 +807,7 @@ CASES = {
     # name: (shape, fields, dtype, model, params)
     "ch3d_f32": (SHAPE, 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
     "ch3d_f64": (SHAPE, 1, np.float64, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
+    "ch3d_f64c": (SHAPE, 1, np.float64, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB, contract=True)),
     "ch2d_f64": ((256, 256), 1, np.float64, "ch", dict(dt=0.005, kappa=1.0, mobility=1.0)),
     "ac3d_f32": ((128, 128, 128), 8, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
@@ -758,7 +862,7 @@ def main():
     ap.add_argument("--case", choices=sorted(CASES) + ["batch_f32"], help="run one workload untimed (for ncu)")
     ap.add_argument("--case-steps", type=int, default=5)
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "batch", "serve"])
-    ap.add_argument("--serve-requests", type=int, default=300)
+    ap.add_argument("--serve-requests", type=int, default=100)
     args = ap.parse_args()
     if args.case:
         return run_case(args.case, args.case_steps)

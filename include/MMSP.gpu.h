@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define MMSP_GPU_ABI_VERSION 2
+#define MMSP_GPU_ABI_VERSION 3
 
 /* Status codes. */
 #define MMSP_GPU_OK            0
@@ -69,6 +69,13 @@ extern "C" {
 /* Storage type of the state (and the arithmetic of the step). */
 #define MMSP_GPU_F64 0   /* plain form: reference operation order, no fused multiply-add */
 #define MMSP_GPU_F32 1   /* precision form: FP32 state and arithmetic, FP64 reductions */
+
+/* mmsp_gpu_desc.flags */
+#define MMSP_GPU_FLAG_CONTRACT 1  /* FP64 Cahn-Hilliard (MMSP_GPU_CH, MMSP_GPU_CH_POLY) in 2D and 3D:
+                                     fused multiply-adds and a regrouped Laplacian (16 FP64 operations
+                                     per cell instead of the reference order's 23); results within
+                                     1e-12 relative of the reference instead of bit-identical.  Other
+                                     models, dims and FP32 ignore it. */
 
 /* Models.  Parameters are read from mmsp_gpu_desc as noted. */
 #define MMSP_GPU_CH       0  /* Cahn-Hilliard, f=c^2(1-c)^2: mu = 2c(1-c)(1-2c) - kappa*lap c;
@@ -118,6 +125,9 @@ typedef struct mmsp_gpu_desc {
     int dtype;        /* MMSP_GPU_F64 or MMSP_GPU_F32 */
     int model;        /* MMSP_GPU_CH ... MMSP_GPU_OSTWALD */
     int bc[3][2];     /* lower/upper boundary per axis; the device path takes periodic only */
+    int flags;        /* MMSP_GPU_FLAG_* (0: none); mmsp_gpu_desc_init clears it.  Added in ABI
+                         version 3 in what was padding, so the layout of the other members is
+                         that of version 2 */
     double dx[3];     /* cell spacing per axis */
     double dt;        /* time step */
     double kappa;     /* gradient coefficient (K of the shipped examples) */
@@ -201,6 +211,14 @@ int mmsp_gpu_state(mmsp_gpu_handle* h, void** dev_ptr);
 
 /* Message of the last failure on this handle ("" if none). */
 const char* mmsp_gpu_last_error(const mmsp_gpu_handle* h);
+
+/* FP64 operations per second of the current device: a probe of independent
+ * fused multiply-add chains on every SM (about 20 ms, on `cuda_stream`,
+ * NULL: the legacy default stream).  Each add, multiply or fused
+ * multiply-add counts one operation.  The FP64 forms of the step are bound
+ * by this rate on GB300, not by memory; it is their roofline.  No
+ * counterpart in the reference (it runs on the CPU). */
+int mmsp_gpu_fp64_rate(void* cuda_stream, double* ops_per_second);
 
 /* One call per update(grid&, steps): create, upload `host`, advance `steps`,
  * download into `host`, destroy.  `stats` may be NULL. */

@@ -150,6 +150,7 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     if (d->model == MMSP_GPU_OSTWALD && (!(d->aux[2] != d->aux[1]) || !(d->aux[4] != 0.0)))
         BAD(MMSP_GPU_EINVAL, "Ostwald ripening needs Calpha != Cbeta and delta != 0");
     if (d->fields > 32) BAD(MMSP_GPU_EUNSUPPORTED, "fields=%d above 32", d->fields);
+    if (d->flags & ~MMSP_GPU_FLAG_CONTRACT) BAD(MMSP_GPU_EINVAL, "unknown flags 0x%x", (unsigned)d->flags);
     long long yz = 1;
     for (int a = (d->dim >= 2 ? d->dim - 2 : 0); a < d->dim; a++) yz *= d->n[a];
     if (yz >= (1LL << 31)) BAD(MMSP_GPU_EUNSUPPORTED, "plane of %lld cells above 2^31", yz);
@@ -175,10 +176,18 @@ static size_t state_bytes(const mmsp_gpu_desc* d)
 // Device scratch of a model beyond the two state buffers: the Ostwald
 // model's chemical-potential grid (one value per cell); for convex
 // splitting, a staging copy of the state for cell-major downloads.
+// FP64 Cahn-Hilliard in 2D/3D keeps the reference's temp grid (mu) between
+// its two passes (pf_ch64.cu).
+static bool two_pass_f64(const mmsp_gpu_desc* d)
+{
+    return d->dtype == MMSP_GPU_F64 && (d->dim == 2 || d->dim == 3) &&
+           (d->model == MMSP_GPU_CH || d->model == MMSP_GPU_CH_POLY);
+}
+
 static size_t work_bytes(const mmsp_gpu_desc* d)
 {
     if (d->model == MMSP_GPU_CH_CONVEX) return state_bytes(d);   // download staging (the guess stays put)
-    if (d->model != MMSP_GPU_OSTWALD) return 0;
+    if (d->model != MMSP_GPU_OSTWALD && !two_pass_f64(d)) return 0;
     return state_bytes(d) / (size_t)d->fields;
 }
 
@@ -217,6 +226,7 @@ static int make_plan(mmsp_gpu_handle* h)
     }
     bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
     cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::plan_ostwald(h->d, h->g, &h->plan)
+                    : two_pass_f64(&h->d) && pf::ch64_eligible(h->d, h->g) ? pf::plan_ch64(h->d, h->g, &h->plan)
                     : ch ? pf::plan_ch(h->d, h->g, &h->plan) : pf::plan_ac(h->d, h->g, &h->plan);
     if (e != cudaSuccess) {
         if (!h->plan.ok && !ch) return fail(h, MMSP_GPU_EUNSUPPORTED, "%s", "too many fields for shared memory");
@@ -388,6 +398,7 @@ static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s, long long step =
     pf::Coeffs c = h->c;
     c.step = step;
     cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, c, in, out, h->work, s)
+                    : h->plan.kind == 6 ? pf::launch_ch64(h->plan, h->d, h->g, c, in, out, h->work, s)
                     : ch ? pf::launch_ch(h->plan, h->d, h->g, c, in, out, h->flags, s)
                          : pf::launch_ac(h->plan, h->d, h->g, c, in, out, h->flags, s);
     h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913

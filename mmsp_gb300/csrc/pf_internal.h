@@ -77,12 +77,14 @@ Coeffs make_coeffs(const mmsp_gpu_desc& d);
 // A prepared launch of one explicit step.
 struct StepPlan {
     const void* fn;    // kernel
+    const void* fn2;   // second kernel of two-pass plans (FP64 Cahn-Hilliard: the update pass)
     dim3 grid, block;
     size_t smem;
     int planes;        // planes of axis X per block (3D streaming)
     int fields;
     int kind;          // 0: generic tile kernel, 1: FP32 3D CH streaming, 2: FP32 3D AC streaming,
-                       // 3: FP32 CH rows of any length, 4: Ostwald ripening (two kernels)
+                       // 3: FP32 CH rows of any length, 4: Ostwald ripening (two kernels),
+                       // 5: convex splitting, 6: FP64 CH in two passes through a work grid
     int ring;          // planes in the shared-memory ring (streaming kernels)
     bool ok;
 };
@@ -96,6 +98,13 @@ bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g);
 cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c, const void* in, void* out,
                               int* err, cudaStream_t s);
+
+// FP64 2D/3D Cahn-Hilliard in two passes, mu into `work` (cells values),
+// then the update (pf_ch64.cu).  Needs the work grid, so only handles use it.
+bool ch64_eligible(const mmsp_gpu_desc& d, const Geom& g);
+cudaError_t plan_ch64(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
+cudaError_t launch_ch64(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* in,
+                        void* out, void* work, cudaStream_t s);
 
 // FP32 2D/3D Cahn-Hilliard for any row length up to 1024 (pf_rows.cu).
 bool ch_rows_eligible(const mmsp_gpu_desc& d, const Geom& g);

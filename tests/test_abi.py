@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_version_and_strerror(lib):
-    assert lib.mmsp_gpu_version() == 2
+    assert lib.mmsp_gpu_version() == 3
     assert lib.mmsp_gpu_strerror(0) == b"ok"
     assert lib.mmsp_gpu_strerror(-4) == b"unsupported configuration"
 
@@ -55,7 +55,13 @@ def test_desc_init_defaults(lib):
     assert lib.mmsp_gpu_desc_init(ctypes.byref(d), 2, n, 3, native.F64, native.OSTWALD) == 0
     assert (d.dt, d.kappa, d.mobility) == (0.001, 2.0, 1.0)              # ostwald.cpp:66-80
     assert list(d.aux) == [1.0, 0.05, 0.95, 2.0, 1.0, 3.0]
-    assert ctypes.sizeof(native.Desc) == 4 * 13 + 4 + 8 * 15     # C layout: 13 ints, padding, 15 doubles
+    assert ctypes.sizeof(native.Desc) == 4 * 14 + 8 * 15          # C layout: 14 ints, 15 doubles
+    assert native.Desc.dx.offset == 56                             # where ABI version 2 had it
+    assert d.flags == 0
+    d.flags = 2
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL   # unknown flag
+    d.flags = native.FLAG_CONTRACT
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.OK
 
 
 def test_ostwald_validation_and_footprint(lib):

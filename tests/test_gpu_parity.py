@@ -251,6 +251,79 @@ def test_full_3d_256_fp64_checksum_and_fp32_error(gpu):
     assert abs(st32.mass - m["mass0"]) / m["mass0"] < 1e-6
 
 
+CONTRACT_CASES = [
+    ("ch", (9, 11), dict(kappa=1.0, mobility=1.0, dt=0.005)),
+    ("ch", (40, 3, 70), dict(kappa=1.0, mobility=1.0, dt=0.002)),
+    ("ch", (17, 33, 45), dict(kappa=0.7, mobility=1.3, dt=0.0005, dx=[0.9, 1.1, 1.7])),
+    ("ch", (1, 4, 6), dict(kappa=1.0, mobility=1.0, dt=0.002)),
+    ("ch_poly", (24, 20, 36), dict(r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=0.005)),
+    ("ch_poly", (33, 45), dict(r=0.8, u=1.2, kappa=1.0, mobility=0.5, dt=0.01, dx=[1.2, 0.8])),
+]
+
+
+@pytest.mark.parametrize("model,shape,prm", CONTRACT_CASES,
+                         ids=["%s-%s" % (m, "x".join(map(str, s))) for m, s, _ in CONTRACT_CASES])
+def test_fp64_contracted_against_oracle(gpu, oracle, model, shape, prm):
+    """FP64 with MMSP_GPU_FLAG_CONTRACT (fused multiply-adds, regrouped
+    Laplacian): within TOL_SHIPPED relative of the oracle, which is
+    bit-identical to the reference; the flag-free run stays bitwise."""
+    from mmsp_gb300 import inputs
+
+    c0 = inputs.noisy_composition(shape, 0.45 if model == "ch" else 0.0, 0.03 if model == "ch" else 0.1,
+                                  300 + len(shape))
+    steps = 150    # past the graph threshold
+    d = gpu.make_desc(shape, 1, np.float64, model, contract=True, **prm)
+    got = run_gpu(gpu, d, c0, steps)
+    dx = prm.get("dx")
+    if model == "ch":
+        want = oracle.ch_baseline(c0, steps, prm["kappa"], prm["mobility"], prm["dt"], dx=dx)
+    else:
+        want = oracle.ch_shipped(c0, steps, prm["r"], prm["u"], prm["kappa"], prm["mobility"], prm["dt"], dx=dx)
+    assert np.isfinite(want).all()    # a stable case
+    rel = np.abs(got - want).max() / np.abs(want).max()
+    assert rel <= TOL_SHIPPED, rel
+    if model == "ch":
+        exact = run_gpu(gpu, gpu.make_desc(shape, 1, np.float64, model, **prm), c0, steps)
+        assert np.array_equal(exact, want)
+
+
+def test_full_2d_256_fp64_contracted(gpu):
+    """2D 256^2 x 2000 steps: the contracted FP64 form within 1e-12 relative
+    of the reference (whose result the exact form reproduces bit for bit:
+    checksum), and the reference's own sampled values."""
+    from mmsp_gb300 import inputs
+
+    m = FULL["ch2d_256_2000"]
+    c0 = inputs.noisy_composition(tuple(m["shape"]), m["mean"], m["amplitude"], m["seed"])
+    kw = dict(kappa=m["kappa"], mobility=m["M"], dt=m["dt"])
+    exact, _ = gpu.update(c0, m["steps"], gpu.make_desc(c0.shape, 1, np.float64, "ch", **kw))
+    assert sha(exact) == m["sha256"]
+    fast, st = gpu.update(c0, m["steps"], gpu.make_desc(c0.shape, 1, np.float64, "ch", contract=True, **kw))
+    rel = np.abs(fast - exact).max() / np.abs(exact).max()
+    assert rel <= TOL_SHIPPED, rel
+    sample = fast.ravel()[::m["sample_stride"]][:len(m["sample"])]
+    assert np.abs(sample - np.array(m["sample"])).max() <= TOL_SHIPPED * np.abs(exact).max()
+    assert st.mass == pytest.approx(m["mass"], rel=1e-12)
+    assert st.energy == pytest.approx(m["energy"], rel=1e-12)
+
+
+def test_full_3d_256_fp64_contracted(gpu):
+    """3D 256^3 x 1000 steps: the contracted FP64 form within 1e-12 relative
+    of the exact form, which matches the oracle's checksum."""
+    from mmsp_gb300 import inputs
+
+    m = FULL["ch3d_256_1000"]
+    c0 = inputs.noisy_composition(tuple(m["shape"]), m["mean"], m["amplitude"], m["seed"])
+    kw = dict(kappa=m["kappa"], mobility=m["M"], dt=m["dt"])
+    exact, _ = gpu.update(c0, m["steps"], gpu.make_desc(c0.shape, 1, np.float64, "ch", **kw))
+    assert sha(exact) == m["sha256"]
+    fast, st = gpu.update(c0, m["steps"], gpu.make_desc(c0.shape, 1, np.float64, "ch", contract=True, **kw))
+    rel = np.abs(fast - exact).max() / np.abs(exact).max()
+    assert rel <= TOL_SHIPPED, rel
+    assert st.mass == pytest.approx(m["mass"], rel=1e-12)
+    assert st.energy == pytest.approx(m["energy"], rel=1e-12)
+
+
 def test_full_3d_ac_128_n8(gpu):
     """128^3 x 8 grain growth (Voronoi, 200 seeds): dt=0.05 FP64 bit-identical
     to the oracle after 500 steps, FP32 within 1e-5; dt=0.1 diverges at the
