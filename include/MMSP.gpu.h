@@ -58,6 +58,7 @@ extern "C" {
 #define MMSP_GPU_ESTOPPED     -9  /* server stopped */
 #define MMSP_GPU_EIO         -10  /* a grid file could not be opened or written */
 #define MMSP_GPU_ENOCONV     -11  /* an implicit solve reached its iteration limit (the reference aborts) */
+#define MMSP_GPU_EOVERFLOW   -12  /* a sparse cell's item list outgrew its slots (mmsp_gpu_desc.fields) */
 
 /* Boundary-condition codes, identical to include/MMSP.utility.h:23-29. */
 #define MMSP_GPU_BC_MIRROR    0
@@ -113,6 +114,18 @@ extern "C" {
                                 5th), starting from the state two steps back as the example does.
                                 mobility = D, kappa = K; aux = {C0, Ca, Cb, A, omega, tolerance};
                                 at most 10000 iterations per step (MMSP_GPU_ENOCONV beyond)    */
+#define MMSP_GPU_SPARSE_GG 8 /* isotropic sparse phase-field grain growth as shipped
+                                (examples/coarsening/grain_growth/isotropic/sparsePF/graingrowth.cpp:58-120)
+                                on grid<dim,sparse<double> > (include/MMSP.sparse.h:19), FP64: each
+                                cell a list of (grain index, value) items in insertion order, at most
+                                `fields` items (1..32, MMSP_GPU_EOVERFLOW beyond); over the union S
+                                of the indices of the cell and its face neighbours, for |S| >= 2:
+                                e_i' = e_i - dt*(-e_i - e_i^3 + 2 (e_i sum e^2 - lap e_i)), stored
+                                when above epsilon = aux[0]; |S| < 2 copies the list.  As in the
+                                example, the grid written each step starts as the state of two steps
+                                back (empty at the start of each mmsp_gpu_step call, as each update()
+                                call's newGrid is), so items below epsilon keep their old values.
+                                State crosses with mmsp_gpu_sparse_upload / _download only. */
 
 /* Host/device layouts of vector-valued grids (fields > 1). */
 #define MMSP_GPU_CELL_MAJOR  0  /* value j of cell i at i*fields + j (grid<dim,vector<T>> order) */
@@ -123,7 +136,7 @@ typedef struct mmsp_gpu_desc {
     int n[3];         /* extents per axis (x1-x0), axis 0 slowest; unused axes ignored */
     int fields;       /* values per cell: 1 for grid<dim,T>, N for grid<dim,vector<T>> */
     int dtype;        /* MMSP_GPU_F64 or MMSP_GPU_F32 */
-    int model;        /* MMSP_GPU_CH ... MMSP_GPU_OSTWALD */
+    int model;        /* MMSP_GPU_CH ... MMSP_GPU_SPARSE_GG */
     int bc[3][2];     /* lower/upper boundary per axis; the device path takes periodic only */
     int flags;        /* MMSP_GPU_FLAG_* (0: none); mmsp_gpu_desc_init clears it.  Added in ABI
                          version 3 in what was padding, so the layout of the other members is
@@ -220,6 +233,21 @@ const char* mmsp_gpu_last_error(const mmsp_gpu_handle* h);
  * counterpart in the reference (it runs on the CPU). */
 int mmsp_gpu_fp64_rate(void* cuda_stream, double* ops_per_second);
 
+/* Sparse grids (MMSP_GPU_SPARSE_GG).  Replaces the storage of
+ * grid<dim,sparse<T> > (include/MMSP.sparse.h:19-60: per cell a list of
+ * item{int index; T value} in insertion order, to_buffer/from_buffer
+ * include/MMSP.sparse.cpp:140-163).  Host arrays, K = desc.fields slots per
+ * cell in node order: count[cells] items per cell (0..K), index[cells*K] and
+ * value[cells*K] (double) with the first count[c] slots of cell c in the
+ * list's order; the other slots are ignored on upload and zero on download.
+ * Upload checks the counts (MMSP_GPU_EINVAL), resets the step counter and is
+ * synchronous; download is synchronous and reports MMSP_GPU_EOVERFLOW if a
+ * list outgrew its slots.  The dense transfers, reductions, grid-file output,
+ * batches, the server and mmsp_gpu_step_noalloc refuse sparse grids
+ * (MMSP_GPU_EUNSUPPORTED). */
+int mmsp_gpu_sparse_upload(mmsp_gpu_handle* h, const int32_t* count, const int32_t* index, const void* value);
+int mmsp_gpu_sparse_download(mmsp_gpu_handle* h, int32_t* count, int32_t* index, void* value);
+
 /* One call per update(grid&, steps): create, upload `host`, advance `steps`,
  * download into `host`, destroy.  `stats` may be NULL. */
 int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t bytes, int layout,
@@ -282,10 +310,17 @@ int mmsp_gpu_output_wait(mmsp_gpu_handle* h);
  * step: a work list of (grid, run of rows) items is drained by all warps of
  * the GPU.  Other grids in the batch are advanced by their own kernels in
  * the same step.  All grids share one dtype.  Step chunks replay a CUDA
- * graph.  The run of rows per work item and the block size are chosen by an
- * autotuner on the first step (or mmsp_gpu_batch_tune) and cached per batch
- * shape, in memory and, when the environment variable MMSP_GPU_TUNE_CACHE
- * names a file, in that JSON file. */
+ * graph.  FP32 batches whose grids all join the persistent kernel can also
+ * advance by temporal blocking: each launch loads tiles of every grid with a
+ * halo of 2 cells per step into shared memory, takes 2, 4 or 8 steps there
+ * and writes the tiles back, cutting HBM traffic per step by about that
+ * factor for some redundant halo work.  The run of rows per work item and
+ * the block size of the per-step kernel, and the tile region and steps per
+ * launch of the blocked one (or none), are chosen by an autotuner on the
+ * first step (or mmsp_gpu_batch_tune) and cached per batch shape, in memory
+ * and, when the environment variable MMSP_GPU_TUNE_CACHE names a file, in
+ * that JSON file.  Results do not depend on the choice beyond FP32 rounding
+ * (the blocked kernel contracts the update into one multiply-add). */
 typedef struct mmsp_gpu_batch mmsp_gpu_batch;
 
 typedef struct mmsp_gpu_batch_info {
@@ -299,6 +334,10 @@ typedef struct mmsp_gpu_batch_info {
     int tuned_from_cache;   /* 1 when the tuning came from the cache */
     double tune_ms;         /* wall time spent autotuning */
     size_t device_bytes;    /* device memory the batch holds */
+    int temporal_depth;     /* steps per launch of the persistent kernel: 1, or the autotuned depth of
+                               the temporally blocked kernel (shared-memory tiles, FP32) */
+    int tile_rows, tile_cols;   /* its tile region (halo included), 0 when not used */
+    int tiles;              /* its work items per launch */
 } mmsp_gpu_batch_info;
 
 int mmsp_gpu_batch_create(mmsp_gpu_batch** out, int count, const mmsp_gpu_desc* descs);

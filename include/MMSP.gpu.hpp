@@ -43,6 +43,11 @@
 #include "MMSP.gpu.h"
 
 namespace MMSP {
+
+// MMSP's sparse cell type (include/MMSP.sparse.h:19), declared so that the
+// sparse grid overloads below can name it; the caller's MMSP headers define it.
+template <typename T> class sparse;
+
 namespace gpu {
 
 struct Model {
@@ -50,6 +55,7 @@ struct Model {
     double dt, kappa, mobility, gamma, r, u;
     double aux[6];   // further parameters (mmsp_gpu_desc.aux); zero unless the model takes them
     int flags;       // MMSP_GPU_FLAG_* (mmsp_gpu_desc.flags)
+    int slots;       // sparse grids: item slots per cell on the device (mmsp_gpu_desc.fields; 0: 16)
 };
 
 // The same model with the FP64 Cahn-Hilliard step contracted (fused
@@ -133,6 +139,13 @@ inline Model cahn_hilliard_convex_splitting(double C0 = 0.45, double Ca = 0.05, 
     Model m = {MMSP_GPU_CH_CONVEX, 1.0 / (D * K), K, D, 1.0, 0.0, 0.0, {C0, Ca, Cb, A, omega, tolerance}};
     return m;
 }
+// examples/coarsening/grain_growth/isotropic/sparsePF/graingrowth.cpp:58-120 as shipped, on
+// grid<dim,sparse<double> >: at most `slots` items per cell on the device (MMSP_GPU_EOVERFLOW beyond)
+inline Model sparse_grain_growth_shipped(double dt = 0.01, double epsilon = 1.0e-8, int slots = 16)
+{
+    Model m = {MMSP_GPU_SPARSE_GG, dt, 1.0, 1.0, 1.0, 0.0, 0.0, {epsilon, 0.0, 0.0, 0.0, 0.0, 0.0}, 0, slots};
+    return m;
+}
 // allen-cahn.cpp:57-70 as shipped (scalar grid)
 inline Model allen_cahn_shipped(double r, double u, double K, double M, double dt)
 {
@@ -211,6 +224,46 @@ int try_update(Grid<dim, Vec<T> >& g, int steps, const Model& m, mmsp_gpu_stats*
     if (rc) return report(rc, "device step");
     for (int i = 0; i < n; i++)
         for (int j = 0; j < N; j++) g(i)[j] = buf[(size_t)i * N + j];
+    return MMSP_GPU_OK;
+}
+
+// Sparse grids: grid<dim,sparse<double> > (the sparsePF example).  Each
+// cell's items travel in their stored order (length/index/value of
+// include/MMSP.sparse.h:82-103) and come back through set(), so the host
+// grid ends as the reference's update() leaves it.
+template <template <int, typename> class Grid, int dim, typename T>
+int try_update(Grid<dim, sparse<T> >& g, int steps, const Model& m, mmsp_gpu_stats* stats = 0)
+{
+    (void)stats;   // the example reports no reductions
+    const int K = m.slots > 0 ? m.slots : 16;
+    mmsp_gpu_desc d;
+    int rc = describe(g, dim, K, dtype_of<T>::value, m, &d);
+    if (rc) return report(rc, "descriptor");
+    const int n = nodes(g);
+    std::vector<int32_t> count((size_t)n), index((size_t)n * K, 0);
+    std::vector<double> value((size_t)n * K, 0.0);
+    for (int i = 0; i < n; i++) {
+        const int len = length(g(i));
+        if (len > K) return report(MMSP_GPU_EOVERFLOW, "sparse cell longer than the slots");
+        count[i] = len;
+        for (int h = 0; h < len; h++) {
+            index[(size_t)i * K + h] = MMSP::index(g(i), h);
+            value[(size_t)i * K + h] = MMSP::value(g(i), h);
+        }
+    }
+    mmsp_gpu_handle* hd = 0;
+    rc = mmsp_gpu_create(&hd, &d);
+    if (rc) return report(rc, "create");
+    rc = mmsp_gpu_sparse_upload(hd, &count[0], &index[0], &value[0]);
+    if (!rc) rc = mmsp_gpu_step(hd, steps);
+    if (!rc) rc = mmsp_gpu_sparse_download(hd, &count[0], &index[0], &value[0]);
+    if (rc) std::cerr << "MMSP::gpu::update: " << mmsp_gpu_last_error(hd) << std::endl;
+    mmsp_gpu_destroy(hd);
+    if (rc) return report(rc, "device step");
+    for (int i = 0; i < n; i++) {
+        g(i) = sparse<T>();
+        for (int h = 0; h < count[i]; h++) MMSP::set(g(i), index[(size_t)i * K + h]) = value[(size_t)i * K + h];
+    }
     return MMSP_GPU_OK;
 }
 

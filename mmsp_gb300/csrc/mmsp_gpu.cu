@@ -50,6 +50,7 @@ extern "C" const char* mmsp_gpu_strerror(int code)
     case MMSP_GPU_ESTOPPED: return "server stopped";
     case MMSP_GPU_EIO: return "grid file could not be written";
     case MMSP_GPU_ENOCONV: return "implicit solver did not converge";
+    case MMSP_GPU_EOVERFLOW: return "sparse cell list outgrew its slots";
     default: return "unknown status";
     }
 }
@@ -90,6 +91,10 @@ extern "C" int mmsp_gpu_desc_init(mmsp_gpu_desc* d, int dim, const int* n, int f
         d->aux[4] = 1.2;     // omega
         d->aux[5] = 1.0e-14; // tolerance
         break;
+    case MMSP_GPU_SPARSE_GG:                                      // sparsePF/graingrowth.cpp:77-78
+        d->dt = 0.01;
+        d->aux[0] = 1.0e-8;   // epsilon
+        break;
     case MMSP_GPU_OSTWALD:                                        // ostwald.cpp:66-80
         d->dt = 0.001;
         d->kappa = 2.0;
@@ -111,7 +116,7 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
     if (!d) BAD(MMSP_GPU_EINVAL, "NULL descriptor");
     if (d->dim < 1 || d->dim > 3) BAD(MMSP_GPU_EINVAL, "dim %d outside 1..3", d->dim);
     if (d->dtype != MMSP_GPU_F64 && d->dtype != MMSP_GPU_F32) BAD(MMSP_GPU_EINVAL, "dtype %d", d->dtype);
-    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_CH_CONVEX) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
+    if (d->model < MMSP_GPU_CH || d->model > MMSP_GPU_SPARSE_GG) BAD(MMSP_GPU_EINVAL, "model %d", d->model);
     long long cells = 1;
     for (int a = 0; a < d->dim; a++) {
         if (d->n[a] < 1) BAD(MMSP_GPU_EINVAL, "extent n[%d]=%d", a, d->n[a]);
@@ -138,6 +143,11 @@ static int validate(const mmsp_gpu_desc* d, char* why, size_t nwhy)
                                            "n[%d]=%d", a, d->n[a]);
         if (!(d->aux[4] > 0.0 && d->aux[4] < 2.0) || !(d->aux[5] > 0.0) || !(d->aux[1] != d->aux[0]))
             BAD(MMSP_GPU_EINVAL, "convex splitting: omega in (0,2), tolerance > 0 and Ca != C0");
+    }
+    if (d->model == MMSP_GPU_SPARSE_GG) {
+        if (d->dtype != MMSP_GPU_F64) BAD(MMSP_GPU_EUNSUPPORTED, "sparse grain growth runs in FP64");
+        if (!isfinite(d->aux[0])) BAD(MMSP_GPU_EINVAL, "sparse grain growth: epsilon (aux[0]) not finite");
+        if (cells >= (1LL << 31)) BAD(MMSP_GPU_EUNSUPPORTED, "sparse grid of %lld cells above 2^31", cells);
     }
     if (d->model == MMSP_GPU_OSTWALD && d->fields < 2)
         BAD(MMSP_GPU_EINVAL, "Ostwald ripening takes a composition and at least one order parameter, fields=%d",
@@ -168,6 +178,11 @@ static size_t esize_of(const mmsp_gpu_desc* d) { return d->dtype == MMSP_GPU_F64
 
 static size_t state_bytes(const mmsp_gpu_desc* d)
 {
+    if (d->model == MMSP_GPU_SPARSE_GG) {
+        long long cells = 1;
+        for (int a = 0; a < d->dim; a++) cells *= d->n[a];
+        return pf::sparse_layout(cells, d->fields).bytes;
+    }
     size_t n = (size_t)d->fields;
     for (int a = 0; a < d->dim; a++) n *= (size_t)d->n[a];
     return n * esize_of(d);
@@ -221,6 +236,11 @@ static int make_plan(mmsp_gpu_handle* h)
 {
     if (h->d.model == MMSP_GPU_CH_CONVEX) {   // kernels are launched directly (pf_convex.cu)
         h->plan.kind = 5;
+        h->plan.ok = true;
+        return MMSP_GPU_OK;
+    }
+    if (h->d.model == MMSP_GPU_SPARSE_GG) {   // pf_sparse.cu
+        h->plan.kind = 7;
         h->plan.ok = true;
         return MMSP_GPU_OK;
     }
@@ -315,6 +335,8 @@ extern "C" int mmsp_gpu_set_stream(mmsp_gpu_handle* h, void* s)
 static int check_io(mmsp_gpu_handle* h, const void* p, size_t bytes, int layout)
 {
     if (!h || !p) return MMSP_GPU_EINVAL;
+    if (h->d.model == MMSP_GPU_SPARSE_GG)
+        return fail(h, MMSP_GPU_EUNSUPPORTED, "%s", "sparse grids cross with mmsp_gpu_sparse_upload/_download");
     if (bytes != h->bytes) {
         char a[64], b[64];
         snprintf(a, sizeof a, "%zu", bytes);
@@ -399,6 +421,7 @@ static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s, long long step =
     c.step = step;
     cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, c, in, out, h->work, s)
                     : h->plan.kind == 6 ? pf::launch_ch64(h->plan, h->d, h->g, c, in, out, h->work, s)
+                    : h->plan.kind == 7 ? pf::launch_sparse_gg(h->d, h->g, c, in, out, h->flags, s)
                     : ch ? pf::launch_ch(h->plan, h->d, h->g, c, in, out, h->flags, s)
                          : pf::launch_ac(h->plan, h->d, h->g, c, in, out, h->flags, s);
     h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913
@@ -535,6 +558,12 @@ extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
     if (steps == 0) return MMSP_GPU_OK;
     cudaError_t e = cudaEventRecord(h->ev0, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "event");
+    if (h->d.model == MMSP_GPU_SPARSE_GG) {
+        // each call starts newGrid with empty cells, as update()'s copy-constructed newGrid
+        // (sparsePF/graingrowth.cpp:67); within the call it keeps the state of two steps back
+        e = cudaMemsetAsync(h->buf[h->cur ^ 1], 0, sizeof(int) * (size_t)h->g.cells, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "sparse newGrid");
+    }
     int left = steps;
     if (h->d.model == MMSP_GPU_CH_CONVEX) {
         int rc = convex_steps(h, steps);
@@ -567,15 +596,18 @@ extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
     return MMSP_GPU_OK;
 }
 
-// After a synchronisation: report (and clear) a kernel's timed-out wait.
+// After a synchronisation: report (and clear) a kernel's timed-out wait
+// (word 0) or a sparse list that outgrew its slots (word 1).
 static int check_flags(mmsp_gpu_handle* h)
 {
-    int f = 0;
-    cudaError_t e = cudaMemcpy(&f, h->flags, sizeof(int), cudaMemcpyDeviceToHost);
+    int f[2] = {0, 0};
+    cudaError_t e = cudaMemcpy(f, h->flags, sizeof(f), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(h, e, "flags");
-    if (f) {
-        cudaMemset(h->flags, 0, sizeof(int));
-        return fail(h, MMSP_GPU_ETIMEDOUT, "%s", "a step kernel's bounded wait ran out; the state is invalid");
+    if (f[0] || f[1]) {
+        cudaMemset(h->flags, 0, sizeof(f));
+        if (f[0]) return fail(h, MMSP_GPU_ETIMEDOUT, "%s", "a step kernel's bounded wait ran out; the state is invalid");
+        return fail(h, MMSP_GPU_EOVERFLOW, "%s", "a sparse cell's list outgrew its slots (desc.fields); "
+                                                  "the state is invalid");
     }
     return MMSP_GPU_OK;
 }
@@ -591,6 +623,8 @@ extern "C" int mmsp_gpu_synchronize(mmsp_gpu_handle* h)
 extern "C" int mmsp_gpu_reduce(mmsp_gpu_handle* h, mmsp_gpu_stats* st)
 {
     if (!h || !st) return MMSP_GPU_EINVAL;
+    if (h->d.model == MMSP_GPU_SPARSE_GG)
+        return fail(h, MMSP_GPU_EUNSUPPORTED, "%s", "no reductions of sparse grids (the example reports none)");
     cudaError_t e = pf::launch_reduce(h->d, h->g, h->c, h->buf[h->cur], h->partials, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "reduce");
     double res[2];
@@ -625,6 +659,7 @@ extern "C" int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t byt
                                mmsp_gpu_stats* stats)
 {
     if (!host || steps < 0) return MMSP_GPU_EINVAL;
+    if (desc && desc->model == MMSP_GPU_SPARSE_GG) return MMSP_GPU_EUNSUPPORTED;   // lists: use a handle
     mmsp_gpu_handle* h = nullptr;
     int rc = mmsp_gpu_create(&h, desc);
     if (rc) return rc;
@@ -634,4 +669,56 @@ extern "C" int mmsp_gpu_update(const mmsp_gpu_desc* desc, void* host, size_t byt
     if (!rc) rc = mmsp_gpu_download(h, host, bytes, layout);
     mmsp_gpu_destroy(h);
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Sparse grids: host cell-major slots through a staging copy in the idle
+// buffer (newGrid, which every step call clears anyway).
+
+extern "C" int mmsp_gpu_sparse_upload(mmsp_gpu_handle* h, const int32_t* count, const int32_t* index, const void* value)
+{
+    if (!h || !count || !index || !value) return MMSP_GPU_EINVAL;
+    if (h->d.model != MMSP_GPU_SPARSE_GG) return fail(h, MMSP_GPU_EINVAL, "%s", "not a sparse grid");
+    const long long cells = h->g.cells;
+    const int K = h->d.fields;
+    for (long long c = 0; c < cells; c++)
+        if (count[c] < 0 || count[c] > K)
+            return fail(h, MMSP_GPU_EINVAL, "%s", "a cell's count is outside 0..fields");
+    const pf::SparseLayout L = pf::sparse_layout(cells, K);
+    char* st = static_cast<char*>(h->buf[1]);
+    cudaError_t e = cudaMemcpyAsync(st, count, sizeof(int) * (size_t)cells, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(st + L.idx_off, index, sizeof(int) * (size_t)cells * K, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(st + L.val_off, value, sizeof(double) * (size_t)cells * K, cudaMemcpyHostToDevice,
+                            h->stream);
+    if (e == cudaSuccess) e = pf::launch_sparse_pack(st, h->buf[0], cells, K, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(st, 0, sizeof(int) * (size_t)cells, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "sparse upload");
+    h->cur = 0;
+    h->steps = 0;
+    h->timed = false;
+    return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_sparse_download(mmsp_gpu_handle* h, int32_t* count, int32_t* index, void* value)
+{
+    if (!h || !count || !index || !value) return MMSP_GPU_EINVAL;
+    if (h->d.model != MMSP_GPU_SPARSE_GG) return fail(h, MMSP_GPU_EINVAL, "%s", "not a sparse grid");
+    const long long cells = h->g.cells;
+    const int K = h->d.fields;
+    const pf::SparseLayout L = pf::sparse_layout(cells, K);
+    char* st = static_cast<char*>(h->buf[h->cur ^ 1]);
+    cudaError_t e = pf::launch_sparse_unpack(h->buf[h->cur], st, cells, K, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(count, st, sizeof(int) * (size_t)cells, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(index, st + L.idx_off, sizeof(int) * (size_t)cells * K, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(value, st + L.val_off, sizeof(double) * (size_t)cells * K, cudaMemcpyDeviceToHost,
+                            h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "sparse download");
+    return check_flags(h);
 }

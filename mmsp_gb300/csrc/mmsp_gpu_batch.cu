@@ -40,7 +40,8 @@ struct Member {
 };
 
 struct Tuning {
-    int rows = 0, threads = 0;
+    int rows = 0, threads = 0;   // per-step kernel: rows per work item, block size
+    int ks = 0, shape = 0;       // temporally blocked kernel: steps per launch (0: not used), region shape
 };
 
 std::mutex g_tune_mu;
@@ -67,6 +68,9 @@ struct mmsp_gpu_batch {
     bool unit;
     int npersistent;
     Tuning tune;
+    // temporally blocked kernel (FP32 batches of persistent grids only)
+    TbItem* d_tb;
+    int tb_nitems, tb_cap, tb_blocks;
     bool tuned, tuned_from_cache;
     double tune_ms;
     int blocks;
@@ -97,6 +101,7 @@ static void brelease(mmsp_gpu_batch* b)
     if (b->counters) cudaFree(b->counters);
     if (b->d_insts) cudaFree(b->d_insts);
     if (b->d_items) cudaFree(b->d_items);
+    if (b->d_tb) cudaFree(b->d_tb);
     if (b->own) cudaStreamDestroy(b->own);
 }
 
@@ -109,7 +114,8 @@ extern "C" int mmsp_gpu_batch_create(mmsp_gpu_batch** out, int count, const mmsp
         if (rc) return rc;
         if (descs[i].dtype != descs[0].dtype) return MMSP_GPU_EINVAL;
         // serve these through handles: a work grid, or a per-step noise index
-        if (descs[i].model == MMSP_GPU_OSTWALD || descs[i].model == MMSP_GPU_CH_CONVEX || pf::noisy(descs[i]))
+        if (descs[i].model == MMSP_GPU_OSTWALD || descs[i].model == MMSP_GPU_CH_CONVEX ||
+            descs[i].model == MMSP_GPU_SPARSE_GG || pf::noisy(descs[i]))
             return MMSP_GPU_EUNSUPPORTED;
     }
     int ndev = 0;
@@ -317,6 +323,70 @@ static int set_items(mmsp_gpu_batch* b, int rows, int threads)
     return MMSP_GPU_OK;
 }
 
+// The temporally blocked kernel applies when every grid of an FP32 batch
+// joins the persistent kernel (grids with their own plans advance one step
+// per launch).
+static bool tb_possible(const mmsp_gpu_batch* b)
+{
+    return b->dtype == MMSP_GPU_F32 && b->npersistent > 0 && b->npersistent == (int)b->m.size();
+}
+
+// Tiles of every grid for region shape `shape` and depth `ks`, largest first.
+static int set_tb(mmsp_gpu_batch* b, int shape, int ks)
+{
+    const int H = 2 * ks;
+    const int TX = kTbShapes[shape].ri - 2 * H, TZ = kTbShapes[shape].ci - 2 * H;
+    std::vector<TbItem> items;
+    for (int i = 0; i < (int)b->insts.size(); i++) {
+        const int n0 = b->insts[i].n0, n1 = b->insts[i].n1;
+        for (int x0 = 0; x0 < n0; x0 += TX)
+            for (int z0 = 0; z0 < n1; z0 += TZ)
+                items.push_back(TbItem{i, x0, z0, std::min(TX, n0 - x0), std::min(TZ, n1 - z0)});
+    }
+    std::stable_sort(items.begin(), items.end(),
+                     [](const TbItem& a, const TbItem& c) { return a.tx * a.tz > c.tx * c.tz; });
+    if ((int)items.size() > b->tb_cap) {
+        if (b->d_tb) cudaFree(b->d_tb);
+        b->d_tb = nullptr;
+        b->tb_cap = 0;
+        if (cudaMalloc((void**)&b->d_tb, sizeof(TbItem) * items.size()) != cudaSuccess) {
+            cudaGetLastError();
+            return bfail(b, MMSP_GPU_ENOMEM, "tile list");
+        }
+        b->tb_cap = (int)items.size();
+    }
+    cudaError_t e = cudaMemcpyAsync(b->d_tb, items.data(), sizeof(TbItem) * items.size(), cudaMemcpyHostToDevice,
+                                    b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "tile list upload");
+    const void* fn = tb_kernel(shape, ks, b->persistent_model, b->unit);
+    const size_t smem = tb_smem(shape);
+    if ((e = ensure_smem(fn, smem)) != cudaSuccess) return bcuda(b, e, "tile kernel shared memory");
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem)) != cudaSuccess)
+        return bcuda(b, e, "occupancy");
+    b->tb_blocks = std::max(1, per_sm) * sm_count();
+    b->tb_nitems = (int)items.size();
+    b->tune.ks = ks;
+    b->tune.shape = shape;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return MMSP_GPU_OK;
+}
+
+// tune.ks steps of every grid from pool `in` to pool `out` in one launch.
+static cudaError_t step_tb(mmsp_gpu_batch* b, cudaStream_t s, int in, int out)
+{
+    const int parity = (int)(b->launches & 1);
+    cudaError_t e = launch_tb(tb_kernel(b->tune.shape, b->tune.ks, b->persistent_model, b->unit), b->tb_blocks,
+                              tb_smem(b->tune.shape), b->d_insts, b->d_tb, b->tb_nitems, b->pool[in], b->pool[out],
+                              b->counters, parity, s);
+    b->launches++;
+    return e;
+}
+
 // One step from pool `in` to pool `out`.
 static cudaError_t step_once(mmsp_gpu_batch* b, cudaStream_t s, int in, int out)
 {
@@ -371,12 +441,13 @@ static void load_cache_file()
     FILE* f = fopen(path, "r");
     if (!f) return;
     char key[128];
-    int rows, threads;
-    // one entry per line: "key": [rows, threads],
+    Tuning t;
+    // one entry per line: "key": [rows, threads, steps per launch, region shape],
     char line[512];
     while (fgets(line, sizeof line, f))
-        if (sscanf(line, " \"%127[^\"]\" : [ %d , %d ]", key, &rows, &threads) == 3 && rows > 0 && threads > 0)
-            g_tune[key] = Tuning{rows, threads};
+        if (sscanf(line, " \"%127[^\"]\" : [ %d , %d , %d , %d ]", key, &t.rows, &t.threads, &t.ks, &t.shape) == 5 &&
+            t.rows > 0 && t.threads > 0 && t.ks >= 0 && t.shape >= 0 && t.shape < kTbShapeCount)
+            g_tune[key] = t;
     fclose(f);
 }
 
@@ -390,11 +461,22 @@ static void save_cache_file()
     fprintf(f, "{\n");
     size_t i = 0;
     for (const auto& kv : g_tune)
-        fprintf(f, "  \"%s\": [%d, %d]%s\n", kv.first.c_str(), kv.second.rows, kv.second.threads,
-                ++i < g_tune.size() ? "," : "");
+        fprintf(f, "  \"%s\": [%d, %d, %d, %d]%s\n", kv.first.c_str(), kv.second.rows, kv.second.threads,
+                kv.second.ks, kv.second.shape, ++i < g_tune.size() ? "," : "");
     fprintf(f, "}\n");
     fclose(f);
     rename(tmp.c_str(), path);
+}
+
+// Apply a tuning: the per-step kernel's work list always (it takes the steps
+// a temporally blocked launch cannot), and the tile list when ks > 0.
+static int apply_tuning(mmsp_gpu_batch* b, const Tuning& t)
+{
+    int rc = set_items(b, t.rows, t.threads);
+    if (rc) return rc;
+    b->tune.ks = 0;
+    if (t.ks > 0 && tb_possible(b)) return set_tb(b, t.shape, t.ks);
+    return MMSP_GPU_OK;
 }
 
 extern "C" int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force)
@@ -411,15 +493,17 @@ extern "C" int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force)
         load_cache_file();
         auto it = g_tune.find(key);
         if (!force && it != g_tune.end()) {
-            int rc = set_items(b, it->second.rows, it->second.threads);
+            int rc = apply_tuning(b, it->second);
             if (rc) return rc;
             b->tuned = b->tuned_from_cache = true;
             b->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             return MMSP_GPU_OK;
         }
     }
-    // Candidates: rows per work item x threads per block.  Each is timed on
-    // the live state (pool cur -> idle pool) with an even number of launches.
+    // Candidates: the per-step kernel's rows per work item x threads per
+    // block, then (FP32 batches) the temporally blocked kernel's region shape
+    // x steps per launch.  Each is timed on the live state (pool cur -> idle
+    // pool, so the state is not changed) and scored per step.
     static const int kRows[] = {4, 8, 16, 32, 64};
     static const int kThreads[] = {64, 128};
     cudaEvent_t e0, e1;
@@ -427,40 +511,59 @@ extern "C" int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force)
         cudaGetLastError();
         return bfail(b, MMSP_GPU_ECUDA, "tune events");
     }
-    float best = 1e30f;
-    Tuning win{16, 128};
     const long long p0 = b->launches & 1;
+    // time two launches of `one` after a warm-up one; keeps the launch-count
+    // parity, which must keep matching `cur`
+    auto time2 = [&](auto one, float* ms) -> cudaError_t {
+        cudaError_t e = one();
+        if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) e = one();
+        if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+        if (e == cudaSuccess && (b->launches & 1) != p0) e = one();
+        return e;
+    };
+    float best = 1e30f;
+    Tuning win;
+    win.rows = 16;
+    win.threads = 128;
+    int rc = MMSP_GPU_OK;
+    cudaError_t e = cudaSuccess;
     for (int rows : kRows)
         for (int threads : kThreads) {
-            int rc = set_items(b, rows, threads);
-            if (rc) {
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
-                return rc;
-            }
-            cudaError_t e = step_once(b, b->stream, b->cur, b->cur ^ 1);   // warm-up
-            if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
-            for (int k = 0; k < 2 && e == cudaSuccess; k++) e = step_once(b, b->stream, b->cur, b->cur ^ 1);
-            if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
-            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if ((rc = set_items(b, rows, threads))) goto done;
             float ms = 0;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            // keep the launch-count parity: it must keep matching `cur`
-            if (e == cudaSuccess && (b->launches & 1) != p0) e = step_once(b, b->stream, b->cur, b->cur ^ 1);
-            if (e != cudaSuccess) {
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
-                return bcuda(b, e, "tune");
-            }
-            if (ms < best) {
-                best = ms;
-                win = Tuning{rows, threads};
+            e = time2([&] { return step_once(b, b->stream, b->cur, b->cur ^ 1); }, &ms);
+            if (e != cudaSuccess) goto done;
+            if (ms / 2 < best) {
+                best = ms / 2;
+                win.rows = rows;
+                win.threads = threads;
+                win.ks = 0;
             }
         }
+    if (tb_possible(b)) {
+        for (int shape = 0; shape < kTbShapeCount; shape++)
+            for (int ks : kTbDepths) {
+                if (2 * 2 * ks >= std::min(kTbShapes[shape].ri, kTbShapes[shape].ci)) continue;   // no interior
+                if ((rc = set_tb(b, shape, ks))) goto done;
+                float ms = 0;
+                e = time2([&] { return step_tb(b, b->stream, b->cur, b->cur ^ 1); }, &ms);
+                if (e != cudaSuccess) goto done;
+                if (ms / (2 * ks) < best) {
+                    best = ms / (2 * ks);
+                    win.ks = ks;
+                    win.shape = shape;
+                }
+            }
+    }
+done:
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int rc = set_items(b, win.rows, win.threads);
+    if (e != cudaSuccess) return bcuda(b, e, "tune");
     if (rc) return rc;
+    if ((rc = apply_tuning(b, win))) return rc;
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune[key] = win;
@@ -472,6 +575,9 @@ extern "C" int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force)
     return MMSP_GPU_OK;
 }
 
+// A CUDA graph of kBatchGraphSteps steps from pool 0 at counter parity 0:
+// kBatchGraphSteps / ks temporally blocked launches, or one launch per step.
+// Either count is even, so a replay leaves the state in pool 0.
 static int build_batch_graph(mmsp_gpu_batch* b)
 {
     if (b->graph) return MMSP_GPU_OK;
@@ -486,7 +592,9 @@ static int build_batch_graph(mmsp_gpu_batch* b)
     const long long saved = b->launches;
     b->launches = 0;   // the graph starts at counter parity 0
     cudaError_t le = cudaSuccess;
-    for (int i = 0; i < kBatchGraphSteps && le == cudaSuccess; i++) le = step_once(b, cs, i & 1, (i & 1) ^ 1);
+    const int per = b->tune.ks > 0 ? b->tune.ks : 1;
+    for (int i = 0; i < kBatchGraphSteps / per && le == cudaSuccess; i++)
+        le = b->tune.ks > 0 ? step_tb(b, cs, i & 1, (i & 1) ^ 1) : step_once(b, cs, i & 1, (i & 1) ^ 1);
     b->launches = saved;
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(cs, &g);
@@ -514,6 +622,9 @@ extern "C" int mmsp_gpu_batch_step(mmsp_gpu_batch* b, int steps)
     }
     cudaError_t e;
     int left = steps;
+    const int ks = b->tune.ks;
+    // the counter parity moves with every launch and the pool with every
+    // launch too (a blocked launch is ks steps but one pool swap)
     if (steps >= 2 * kBatchGraphSteps) {
         int rc = build_batch_graph(b);
         if (rc) return rc;
@@ -526,9 +637,14 @@ extern "C" int mmsp_gpu_batch_step(mmsp_gpu_batch* b, int steps)
         }
         while (left >= kBatchGraphSteps) {
             if ((e = cudaGraphLaunch(b->graph, b->stream)) != cudaSuccess) return bcuda(b, e, "batch graph");
-            if (b->npersistent > 0) b->launches += kBatchGraphSteps;
+            if (b->npersistent > 0) b->launches += ks > 0 ? kBatchGraphSteps / ks : kBatchGraphSteps;
             left -= kBatchGraphSteps;
         }
+    }
+    while (ks > 0 && left >= ks) {
+        if ((e = step_tb(b, b->stream, b->cur, b->cur ^ 1)) != cudaSuccess) return bcuda(b, e, "batch step");
+        b->cur ^= 1;
+        left -= ks;
     }
     while (left > 0) {
         if ((e = step_once(b, b->stream, b->cur, b->cur ^ 1)) != cudaSuccess) return bcuda(b, e, "batch step");
@@ -580,8 +696,13 @@ extern "C" int mmsp_gpu_batch_get_info(const mmsp_gpu_batch* b, mmsp_gpu_batch_i
     info->items = b->nitems;
     info->tuned_from_cache = b->tuned_from_cache ? 1 : 0;
     info->tune_ms = b->tune_ms;
+    info->temporal_depth = b->tune.ks > 0 ? b->tune.ks : 1;
+    info->tile_rows = b->tune.ks > 0 ? kTbShapes[b->tune.shape].ri : 0;
+    info->tile_cols = b->tune.ks > 0 ? kTbShapes[b->tune.shape].ci : 0;
+    info->tiles = b->tune.ks > 0 ? b->tb_nitems : 0;
     info->device_bytes = 2 * (size_t)b->pool_elems * b->esize + kPartialsBytes + 256 +
-                         sizeof(BatchInst) * b->insts.size() + sizeof(BatchItem) * b->items_cap;
+                         sizeof(BatchInst) * b->insts.size() + sizeof(BatchItem) * b->items_cap +
+                         sizeof(TbItem) * b->tb_cap;
     return MMSP_GPU_OK;
 }
 

@@ -78,7 +78,8 @@ extern "C" int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, 
     if (rc) return rc;
     if (!in || !out || steps < 0) return MMSP_GPU_EINVAL;
     // a work grid of its own, or a noise stream indexed by the handle's step count
-    if (desc->model == MMSP_GPU_OSTWALD || desc->model == MMSP_GPU_CH_CONVEX || pf::noisy(*desc))
+    if (desc->model == MMSP_GPU_OSTWALD || desc->model == MMSP_GPU_CH_CONVEX || desc->model == MMSP_GPU_SPARSE_GG ||
+        pf::noisy(*desc))
         return MMSP_GPU_EUNSUPPORTED;
     mmsp_gpu_desc d = *desc;
     for (int a = d.dim; a < 3; a++) d.n[a] = 1;

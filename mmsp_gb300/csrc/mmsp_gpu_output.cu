@@ -199,6 +199,10 @@ static int file_info(const mmsp_gpu_desc* d, const mmsp_gpu_output_opts* o, Grid
         *why = "output: level must be 0..9";
         return MMSP_GPU_EINVAL;
     }
+    if (d->model == MMSP_GPU_SPARSE_GG) {
+        *why = "output: sparse grids are not written as grid files";
+        return MMSP_GPU_EUNSUPPORTED;
+    }
     memset(fi, 0, sizeof(*fi));
     fi->dim = d->dim;
     fi->vector = o->vector < 0 ? d->fields > 1 : o->vector != 0;

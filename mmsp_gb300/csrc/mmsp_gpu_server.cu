@@ -248,6 +248,7 @@ extern "C" int mmsp_gpu_server_submit(mmsp_gpu_server* s, const mmsp_gpu_desc* d
 {
     if (!s || !desc || !host || steps < 0 || !id) return MMSP_GPU_EINVAL;
     if (layout != MMSP_GPU_CELL_MAJOR && layout != MMSP_GPU_FIELD_MAJOR) return MMSP_GPU_EINVAL;
+    if (desc->model == MMSP_GPU_SPARSE_GG) return MMSP_GPU_EUNSUPPORTED;   // lists, not a dense state
     size_t fp = 0;
     int rc = mmsp_gpu_footprint(desc, &fp);
     if (rc) return rc;

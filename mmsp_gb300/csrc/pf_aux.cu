@@ -63,7 +63,8 @@ Coeffs make_coeffs(const mmsp_gpu_desc& d)
     c.gamma2 = 2.0 * d.gamma;
     c.neg_r = -d.r;
     c.u = d.u;
-    c.dtm = (d.model == MMSP_GPU_GG || d.model == MMSP_GPU_ZENER) ? d.dt : d.dt * d.mobility;
+    c.dtm = (d.model == MMSP_GPU_GG || d.model == MMSP_GPU_ZENER || d.model == MMSP_GPU_SPARSE_GG)
+                ? d.dt : d.dt * d.mobility;
     if (noisy(d)) {
         c.noise = d.aux[0];
         c.seed = (unsigned long long)d.aux[1];

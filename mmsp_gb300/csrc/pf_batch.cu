@@ -216,4 +216,159 @@ cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchIns
     return cudaLaunchKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
 }
 
+
+// ---------------------------------------------------------------------------
+// Temporal blocking: KS steps per launch on shared-memory tiles.
+//
+// A work item is a tile of one FP32 instance: an interior of tx x tz cells
+// whose region, widened by a halo of H = 2*KS cells on every side (the
+// Cahn-Hilliard step reads two cells deep: mu of the neighbours), is loaded
+// once into shared memory with periodic wraps.  Each of the KS steps then
+// computes mu on the region minus one more ring and the update on the region
+// minus two, in place, so after KS steps the interior holds the state KS
+// steps later and goes back to HBM.  HBM traffic per step falls by about KS
+// times; the price is the halo work, which the autotuner weighs against it.
+//
+// The region is RI x CI floats (compile-time); a block of 256 threads sees it
+// as CI columns x (256 / CI) row groups, each thread walking a run of rows
+// of one column with the rows above and below in registers, so a cell-step
+// costs 3 shared loads and 1 store per pass.  Per cell the arithmetic is
+// the batched kernel's FP32 form.
+template <int MODEL>
+static __device__ __forceinline__ float tb_mu(float c, float lap, float kappa, float neg_r, float u)
+{
+    const float fp = MODEL == MMSP_GPU_CH ? c * fmaf(fmaf(4.0f, c, -6.0f), c, 2.0f) : c * fmaf(u, c * c, neg_r);
+    return fmaf(-kappa, lap, fp);
+}
+
+template <bool UNIT>
+static __device__ __forceinline__ float tb_lap(float y, float up, float dn, float l, float r, float w0, float w1)
+{
+    if (UNIT) return fmaf(-4.0f, y, (dn + up) + (r + l));
+    return fmaf(w0, dn + up, fmaf(w1, r + l, -2.0f * (w0 + w1) * y));
+}
+
+template <int RI, int CI, int KS, int MODEL, bool UNIT>
+__global__ void __launch_bounds__(256)
+ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ items, int nitems,
+              const float* __restrict__ in, float* __restrict__ out, int* __restrict__ counters, int parity)
+{
+    constexpr int H = 2 * KS;
+    constexpr int RG = 256 / CI;
+    static_assert(CI % 32 == 0 && 256 % CI == 0 && RI > 2 * H && CI > 2 * H, "tile shape");
+    extern __shared__ __align__(16) float tb_sm[];
+    float* C = tb_sm;              // c, updated in place
+    float* M = tb_sm + RI * CI;    // mu
+    __shared__ int s_item;
+    const int t = threadIdx.x;
+    const int col = t % CI, rg = t / CI;
+    if (blockIdx.x == 0 && t == 0) counters[parity ^ 1] = 0;   // for the next launch
+    while (true) {
+        if (t == 0) s_item = atomicAdd(&counters[parity], 1);
+        __syncthreads();
+        const int k = s_item;
+        if (k >= nitems) break;
+        const TbItem it = items[k];
+        const BatchInst bi = insts[it.inst];
+        const int rows = it.tx + 2 * H, cols = it.tz + 2 * H;
+        const float kappa = (float)bi.kappa, dtm = (float)bi.dtm, neg_r = (float)bi.neg_r, u = (float)bi.u;
+        const float w0 = (float)bi.w0, w1 = (float)bi.w1;
+        const float* src = in + bi.off;
+        // the region with periodic wraps (rows of axis 0, columns of axis 1)
+        if (col < cols) {
+            const int gz = wrapi(it.z0 - H + col, bi.n1);
+            for (int r = rg; r < rows; r += RG)
+                C[r * CI + col] = __ldg(src + (long long)wrapi(it.x0 - H + r, bi.n0) * bi.n1 + gz);
+        }
+        __syncthreads();
+        for (int j = 0; j < KS; j++) {
+            // mu on rows [2j+1, rows-2j-1) x cols [2j+1, cols-2j-1)
+            {
+                const int a = 2 * j + 1, b = rows - 2 * j - 1;
+                const int h = (b - a + RG - 1) / RG;
+                const int r0 = a + rg * h, r1 = min(b, r0 + h);
+                if (col >= a && col < cols - 2 * j - 1 && r0 < r1) {
+                    float up = C[(r0 - 1) * CI + col], cc = C[r0 * CI + col];
+                    for (int r = r0; r < r1; r++) {
+                        const float dn = C[(r + 1) * CI + col];
+                        const float lap = tb_lap<UNIT>(cc, up, dn, C[r * CI + col - 1], C[r * CI + col + 1], w0, w1);
+                        M[r * CI + col] = tb_mu<MODEL>(cc, lap, kappa, neg_r, u);
+                        up = cc;
+                        cc = dn;
+                    }
+                }
+            }
+            __syncthreads();
+            // c' = c + dt*M*lap(mu) on rows [2j+2, rows-2j-2) x cols [2j+2, cols-2j-2), in place
+            {
+                const int a = 2 * j + 2, b = rows - 2 * j - 2;
+                const int h = (b - a + RG - 1) / RG;
+                const int r0 = a + rg * h, r1 = min(b, r0 + h);
+                if (col >= a && col < cols - 2 * j - 2 && r0 < r1) {
+                    float up = M[(r0 - 1) * CI + col], mm = M[r0 * CI + col];
+                    for (int r = r0; r < r1; r++) {
+                        const float dn = M[(r + 1) * CI + col];
+                        const float lap = tb_lap<UNIT>(mm, up, dn, M[r * CI + col - 1], M[r * CI + col + 1], w0, w1);
+                        C[r * CI + col] = fmaf(dtm, lap, C[r * CI + col]);
+                        up = mm;
+                        mm = dn;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // the interior back to HBM
+        if (col >= H && col < H + it.tz) {
+            float* dst = out + bi.off + (it.z0 - H + col);
+            for (int r = H + rg; r < H + it.tx; r += RG) dst[(long long)(it.x0 - H + r) * bi.n1] = C[r * CI + col];
+        }
+        __syncthreads();   // the region is reloaded by the next item
+    }
+}
+
+namespace {
+template <int RI, int CI, int KS, int MODEL>
+const void* tb_unit(bool unit)
+{
+    return unit ? (const void*)&ch2_tb_kernel<RI, CI, KS, MODEL, true> : (const void*)&ch2_tb_kernel<RI, CI, KS, MODEL, false>;
+}
+template <int RI, int CI, int KS>
+const void* tb_model(int model, bool unit)
+{
+    return model == MMSP_GPU_CH ? tb_unit<RI, CI, KS, MMSP_GPU_CH>(unit) : tb_unit<RI, CI, KS, MMSP_GPU_CH_POLY>(unit);
+}
+template <int RI, int CI>
+const void* tb_depth(int ks, int model, bool unit)
+{
+    switch (ks) {
+    case 2: return tb_model<RI, CI, 2>(model, unit);
+    case 4: return tb_model<RI, CI, 4>(model, unit);
+    case 8: return tb_model<RI, CI, 8>(model, unit);
+    default: return nullptr;
+    }
+}
+}  // namespace
+
+const TbShape kTbShapes[kTbShapeCount] = {{64, 128}, {96, 128}, {128, 64}};
+
+const void* tb_kernel(int shape, int ks, int model, bool unit)
+{
+    switch (shape) {
+    case 0: return tb_depth<64, 128>(ks, model, unit);
+    case 1: return tb_depth<96, 128>(ks, model, unit);
+    case 2: return tb_depth<128, 64>(ks, model, unit);
+    default: return nullptr;
+    }
+}
+
+size_t tb_smem(int shape) { return sizeof(float) * 2 * (size_t)kTbShapes[shape].ri * kTbShapes[shape].ci; }
+
+cudaError_t launch_tb(const void* fn, int blocks, size_t smem, const BatchInst* insts, const TbItem* items, int nitems,
+                      const void* in, void* out, int* counters, int parity, cudaStream_t s)
+{
+    void* args[] = {(void*)&insts, (void*)&items, (void*)&nitems, (void*)&in, (void*)&out, (void*)&counters,
+                    (void*)&parity};
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, smem, s);
+}
+
 }  // namespace pf

@@ -31,6 +31,26 @@ inline bool batch_eligible(const mmsp_gpu_desc& d)
     return d.n[1] % 32 == 0 && d.n[1] >= 32 && d.n[1] <= kBatchMaxRow && d.n[0] >= 1;
 }
 
+// A tile of one instance for the temporally blocked kernel: interior rows
+// [x0, x0+tx) and columns [z0, z0+tz).
+struct TbItem {
+    int inst, x0, z0, tx, tz;
+};
+
+// Region shapes (rows x columns, halo included) of the temporally blocked
+// kernel, and the depths (steps per launch) it is built for.
+struct TbShape {
+    int ri, ci;
+};
+constexpr int kTbShapeCount = 3;
+extern const TbShape kTbShapes[kTbShapeCount];
+constexpr int kTbDepths[] = {2, 4, 8};
+
+const void* tb_kernel(int shape, int ks, int model, bool unit);   // FP32 only
+size_t tb_smem(int shape);
+cudaError_t launch_tb(const void* fn, int blocks, size_t smem, const BatchInst* insts, const TbItem* items, int nitems,
+                      const void* in, void* out, int* counters, int parity, cudaStream_t s);
+
 const void* batch_kernel(int dtype, int model, bool unit);
 cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchInst* insts, const BatchItem* items,
                          int nitems, const void* in, void* out, int* counters, int parity, cudaStream_t s);

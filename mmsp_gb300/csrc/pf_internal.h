@@ -140,6 +140,21 @@ cudaError_t launch_convex_sweeps(const mmsp_gpu_desc& d, const Geom& g, const Co
 cudaError_t launch_convex_residual(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* old,
                                    const void* nw, double* partials, cudaStream_t s);
 
+// Sparse phase-field grain growth (pf_sparse.cu).  A state buffer holds
+// count[cells] int32 at 0, index[K][cells] int32 at idx_off and
+// value[K][cells] double at val_off (slot-major); a transfer staging buffer
+// has the same offsets with the host's cell-major [cells][K] slots.
+struct SparseLayout {
+    size_t idx_off, val_off, bytes;
+};
+SparseLayout sparse_layout(long long cells, int K);
+// One step in -> out (out holds the state of two steps back, or empty
+// lists); a list that outgrows K sets err[1].
+cudaError_t launch_sparse_gg(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* in, void* out,
+                             int* err, cudaStream_t s);
+cudaError_t launch_sparse_pack(const void* staging, void* state, long long cells, int K, cudaStream_t s);
+cudaError_t launch_sparse_unpack(const void* state, void* staging, long long cells, int K, cudaStream_t s);
+
 // Reductions: partial sums of (mass, energy) per block into `partials`
 // (4 doubles per block: mass sum, mass compensation, energy sum, energy
 // compensation), then a single-block pass into result[0..1] (mass, energy).

@@ -168,3 +168,36 @@ def convex_start(shape, seed=None, C0: float = 0.45, K: float = 2.0, Ca: float =
     out[..., 0] = c
     out[..., 1] = dfdc - K * lap
     return out
+
+
+def sparse_grains(shape, points: int, seed: int, capacity: int):
+    """A sparse grain start state (grid<dim,sparse<double>>): each cell holds one
+    item (its periodic Voronoi grain index, 1.0), as the sparsePF example's
+    cells start with one set() each (sparsePF/graingrowth.cpp:14-56).
+    Returns (count, index, value) with `capacity` slots per cell."""
+    shape = tuple(int(s) for s in shape)
+    e = voronoi_grains(shape, points, points, seed)
+    cnt = np.ones(shape, np.int32)
+    idx = np.zeros(shape + (capacity,), np.int32)
+    val = np.zeros(shape + (capacity,), np.float64)
+    idx[..., 0] = np.argmax(e, axis=-1)
+    val[..., 0] = 1.0
+    return cnt, idx, val
+
+
+def sparse_circles(shape, capacity: int):
+    """The sparsePF example's own start state (sparsePF/graingrowth.cpp:14-56):
+    index 1 where the distance r < 16 (2D/3D: r from (32, 32) on a period-64
+    lattice of the first two axes; 1D: r = 32 - x), index 0 elsewhere, value 1.0."""
+    shape = tuple(int(s) for s in shape)
+    x = np.indices(shape)
+    if len(shape) == 1:
+        r = 32.0 - x[0]
+    else:
+        r = np.sqrt((32 - x[0] % 64) ** 2.0 + (32 - x[1] % 64) ** 2.0)
+    cnt = np.ones(shape, np.int32)
+    idx = np.zeros(shape + (capacity,), np.int32)
+    val = np.zeros(shape + (capacity,), np.float64)
+    idx[..., 0] = (r < 16.0).astype(np.int32)
+    val[..., 0] = 1.0
+    return cnt, idx, val

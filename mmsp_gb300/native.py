@@ -13,19 +13,20 @@ import numpy as np
 
 from . import build as _build
 
-OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED, ESTOPPED, EIO, ENOCONV = \
-    0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10, -11
+OK, EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, ETIMEDOUT, ENODEV, ENOTFOUND, ECANCELED, ESTOPPED, EIO, ENOCONV, \
+    EOVERFLOW = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10, -11, -12
 BC_MIRROR, BC_NEUMANN, BC_PERIODIC, BC_PARALLEL, BC_DIRICHLET = 0, 1, 2, 3, 4
 F64, F32 = 0, 1
 FLAG_CONTRACT = 1   # MMSP_GPU_FLAG_CONTRACT
-CH, CH_POLY, AC, GG, AC_POLY, ZENER, OSTWALD, CH_CONVEX = 0, 1, 2, 3, 4, 5, 6, 7
+CH, CH_POLY, AC, GG, AC_POLY, ZENER, OSTWALD, CH_CONVEX, SPARSE_GG = 0, 1, 2, 3, 4, 5, 6, 7, 8
 CELL_MAJOR, FIELD_MAJOR = 0, 1
 
 MODELS = {"ch": CH, "ch_poly": CH_POLY, "ac": AC, "gg": GG, "ac_poly": AC_POLY, "zener": ZENER,
-          "ostwald": OSTWALD, "ch_convex": CH_CONVEX}
+          "ostwald": OSTWALD, "ch_convex": CH_CONVEX, "sparse_gg": SPARSE_GG}
 OSTWALD_AUX = ("D", "Calpha", "Cbeta", "A", "delta", "epsilon")   # mmsp_gpu_desc.aux of MMSP_GPU_OSTWALD
 NOISE_AUX = ("noise", "seed")   # mmsp_gpu_desc.aux of MMSP_GPU_CH_POLY / MMSP_GPU_AC_POLY
 CONVEX_AUX = ("C0", "Ca", "Cb", "A", "omega", "tolerance")   # mmsp_gpu_desc.aux of MMSP_GPU_CH_CONVEX
+SPARSE_AUX = ("epsilon",)   # mmsp_gpu_desc.aux of MMSP_GPU_SPARSE_GG
 DTYPES = {np.dtype(np.float64): F64, np.dtype(np.float32): F32}
 
 # Every symbol include/MMSP.gpu.h declares (checked by the CPU test suite).
@@ -35,6 +36,7 @@ EXPORTS = [
     "mmsp_gpu_upload", "mmsp_gpu_download", "mmsp_gpu_upload_device", "mmsp_gpu_download_device",
     "mmsp_gpu_step", "mmsp_gpu_synchronize", "mmsp_gpu_reduce", "mmsp_gpu_state",
     "mmsp_gpu_last_error", "mmsp_gpu_update", "mmsp_gpu_step_noalloc", "mmsp_gpu_fp64_rate",
+    "mmsp_gpu_sparse_upload", "mmsp_gpu_sparse_download",
     "mmsp_gpu_output_opts_init", "mmsp_gpu_write_grid", "mmsp_gpu_output", "mmsp_gpu_output_wait",
     "mmsp_gpu_batch_create", "mmsp_gpu_batch_destroy", "mmsp_gpu_batch_set_stream", "mmsp_gpu_batch_upload",
     "mmsp_gpu_batch_download", "mmsp_gpu_batch_step", "mmsp_gpu_batch_synchronize", "mmsp_gpu_batch_reduce",
@@ -68,7 +70,8 @@ class BatchInfo(ctypes.Structure):
     _fields_ = [("instances", ctypes.c_int), ("persistent", ctypes.c_int), ("fallback", ctypes.c_int),
                 ("rows_per_item", ctypes.c_int), ("threads_per_block", ctypes.c_int), ("blocks", ctypes.c_int),
                 ("items", ctypes.c_int), ("tuned_from_cache", ctypes.c_int), ("tune_ms", ctypes.c_double),
-                ("device_bytes", ctypes.c_size_t)]
+                ("device_bytes", ctypes.c_size_t), ("temporal_depth", ctypes.c_int), ("tile_rows", ctypes.c_int),
+                ("tile_cols", ctypes.c_int), ("tiles", ctypes.c_int)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -135,6 +138,8 @@ def load(build_if_missing: bool = False):
         "mmsp_gpu_update": (i, [dp, vp, sz, i, i, ctypes.POINTER(Stats)]),
         "mmsp_gpu_step_noalloc": (i, [dp, vp, vp, i, vp]),
         "mmsp_gpu_fp64_rate": (i, [vp, vp]),
+        "mmsp_gpu_sparse_upload": (i, [vp, vp, vp, vp]),
+        "mmsp_gpu_sparse_download": (i, [vp, vp, vp, vp]),
         "mmsp_gpu_output_opts_init": (i, [ctypes.POINTER(OutputOpts)]),
         "mmsp_gpu_write_grid": (i, [ctypes.c_char_p, dp, vp, sz, i, ctypes.POINTER(OutputOpts)]),
         "mmsp_gpu_output": (i, [vp, ctypes.c_char_p, ctypes.POINTER(OutputOpts)]),
@@ -200,7 +205,8 @@ def make_desc(shape, fields=1, dtype=np.float64, model="ch", dx=None, bc=None, d
     for name, v in (("dt", dt), ("kappa", kappa), ("mobility", mobility), ("gamma", gamma), ("r", r), ("u", u)):
         if v is not None:
             setattr(d, name, float(v))
-    names = OSTWALD_AUX if m == OSTWALD else CONVEX_AUX if m == CH_CONVEX else NOISE_AUX
+    names = OSTWALD_AUX if m == OSTWALD else CONVEX_AUX if m == CH_CONVEX else SPARSE_AUX if m == SPARSE_GG \
+        else NOISE_AUX
     for name, v in aux.items():
         if name not in names:
             raise TypeError("unknown model parameter %r" % name)
@@ -292,6 +298,28 @@ class Stepper:
 
     def output_wait(self):
         _check(self.L.mmsp_gpu_output_wait(self.h), self.h, "output_wait")
+
+    def sparse_upload(self, count, index, value):
+        """A sparse grid's lists (mmsp_gpu_sparse_upload): count has the grid's
+        shape, index and value shape + (K,) with K = desc.fields."""
+        K = self.fields
+        c = np.ascontiguousarray(count, dtype=np.int32)
+        ix = np.ascontiguousarray(index, dtype=np.int32)
+        v = np.ascontiguousarray(value, dtype=np.float64)
+        if c.shape != self.shape or ix.shape != self.shape + (K,) or v.shape != ix.shape:
+            raise ValueError("sparse arrays of shape %s / %s, grid %s with %d slots" % (c.shape, ix.shape, self.shape, K))
+        _check(self.L.mmsp_gpu_sparse_upload(self.h, c.ctypes.data, ix.ctypes.data, v.ctypes.data), self.h,
+               "sparse_upload")
+
+    def sparse_download(self):
+        """(count, index, value) of a sparse grid (mmsp_gpu_sparse_download)."""
+        K = self.fields
+        c = np.empty(self.shape, np.int32)
+        ix = np.empty(self.shape + (K,), np.int32)
+        v = np.empty(self.shape + (K,), np.float64)
+        _check(self.L.mmsp_gpu_sparse_download(self.h, c.ctypes.data, ix.ctypes.data, v.ctypes.data), self.h,
+               "sparse_download")
+        return c, ix, v
 
     def upload_device(self, ptr: int, nbytes: int, layout: int = FIELD_MAJOR):
         _check(self.L.mmsp_gpu_upload_device(self.h, ctypes.c_void_p(ptr), nbytes, layout), self.h, "upload_device")

@@ -604,3 +604,146 @@ void pfo_pow3(const double* x, double* y, long n)
 {
     for (long i = 0; i < n; i++) y[i] = pow(x[i], 3);
 }
+
+/* ---- isotropic sparse phase-field grain growth ------------------------------------------------
+ * examples/coarsening/grain_growth/isotropic/sparsePF/graingrowth.cpp:58-120 over
+ * grid<dim,sparse<double>> (include/MMSP.sparse.h:19, MMSP.sparse.cpp).  A cell is a list of
+ * (index, value) items in insertion order; set() overwrites an item or appends one
+ * (MMSP.sparse.cpp set), operator[] reads 0 for an absent index.  Here a list lives in K slots:
+ * cnt[c] items, idx[c*K + h], val[c*K + h].
+ *
+ * The sparse Laplacian (include/MMSP.grid.cpp:2110-2128) combines the items of yh, 2.0*y and yl
+ * through sparse operator+/- (MMSP.sparse.cpp), which start every index at 0 and add or
+ * subtract; each operation is exact where an index is absent, so its value for index i is the
+ * dense expression weight*((yh_i - 2.0*y_i) + yl_i), summed over axes from 0.0, with absent
+ * items read as 0.  Only the sign of an exact zero can differ, and the update below cannot
+ * carry it into a stored value.
+ *
+ * update() builds newGrid by the copy constructor, whose cells start empty, and never clears
+ * it: after swap() the grid written at step s holds the state of step s-2, and set() leaves
+ * the items it does not overwrite.  Those stale items are part of the state (they enter the
+ * neighbour sets, the sum of squares and the Laplacians), so this restatement keeps them too:
+ * buffer B starts empty on every call, as each update() call's newGrid does. */
+static inline int sp_find(const int* cnt, const int* idx, int K, long c, int i)
+{
+    const int n = cnt[c];
+    const int* ix = idx + c * K;
+    for (int h = 0; h < n; h++)
+        if (ix[h] == i) return h;
+    return -1;
+}
+
+static inline double sp_get(const int* cnt, const int* idx, const double* val, int K, long c, int i)
+{
+    const int h = sp_find(cnt, idx, K, c, i);
+    return h < 0 ? 0.0 : val[c * K + h];
+}
+
+#define PFO_SPARSE_SET 256   /* largest neighbour set (union of 2*dim+1 lists) */
+
+int pfo_sparse_gg(const pfo_grid* g, int K, int* cnt, int* idx, double* val, int steps, double dt, double eps,
+                  int threads, int* longest)
+{
+    geo q;
+    if (K < 1 || K > 64 || steps < 0 || !cnt || !idx || !val || geo_init(&q, g) != 0) return -1;
+    const long cells = q.cells;
+    int* bc = (int*)calloc((size_t)cells, sizeof(int));
+    int* bi = (int*)calloc((size_t)cells * K, sizeof(int));
+    double* bv = (double*)calloc((size_t)cells * K, sizeof(double));
+    if (!bc || !bi || !bv) {
+        free(bc); free(bi); free(bv); geo_free(&q);
+        return -1;
+    }
+    int *ac = cnt, *ai = idx, *xc_ = bc, *xi = bi;
+    double *av = val, *xv = bv;
+    int overflow = 0, maxlen = 0;
+    for (long c = 0; c < cells; c++) {
+        if (cnt[c] < 0 || cnt[c] > K) overflow = 1;
+        if (cnt[c] > maxlen) maxlen = cnt[c];
+    }
+    const int off = 3 - q.dim;
+    const int nt = nthreads(threads);
+    for (int step = 0; step < steps && !overflow; step++) {
+        int ovf = 0, mx = 0;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nt) schedule(static) reduction(| : ovf) reduction(max : mx)
+#endif
+        for (long c = 0; c < cells; c++) {
+            int xc[3];
+            xc[0] = (int)(c / q.st[0]);
+            xc[1] = (int)((c / q.st[1]) % q.n[1]);
+            xc[2] = (int)(c % q.n[2]);
+            /* nonzero fields of the neighbourhood, in the example's visiting order:
+             * per axis the low neighbour, the cell itself, the high neighbour */
+            int S[PFO_SPARSE_SET];
+            int ns = 0;
+            for (int ra = 0; ra < q.dim; ra++) {
+                const int a = off + ra;
+                for (int k = -1; k <= 1; k++) {
+                    const long nc = k < 0 ? c + NB_LO(&q, a, xc[a]) : k > 0 ? c + NB_HI(&q, a, xc[a]) : c;
+                    for (int h = 0; h < ac[nc]; h++) {
+                        const int i = ai[nc * K + h];
+                        int seen = 0;
+                        for (int s = 0; s < ns; s++)
+                            if (S[s] == i) { seen = 1; break; }
+                        if (!seen) {
+                            if (ns == PFO_SPARSE_SET) { ovf = 1; break; }
+                            S[ns++] = i;
+                        }
+                    }
+                }
+            }
+            if (ns < 2) {
+                /* newGrid(n) = oldGrid(n): the whole list */
+                xc_[c] = ac[c];
+                for (int h = 0; h < ac[c]; h++) {
+                    xi[c * K + h] = ai[c * K + h];
+                    xv[c * K + h] = av[c * K + h];
+                }
+            } else {
+                double sum = 0.0;
+                for (int h = 0; h < ac[c]; h++) {
+                    const double phi = av[c * K + h];
+                    sum += phi * phi;
+                }
+                for (int s = 0; s < ns; s++) {
+                    const int i = S[s];
+                    const double phi = sp_get(ac, ai, av, K, c, i);
+                    double lap = 0.0;
+                    for (int ra = 0; ra < q.dim; ra++) {
+                        const int a = off + ra;
+                        const double yh = sp_get(ac, ai, av, K, c + NB_HI(&q, a, xc[a]), i);
+                        const double yl = sp_get(ac, ai, av, K, c + NB_LO(&q, a, xc[a]), i);
+                        lap += q.w[ra] * (yh - 2.0 * phi + yl);
+                    }
+                    const double value = phi - dt * (-phi - pow(phi, 3) + 2.0 * (phi * sum - lap));
+                    if (value > eps) {
+                        int h = sp_find(xc_, xi, K, c, i);
+                        if (h < 0) {
+                            if (xc_[c] == K) { ovf = 1; continue; }
+                            h = xc_[c]++;
+                            xi[c * K + h] = i;
+                        }
+                        xv[c * K + h] = value;
+                    }
+                }
+            }
+            if (xc_[c] > mx) mx = xc_[c];
+        }
+        overflow |= ovf;
+        if (mx > maxlen) maxlen = mx;
+        /* swap(oldGrid, newGrid) */
+        int* t = ac; ac = xc_; xc_ = t;
+        t = ai; ai = xi; xi = t;
+        double* tv = av; av = xv; xv = tv;
+    }
+    if (ac != cnt) {
+        memcpy(cnt, ac, sizeof(int) * (size_t)cells);
+        memcpy(idx, ai, sizeof(int) * (size_t)cells * K);
+        memcpy(val, av, sizeof(double) * (size_t)cells * K);
+    }
+    free(bc); free(bi); free(bv);
+    geo_free(&q);
+    if (longest) *longest = maxlen;
+    return overflow ? -3 : 0;
+}

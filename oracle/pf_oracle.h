@@ -132,6 +132,16 @@ int pfo_ch_mass_energy(const pfo_grid* g, const double* c, double kappa,
 int pfo_ac_mass_energy(const pfo_grid* g, int N, const double* eta,
                        double gamma, double kappa, double* mass, double* energy);
 
+/* Isotropic sparse phase-field grain growth exactly as shipped
+ * (examples/coarsening/grain_growth/isotropic/sparsePF/graingrowth.cpp:58-120) on
+ * grid<dim,sparse<double>> (include/MMSP.sparse.h:19): per cell a list of (index, value)
+ * items in insertion order, in K slots: cnt[c] items at idx[c*K + h], val[c*K + h].  One call
+ * is one update() call: its newGrid starts with empty cells and keeps the stale items of two
+ * steps back, as the example's does.  *longest gets the longest list seen.  Returns -3 when
+ * a list would exceed K items. */
+int pfo_sparse_gg(const pfo_grid* g, int K, int* cnt, int* idx, double* val, int steps, double dt, double eps,
+                  int threads, int* longest);
+
 /* pow(x,3) through the C library, for checking a device cube routine. */
 void pfo_pow3(const double* x, double* y, long n);
 

@@ -54,6 +54,9 @@ def lib():
              + [ctypes.c_uint64, ctypes.c_longlong, ctypes.c_int]),
             ("pfo_ac_scalar_shipped", [gp, dp, ctypes.c_int] + [ctypes.c_double] * 5 + [ctypes.c_int]),
             ("pfo_laplacian", [gp, dp, dp]),
+            ("pfo_sparse_gg", [gp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), dp,
+                               ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                               ctypes.POINTER(ctypes.c_int)]),
             ("pfo_ch_mass_energy", [gp, dp, ctypes.c_double, dp, dp]),
             ("pfo_ac_mass_energy", [gp, ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, dp, dp]),
         ]:
@@ -228,3 +231,24 @@ def pow3(x):
 
 def ref_available() -> bool:
     return os.path.exists(REF_BIN)
+
+
+def sparse_gg(cnt, idx, val, steps, dt=0.01, eps=1e-8, dx=None, bc=None, threads=0):
+    """Sparse phase-field grain growth (pfo_sparse_gg): one update() call of
+    the sparsePF example.  cnt has the grid's shape (items per cell); idx and
+    val have shape + (K,), the first cnt items of each cell in stored order.
+    Returns (cnt, idx, val, longest list seen)."""
+    cnt = np.array(cnt, dtype=np.int32, order="C", copy=True)
+    K = int(np.asarray(idx).shape[-1])
+    idx = np.array(idx, dtype=np.int32, order="C", copy=True)
+    val = np.array(val, dtype=np.float64, order="C", copy=True)
+    assert idx.shape == cnt.shape + (K,) and val.shape == idx.shape
+    g = _grid(cnt.shape, dx, bc)
+    longest = ctypes.c_int(0)
+    ip = ctypes.POINTER(ctypes.c_int)
+    rc = lib().pfo_sparse_gg(ctypes.byref(g), K, cnt.ctypes.data_as(ip), idx.ctypes.data_as(ip), _ptr(val),
+                             int(steps), float(dt), float(eps), int(threads), ctypes.byref(longest))
+    if rc == -3:
+        raise OverflowError("a sparse cell list exceeded %d items" % K)
+    _check(rc, "sparse_gg")
+    return cnt, idx, val, longest.value

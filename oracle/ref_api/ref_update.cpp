@@ -11,6 +11,7 @@
 //   examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:103-143
 //   examples/coarsening/ostwald_ripening/isotropic/phase_field/ostwald.cpp:56-123
 //   examples/phase_transitions/cahn-hilliard/convex_splitting/cahn-hilliard.cpp:273-463
+//   examples/coarsening/grain_growth/isotropic/sparsePF/graingrowth.cpp:58-120
 // The "shipped" models are those loops with the examples' own expressions;
 // the "baseline" models substitute f(c)=c^2(1-c)^2 for Cahn-Hilliard and
 // f = sum(-e^2/2+e^4/4) + gamma*sum_{i<j} e_i^2 e_j^2 for grain growth, with
@@ -25,6 +26,7 @@
 //   ostwald          dt L D Calpha Cbeta A delta epsilon kappa
 //   ch_convex        dt D K C0 Ca Cb A omega tolerance   (prints "iterations <n>" of the last step)
 //   ac_scalar        r u K M dt
+//   sparsepf         dt epsilon   (IN/OUT are sparse list files, see run_sparse)
 // Prints "update_seconds <t>" (std::chrono around update() only).
 #include "MMSP.hpp"
 
@@ -301,7 +303,113 @@ template <int dim> void convex_update(grid<dim, vector<double> >& oldGrid, int s
 	std::printf("iterations %u\n", iter);
 }
 
+// examples/coarsening/grain_growth/isotropic/sparsePF/graingrowth.cpp:58-120 with dt and
+// epsilon from the command line, on the reference's grid<dim,sparse<double> >.
+template <int dim> void sparse_update(grid<dim, sparse<double> >& oldGrid, int steps,
+                                      const std::vector<double>& p)
+{
+	ghostswap(oldGrid);
+	grid<dim, sparse<double> > newGrid(oldGrid);
+	const double dt = p[0];
+	const double epsilon = p[1];
+	for (int step = 0; step < steps; step++) {
+		for (int n = 0; n < nodes(oldGrid); n++) {
+			vector<int> x = position(oldGrid, n);
+			sparse<bool> neighbors;
+			for (int j = 0; j < dim; j++)
+				for (int k = -1; k <= 1; k++) {
+					x[j] += k;
+					for (int h = 0; h < length(oldGrid(x)); h++) {
+						int i = index(oldGrid(x), h);
+						set(neighbors, i) = 1;
+					}
+					x[j] -= k;
+				}
+			if (length(neighbors) < 2)
+				newGrid(n) = oldGrid(n);
+			else {
+				sparse<double> lap = laplacian(oldGrid, n);
+				double sum = 0.0;
+				for (int j = 0; j < length(oldGrid(n)); j++) {
+					double phi = value(oldGrid(n), j);
+					sum += phi * phi;
+				}
+				for (int j = 0; j < length(neighbors); j++) {
+					int i = index(neighbors, j);
+					double phi = oldGrid(n)[i];
+					double v = phi - dt * (-phi - pow(phi, 3) + 2.0 * (phi * sum - lap[i]));
+					if (v > epsilon) set(newGrid(n), i) = v;
+				}
+			}
+		}
+		swap(oldGrid, newGrid);
+		ghostswap(oldGrid);
+	}
+}
+
 } // namespace MMSP
+
+// Sparse grids travel as a plain binary list file (not the MMSP grid format, whose item
+// padding bytes are uninitialised): int32 dim, int32 n[dim], then per cell in node order
+// int32 count and count x (int32 index, float64 value).
+template <int dim> MMSP::grid<dim, MMSP::sparse<double> >* make_sparse_grid(const int* n);
+template <> MMSP::grid<1, MMSP::sparse<double> >* make_sparse_grid<1>(const int* n)
+{
+	return new MMSP::grid<1, MMSP::sparse<double> >(0, 0, n[0]);
+}
+template <> MMSP::grid<2, MMSP::sparse<double> >* make_sparse_grid<2>(const int* n)
+{
+	return new MMSP::grid<2, MMSP::sparse<double> >(0, 0, n[0], 0, n[1]);
+}
+template <> MMSP::grid<3, MMSP::sparse<double> >* make_sparse_grid<3>(const int* n)
+{
+	return new MMSP::grid<3, MMSP::sparse<double> >(0, 0, n[0], 0, n[1], 0, n[2]);
+}
+
+static double now_s();
+
+template <int dim> int run_sparse(std::ifstream& in, const char* out, int steps, const std::vector<double>& p)
+{
+	int n[3] = {1, 1, 1};
+	in.read(reinterpret_cast<char*>(n), sizeof(int) * dim);
+	MMSP::grid<dim, MMSP::sparse<double> >* g = make_sparse_grid<dim>(n);
+	for (int i = 0; i < MMSP::nodes(*g); i++) {
+		int count = 0;
+		in.read(reinterpret_cast<char*>(&count), sizeof(int));
+		for (int h = 0; h < count; h++) {
+			int index = 0;
+			double v = 0.0;
+			in.read(reinterpret_cast<char*>(&index), sizeof(int));
+			in.read(reinterpret_cast<char*>(&v), sizeof(double));
+			MMSP::set((*g)(i), index) = v;
+		}
+	}
+	if (!in) {
+		delete g;
+		return 4;
+	}
+	double t0 = now_s();
+	MMSP::sparse_update(*g, steps, p);
+	double t1 = now_s();
+	std::printf("update_seconds %.9f\n", t1 - t0);
+	std::ofstream o(out, std::ios::binary);
+	int d = dim;
+	o.write(reinterpret_cast<const char*>(&d), sizeof(int));
+	o.write(reinterpret_cast<const char*>(n), sizeof(int) * dim);
+	for (int i = 0; i < MMSP::nodes(*g); i++) {
+		const MMSP::sparse<double>& s = (*g)(i);
+		int count = MMSP::length(s);
+		o.write(reinterpret_cast<const char*>(&count), sizeof(int));
+		for (int h = 0; h < count; h++) {
+			int index = MMSP::index(s, h);
+			double v = MMSP::value(s, h);
+			o.write(reinterpret_cast<const char*>(&index), sizeof(int));
+			o.write(reinterpret_cast<const char*>(&v), sizeof(double));
+		}
+	}
+	delete g;
+	return o ? 0 : 4;
+}
 
 static double now_s()
 {
@@ -353,10 +461,19 @@ int main(int argc, char* argv[])
 	for (int i = 5; i < argc; i++) p.push_back(std::atof(argv[i]));
 	size_t need = (model == "ch_baseline") ? 3 : (model == "ch_shipped" || model == "ac_scalar") ? 5
 	            : (model == "ac_baseline") ? 4 : (model == "graingrowth" || model == "zener") ? 1
-	            : (model == "ostwald" || model == "ch_convex") ? 9 : 0;
+	            : (model == "ostwald" || model == "ch_convex") ? 9 : (model == "sparsepf") ? 2 : 0;
 	if (need == 0 || p.size() != need) {
 		std::cerr << "bad model or parameter count" << std::endl;
 		return 1;
+	}
+	if (model == "sparsepf") {
+		std::ifstream in(argv[2], std::ios::binary);
+		int d = 0;
+		in.read(reinterpret_cast<char*>(&d), sizeof(int));
+		int rc = d == 1 ? run_sparse<1>(in, argv[3], steps, p) : d == 2 ? run_sparse<2>(in, argv[3], steps, p)
+		       : d == 3 ? run_sparse<3>(in, argv[3], steps, p) : 2;
+		if (rc) std::cerr << "sparse list file could not be read or written" << std::endl;
+		return rc;
 	}
 	std::ifstream hdr(argv[2]);
 	std::string type;

@@ -5,7 +5,7 @@
 // they exist) or against tests/cpp/mini_grid.hpp.  Raw little-endian values,
 // cell-major, are read from IN and the result is written to OUT.
 //
-// usage: dropin_main ch|ch_f32|gg|ac_f32 IN OUT STEPS n0 n1 n2 [fields]
+// usage: dropin_main ch|ch_f32|gg|gg_f32|sparse IN OUT STEPS n0 n1 n2 [fields]
 #ifdef USE_REFERENCE_GRID
 #include "MMSP.hpp"
 #else
@@ -46,7 +46,50 @@ template <int dim, typename T> void update(grid<dim, vector<T> >& g, int steps)
 {
     MMSP::gpu::update(g, steps, MMSP::gpu::grain_growth_shipped(0.01));
 }
+template <int dim, typename T> void update(grid<dim, sparse<T> >& g, int steps)
+{
+    MMSP::gpu::update(g, steps, MMSP::gpu::sparse_grain_growth_shipped(0.01, 1.0e-8, 32));
+}
 }  // namespace MMSP
+
+// Sparse grids as the plain list file: int32 dim, int32 extents, then per
+// cell int32 count and count x (int32 index, float64 value).
+static int sparse_case(const char* in, const char* out, int steps, int n0, int n1, int n2)
+{
+    MMSP::grid<3, MMSP::sparse<double> > g(0, 0, n0, 0, n1, 0, n2);
+    FILE* p = std::fopen(in, "rb");
+    if (!p) return 2;
+    int hdr[4];
+    bool ok = std::fread(hdr, sizeof(int), 4, p) == 4 && hdr[0] == 3;
+    for (int i = 0; ok && i < nodes(g); i++) {
+        int count = 0;
+        ok = std::fread(&count, sizeof(int), 1, p) == 1;
+        for (int h = 0; ok && h < count; h++) {
+            int index = 0;
+            double v = 0.0;
+            ok = std::fread(&index, sizeof(int), 1, p) == 1 && std::fread(&v, sizeof(double), 1, p) == 1;
+            if (ok) MMSP::set(g(i), index) = v;
+        }
+    }
+    std::fclose(p);
+    if (!ok) return 2;
+    MMSP::update(g, steps);
+    p = std::fopen(out, "wb");
+    if (!p) return 3;
+    std::fwrite(hdr, sizeof(int), 4, p);
+    for (int i = 0; i < nodes(g); i++) {
+        int count = length(g(i));
+        std::fwrite(&count, sizeof(int), 1, p);
+        for (int h = 0; h < count; h++) {
+            int index = MMSP::index(g(i), h);
+            double v = MMSP::value(g(i), h);
+            std::fwrite(&index, sizeof(int), 1, p);
+            std::fwrite(&v, sizeof(double), 1, p);
+        }
+    }
+    std::fclose(p);
+    return 0;
+}
 
 template <typename T> static int scalar_case(const char* in, const char* out, int steps, int n0, int n1, int n2)
 {
@@ -121,5 +164,6 @@ int main(int argc, char* argv[])
     if (mode == "ch_f32") return scalar_case<float>(argv[2], argv[3], steps, n0, n1, n2);
     if (mode == "gg") return vector_case<double>(argv[2], argv[3], steps, n0, n1, n2, N);
     if (mode == "gg_f32") return vector_case<float>(argv[2], argv[3], steps, n0, n1, n2, N);
+    if (mode == "sparse") return sparse_case(argv[2], argv[3], steps, n0, n1, n2);
     return 1;
 }

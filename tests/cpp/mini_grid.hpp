@@ -9,6 +9,7 @@
 #define MINI_GRID_HPP
 #include <cstdarg>
 #include <cstdlib>
+#include <utility>
 #include <vector>
 
 namespace MMSP {
@@ -26,6 +27,28 @@ public:
 private:
     std::vector<T> d;
 };
+
+// the sparse cell of include/MMSP.sparse.h:19: (index, value) items in
+// insertion order; set() overwrites an item or appends one
+template <typename T> class sparse {
+public:
+    T& set(int index)
+    {
+        for (size_t h = 0; h < d.size(); h++)
+            if (d[h].first == index) return d[h].second;
+        d.push_back(std::make_pair(index, T(0)));
+        return d.back().second;
+    }
+    int length() const { return (int)d.size(); }
+    int index(int h) const { return d[h].first; }
+    T value(int h) const { return d[h].second; }
+private:
+    std::vector<std::pair<int, T> > d;
+};
+template <typename T> int length(const sparse<T>& s) { return s.length(); }
+template <typename T> T& set(sparse<T>& s, int index) { return s.set(index); }
+template <typename T> int index(const sparse<T>& s, int h) { return s.index(h); }
+template <typename T> T value(const sparse<T>& s, int h) { return s.value(h); }
 
 template <typename T> inline void resize_cell(T&, int) {}
 template <typename T> inline void resize_cell(vector<T>& v, int n) { v.resize(n); }

@@ -12,6 +12,11 @@ Small fixtures: seeded start states are written as MMSP grid files with
 is read back.  Each ``.npz`` holds the start state, the reference's result,
 the model, its parameters and the step count.
 
+Sparse fixtures (``sparse*.npz``): sparse phase-field grain growth through
+the reference's own ``grid<dim,sparse<double>>``, ``laplacian`` and ``swap``
+(ref_update's sparsepf mode, fed a plain list file); the C oracle is checked
+against each before it is saved.
+
 Full-size checksums (``full_size.json``): 2D CH 256x256 x 2000 steps is run
 through the reference itself; the 3D configurations (256^3 CH, 128^3 x 8 AC)
 would take hours through the reference's per-cell allocations, so they are
@@ -104,6 +109,80 @@ def run_ref(model, data, vector, fields, steps, params, dx=None, bc=None, want_s
     return out.data, secs
 
 
+# sparse phase-field grain growth: (name, shape, start, steps); dt 0.01, epsilon 1e-8 as shipped
+SPARSE = [
+    ("sparse2d_grains", (48, 40), ("grains", 12, 3), 150),
+    ("sparse3d_grains", (16, 12, 10), ("grains", 8, 4), 40),
+    ("sparse2d_circles", (128, 64), ("circles",), 200),
+    ("sparse3d_circles", (64, 32, 4), ("circles",), 40),
+]
+SPARSE_CAPACITY = 32
+
+
+def write_sparse(path, cnt, idx, val):
+    """The plain list file ref_update's sparsepf mode reads: int32 dim, int32
+    extents, then per cell int32 count and count x (int32 index, float64 value)."""
+    with open(path, "wb") as f:
+        f.write(np.int32(cnt.ndim).tobytes())
+        f.write(np.asarray(cnt.shape, np.int32).tobytes())
+        c = cnt.ravel()
+        ii = idx.reshape(c.size, -1)
+        vv = val.reshape(c.size, -1)
+        for k in range(c.size):
+            f.write(np.int32(c[k]).tobytes())
+            for h in range(c[k]):
+                f.write(np.int32(ii[k, h]).tobytes())
+                f.write(np.float64(vv[k, h]).tobytes())
+
+
+def read_sparse(path, capacity):
+    b = open(path, "rb").read()
+    dim = int(np.frombuffer(b, np.int32, 1, 0)[0])
+    shape = tuple(int(v) for v in np.frombuffer(b, np.int32, dim, 4))
+    p = 4 + 4 * dim
+    n = int(np.prod(shape))
+    cnt = np.zeros(n, np.int32)
+    idx = np.zeros((n, capacity), np.int32)
+    val = np.zeros((n, capacity), np.float64)
+    item = np.dtype([("i", "<i4"), ("v", "<f8")])
+    for k in range(n):
+        c = int(np.frombuffer(b, np.int32, 1, p)[0])
+        p += 4
+        if c > capacity:
+            raise OverflowError("list of %d items" % c)
+        it = np.frombuffer(b, item, c, p)
+        p += 12 * c
+        cnt[k] = c
+        idx[k, :c] = it["i"]
+        val[k, :c] = it["v"]
+    return cnt.reshape(shape), idx.reshape(shape + (capacity,)), val.reshape(shape + (capacity,))
+
+
+def make_sparse(only=None):
+    """Sparse fixtures: the reference's sparse update (ref_update sparsepf) on
+    grid<dim,sparse<double>>; the C oracle must agree bit for bit."""
+    for name, shape, spec, steps in SPARSE:
+        if only and name not in only:
+            continue
+        if spec[0] == "grains":
+            c0, i0, v0 = inputs.sparse_grains(shape, spec[1], spec[2], SPARSE_CAPACITY)
+        else:
+            c0, i0, v0 = inputs.sparse_circles(shape, SPARSE_CAPACITY)
+        with tempfile.TemporaryDirectory() as td:
+            fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+            write_sparse(fin, c0, i0, v0)
+            res = subprocess.run([pf_oracle.REF_BIN, "sparsepf", fin, fout, str(steps), "0.01", "1e-08"],
+                                 check=True, capture_output=True, text=True)
+            cr, ir, vr = read_sparse(fout, SPARSE_CAPACITY)
+        co, io, vo, longest = pf_oracle.sparse_gg(c0, i0, v0, steps, 0.01, 1e-8)
+        assert np.array_equal(cr, co) and np.array_equal(ir, io) and np.array_equal(vr, vo), name
+        k = max(int(cr.max()), int(c0.max()))   # slots in use
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), model="sparsepf", steps=steps,
+                            params=np.asarray([0.01, 1e-8]), start_count=c0, start_index=i0[..., :k],
+                            start_value=v0[..., :k], count=cr, index=ir[..., :k], value=vr[..., :k])
+        print("%-24s %s steps=%d longest list %d, ref %s" % (name, shape, steps, longest, res.stdout.split()[-1]))
+
+
 def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
 
@@ -189,5 +268,6 @@ if __name__ == "__main__":
     if not pf_oracle.ref_available():
         sys.exit("build the reference program first: make -C oracle ref")
     make_small(set(args.only) if args.only else None)
+    make_sparse(set(args.only) if args.only else None)
     if args.full:
         make_full()

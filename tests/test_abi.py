@@ -166,3 +166,23 @@ def test_noalloc_refuses_misaligned_and_overlapping_pointers(lib):
     assert call(base + 4096, base) == native.EINVAL                    # input overlaps the output's tail
     assert call(base, base + 16, 0) == native.EINVAL                   # a zero-step copy checks too
     assert call(0, base) == native.EINVAL                              # NULL
+
+
+def test_sparse_descriptor_validation(lib):
+    """Sparse grain growth: FP64 only, 1..32 slots per cell, finite epsilon;
+    defaults of the sparsePF example (dt 0.01, epsilon 1e-8)."""
+    from mmsp_gb300 import native
+
+    d = native.make_desc((32, 16), 8, np.float64, "sparse_gg")
+    assert (d.dt, d.aux[0]) == (0.01, 1e-8)
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.OK
+    b = ctypes.c_size_t()
+    assert lib.mmsp_gpu_footprint(ctypes.byref(d), ctypes.byref(b)) == 0
+    assert b.value >= 2 * 32 * 16 * (4 + 8 * 12)
+    d = native.make_desc((32, 16), 8, np.float32, "sparse_gg")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EUNSUPPORTED
+    d = native.make_desc((32, 16), 40, np.float64, "sparse_gg")
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EUNSUPPORTED
+    d = native.make_desc((32, 16), 8, np.float64, "sparse_gg", epsilon=float("inf"))
+    assert lib.mmsp_gpu_validate(ctypes.byref(d)) == native.EINVAL
+    assert lib.mmsp_gpu_strerror(native.EOVERFLOW) == b"sparse cell list outgrew its slots"

@@ -118,3 +118,36 @@ def test_run_loop_writes_the_snapshots_of_main(gpu, oracle, tmp_path):
     g = gridfile.read(str(tmp_path / "gg") + ".30.dat")
     want = oracle.ac_graingrowth(e0, 30, 0.01)
     assert g.vector and g.fields == 2 and np.abs(g.data - want).max() <= 1e-12 * np.abs(want).max()
+
+
+@pytest.mark.gpu
+def test_dropin_sparse_grid_on_device(gpu, oracle, tmp_path):
+    """update(grid<3,sparse<double>>&, steps) through MMSP::gpu::update: the
+    items of every cell, in stored order, as the oracle's sparsePF update."""
+    from mmsp_gb300 import inputs
+
+    exe = build_mini(str(tmp_path))
+    shape, K = (10, 12, 8), 32
+    c0, i0, v0 = inputs.sparse_grains(shape, 7, 12, K)
+    fi, fo = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    with open(fi, "wb") as f:
+        f.write(np.asarray([3] + list(shape), np.int32).tobytes())
+        for c, ii, vv in zip(c0.ravel(), i0.reshape(-1, K), v0.reshape(-1, K)):
+            f.write(np.int32(c).tobytes())
+            for h in range(c):
+                f.write(np.int32(ii[h]).tobytes() + np.float64(vv[h]).tobytes())
+    r = subprocess.run([exe, "sparse", fi, fo, "30"] + [str(s) for s in shape], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    wc, wi, wv, _ = oracle.sparse_gg(c0, i0, v0, 30)
+    b = open(fo, "rb").read()
+    p = 16
+    wi, wv = wi.reshape(-1, K), wv.reshape(-1, K)
+    for k, n in enumerate(wc.ravel()):
+        assert int(np.frombuffer(b, np.int32, 1, p)[0]) == n
+        p += 4
+        for h in range(n):
+            assert int(np.frombuffer(b, np.int32, 1, p)[0]) == wi[k, h]
+            v = float(np.frombuffer(b, np.float64, 1, p + 4)[0])
+            assert abs(v - wv[k, h]) <= 1e-12 * max(1.0, abs(wv[k, h]))
+            p += 12
+    assert p == len(b)

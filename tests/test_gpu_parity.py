@@ -18,7 +18,9 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+FIXTURES = sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(f).startswith("sparse"))
+SPARSE_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "sparse*.npz")))
 TOL_SHIPPED = 1e-12   # relative, forms with pow(x,3)
 TOL_F32 = 1e-5        # absolute, FP32 against FP64 after the stated steps
 

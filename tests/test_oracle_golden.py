@@ -16,7 +16,9 @@ import pytest
 
 from conftest import GOLDEN
 
-FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+FIXTURES = sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(f).startswith("sparse"))
+SPARSE_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "sparse*.npz")))
 
 
 def run_oracle(o, z, x=None, steps=None):
@@ -130,3 +132,44 @@ def test_oracle_random_cases_against_reference_program(oracle, case):
         ref, _ = make_golden.run_ref("ac_baseline", x0, True, 3, 11, (1.5, 2.0, 1.0, 0.05))
         got = oracle.ac_baseline(x0, 11, 1.5, 2.0, 1.0, 0.05)
     assert np.array_equal(ref, got)
+
+
+def sparse_slots(z, capacity):
+    """Start state of a sparse fixture in `capacity` slots per cell."""
+    c0 = z["start_count"]
+    k = z["start_index"].shape[-1]
+    idx = np.zeros(c0.shape + (capacity,), np.int32)
+    val = np.zeros(c0.shape + (capacity,), np.float64)
+    idx[..., :k] = z["start_index"]
+    val[..., :k] = z["start_value"]
+    return c0, idx, val
+
+
+@pytest.mark.parametrize("path", SPARSE_FIXTURES, ids=[os.path.basename(f)[:-4] for f in SPARSE_FIXTURES])
+def test_sparse_oracle_matches_reference_fixture(oracle, path):
+    """Sparse phase-field grain growth: counts, indices (in stored order) and
+    values bit for bit against the reference's grid<dim,sparse<double>>."""
+    z = np.load(path)
+    dt, eps = [float(v) for v in z["params"]]
+    c0, i0, v0 = sparse_slots(z, 16)
+    cnt, idx, val, _ = oracle.sparse_gg(c0, i0, v0, int(z["steps"]), dt, eps)
+    k = z["index"].shape[-1]
+    assert np.array_equal(cnt, z["count"])
+    live = np.arange(k) < cnt[..., None]
+    assert np.array_equal(np.where(live, idx[..., :k], 0), np.where(live, z["index"], 0))
+    assert np.array_equal(np.where(live, val[..., :k], 0.0), np.where(live, z["value"], 0.0))
+
+
+def test_sparse_oracle_overflow_and_threads(oracle):
+    """A list that would outgrow its slots is an error, not a silent drop;
+    threaded runs equal the serial one."""
+    from mmsp_gb300 import inputs
+
+    c0, i0, v0 = inputs.sparse_grains((24, 20), 9, 5, 3)
+    with pytest.raises(OverflowError):
+        oracle.sparse_gg(c0, i0, v0, 60)
+    c0, i0, v0 = inputs.sparse_grains((24, 20), 9, 5, 16)
+    a = oracle.sparse_gg(c0, i0, v0, 30, threads=1)
+    b = oracle.sparse_gg(c0, i0, v0, 30, threads=4)
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
