@@ -296,7 +296,52 @@ def other_models(native, inputs, timed):
                      "cpu_oracle_value_updates_per_s": cpu_rate, "cpu_sample": "2 FP64 steps, 1 thread",
                      "f64_speedup_vs_cpu": vals / (ms64 / 1e3) / cpu_rate}
     out.update(convex_splitting(native, inputs, timed))
+    out.update(sparse_grain_growth(native, inputs))
     return out
+
+
+def sparse_grain_growth(native, inputs):
+    """Sparse phase-field grain growth (the sparsePF example's update, FP64)
+    on a 512^2 grid of 64 periodic Voronoi grains, 16 item slots per cell,
+    200 steps in one call, beside the oracle (the example's loops restated
+    in C, one thread) on 2 steps.  Algorithmic bytes of a step: every
+    cell's list read and the new list written once (int32 count, then
+    int32 index + float64 value per item), at the lists' mean length."""
+    import torch
+
+    from oracle import pf_oracle
+
+    shape, K, steps = (512, 512), 16, 200
+    c0, i0, v0 = inputs.sparse_grains(shape, 64, 21, K)
+    d = native.make_desc(shape, K, np.float64, "sparse_gg")
+    with native.Stepper(d) as s:
+        s.sparse_upload(c0, i0, v0)
+        s.step(8)
+        s.synchronize()
+        s.sparse_upload(c0, i0, v0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        s.step(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        cnt, _, _ = s.sparse_download()
+    cells = int(np.prod(shape))
+    mean_items = 0.5 * (float(c0.mean()) + float(cnt.mean()))
+    alg = cells * 2 * (4 + 12 * mean_items)
+    peak = peaks()[0]
+    t0 = time.perf_counter()
+    pf_oracle.sparse_gg(c0, i0, v0, 2, 0.01, 1e-8, threads=1)
+    cpu_s = (time.perf_counter() - t0) / 2
+    rate = cells * steps / (ms / 1e3)
+    return {"sparse2d_512_g64_200": {"f64_ms": ms, "cell_updates_per_s": rate, "mean_items_per_cell": mean_items,
+                                     "longest_list": int(cnt.max()),
+                                     "roofline": {"bound": "hbm", "alg_bytes_per_step": alg,
+                                                  "achieved_gbs": alg / (ms / 1e3 / steps) / 1e9, "peak": peak,
+                                                  "frac": alg / (ms / 1e3 / steps) / 1e9 / peak},
+                                     "cpu_oracle_cell_updates_per_s": cells / cpu_s, "cpu_sample": "2 steps, 1 thread",
+                                     "speedup_vs_cpu": rate / (cells / cpu_s)}}
 
 
 def convex_splitting(native, inputs, timed):
@@ -772,17 +817,25 @@ def serving(native, n, rate, seed, sequential=True):
     if sequential:
         seq = 0.0
         err = 0.0
+        by_kind = {}
         for (sh, f, m, p, st, _), x, r in zip(reqs, states, results):
             d = native.make_desc(sh, f, np.float64, m, contract=True, **p)
             t0 = time.perf_counter()
             o64, _ = native.update(x.astype(np.float64), st, d)
             seq += time.perf_counter() - t0
-            err = max(err, float(np.abs(o64 - r.astype(np.float64)).max()))
+            e = float(np.abs(o64 - r.astype(np.float64)).max())
+            err = max(err, e)
+            kind = "ac3d" if m == "ac" else "ch%dd" % len(sh)
+            k = by_kind.setdefault(kind, {"requests": 0, "max_err_vs_f64": 0.0, "within_1e-5": 0})
+            k["requests"] += 1
+            k["max_err_vs_f64"] = max(k["max_err_vs_f64"], e)
+            k["within_1e-5"] += int(e <= 1e-5)
         out["sequential_f64"] = {"solves_per_s": n / seq, "seconds": seq,
                                  "how": "the same requests one at a time in FP64 (contracted form) through "
                                         "mmsp_gpu_update: host buffer in, steps, host buffer out"}
         out["speedup_vs_sequential_f64"] = (n / span) / (n / seq)
         out["max_err_vs_f64"] = err
+        out["err_by_kind"] = by_kind
     return out
 
 
@@ -813,6 +866,7 @@ CASES = {
     "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ostwald3d_f32": ((256, 128, 64), 2, np.float32, "ostwald", {}),
     "convex2d_f64": ((400, 200), 2, np.float64, "ch_convex", {}),
+    "sparse2d_f64": ((512, 512), 16, np.float64, "sparse_gg", {}),
 }
 
 
@@ -834,6 +888,14 @@ def run_case(name: str, steps: int):
         print("case batch_f32: %d steps, rows/item %d, threads %d" % (steps, inf.rows_per_item, inf.threads_per_block))
         return 0
     shape, fields, dtype, model, params = CASES[name]
+    if model == "sparse_gg":
+        d = native.make_desc(shape, fields, dtype, model, **params)
+        with native.Stepper(d) as s:
+            s.sparse_upload(*inputs.sparse_grains(shape, 64, 21, fields))
+            s.step(steps)
+            cnt, _, _ = s.sparse_download()
+        print("case %s: %d steps, mean items %.3f" % (name, steps, float(cnt.mean())))
+        return 0
     if fields == 1:
         x = inputs.noisy_composition(shape, MEAN, AMP, SEED)
     elif model == "ostwald":

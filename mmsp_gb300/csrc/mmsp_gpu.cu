@@ -224,12 +224,70 @@ static void release(mmsp_gpu_handle* h)
     if (h->cs_host) cudaFreeHost(h->cs_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->external) return;   // the caller's block and stream
     if (h->buf[0]) cudaFree(h->buf[0]);
     if (h->buf[1]) cudaFree(h->buf[1]);
     if (h->partials) cudaFree(h->partials);
     if (h->work) cudaFree(h->work);
     if (h->flags) cudaFree(h->flags);
     if (h->own) cudaStreamDestroy(h->own);
+}
+
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+size_t pf::handle_block_bytes(const mmsp_gpu_desc& d)
+{
+    return 2 * align256(state_bytes(&d)) + align256(pf::kPartialsBytes) + 256 + align256(work_bytes(&d));
+}
+
+static int make_plan(mmsp_gpu_handle* h);
+
+int pf::create_in(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc, void* block, cudaStream_t stream)
+{
+    if (!out || !block || ((uintptr_t)block & 255)) return MMSP_GPU_EINVAL;
+    *out = nullptr;
+    int rc = validate(desc, nullptr, 0);
+    if (rc) return rc;
+    mmsp_gpu_handle* h = new (std::nothrow) mmsp_gpu_handle();
+    if (!h) return MMSP_GPU_ENOMEM;
+    memset(h, 0, sizeof(*h));
+    h->external = true;
+    h->d = *desc;
+    for (int a = desc->dim; a < 3; a++) h->d.n[a] = 1;
+    h->g = pf::make_geom(h->d);
+    h->c = pf::make_coeffs(h->d);
+    cudaGetDevice(&h->device);
+    h->esize = esize_of(&h->d);
+    h->bytes = state_bytes(&h->d);
+    h->elems = h->bytes / h->esize;
+    h->own = h->stream = stream;
+    char* p = static_cast<char*>(block);
+    h->buf[0] = p;
+    p += align256(h->bytes);
+    h->buf[1] = p;
+    p += align256(h->bytes);
+    h->partials = reinterpret_cast<double*>(p);
+    p += align256(pf::kPartialsBytes);
+    h->flags = reinterpret_cast<int*>(p);
+    p += 256;
+    if (work_bytes(&h->d)) h->work = p;
+    cudaError_t e = cudaEventCreate(&h->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->flags, 0, 256, stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release(h);
+        delete h;
+        return MMSP_GPU_ECUDA;
+    }
+    rc = make_plan(h);
+    if (rc) {
+        release(h);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return MMSP_GPU_OK;
 }
 
 static int make_plan(mmsp_gpu_handle* h)
@@ -365,6 +423,9 @@ static int upload(mmsp_gpu_handle* h, const void* src, size_t bytes, int layout,
         e = cudaMemcpyAsync(h->buf[1], h->buf[0], h->bytes, cudaMemcpyDeviceToDevice, h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, "upload guess");
     }
+    // the noise stream's step index counts from the upload
+    if ((e = cudaMemsetAsync(h->flags + 4, 0, sizeof(long long), h->stream)) != cudaSuccess)
+        return cuda_fail(h, e, "upload step counter");
     h->steps = 0;
     h->timed = false;
     if (sync && (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(h, e, "upload sync");
@@ -410,21 +471,22 @@ extern "C" int mmsp_gpu_download_device(mmsp_gpu_handle* h, void* dev, size_t by
     return download(h, dev, bytes, layout, cudaMemcpyDeviceToDevice, false);
 }
 
-// One step on `s`; `step` indexes the noise stream of the stochastic forms
-// (steps since the last upload) and is unused otherwise.
-static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s, long long step = 0)
+// One step on `s`.  The stochastic forms read the index of their noise
+// stream from the handle's device step counter and advance it after the
+// step, so CUDA-graph replays of noisy steps draw new deviates every step.
+static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s)
 {
     bool ch = h->d.model == MMSP_GPU_CH || h->d.model == MMSP_GPU_CH_POLY;
     const void* in = h->buf[h->cur];
     void* out = h->buf[h->cur ^ 1];
-    pf::Coeffs c = h->c;
-    c.step = step;
+    const pf::Coeffs& c = h->c;
     cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, c, in, out, h->work, s)
-                    : h->plan.kind == 6 ? pf::launch_ch64(h->plan, h->d, h->g, c, in, out, h->work, s)
+                    : h->plan.kind == 6 ? pf::launch_ch64(h->plan, h->d, h->g, c, in, out, h->work, h->flags, s)
                     : h->plan.kind == 7 ? pf::launch_sparse_gg(h->d, h->g, c, in, out, h->flags, s)
                     : ch ? pf::launch_ch(h->plan, h->d, h->g, c, in, out, h->flags, s)
                          : pf::launch_ac(h->plan, h->d, h->g, c, in, out, h->flags, s);
     h->cur ^= 1;   // swap(oldGrid, newGrid), include/MMSP.grid.cpp:1913
+    if (e == cudaSuccess && pf::noisy(h->d)) e = pf::launch_advance_step(h->flags, s);
     return e;
 }
 
@@ -568,11 +630,6 @@ extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
     if (h->d.model == MMSP_GPU_CH_CONVEX) {
         int rc = convex_steps(h, steps);
         if (rc) return rc;
-        left = 0;
-    } else if (pf::noisy(h->d)) {
-        // the step index is a kernel argument, so no graph replay
-        for (int k = 0; k < steps; k++)
-            if ((e = one_step(h, h->stream, h->steps + k)) != cudaSuccess) return cuda_fail(h, e, "step");
         left = 0;
     } else if (steps >= kGraphMin) {
         int rc = build_graph(h);

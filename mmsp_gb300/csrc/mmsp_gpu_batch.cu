@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <new>
@@ -488,6 +489,25 @@ extern "C" int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force)
     }
     const auto t0 = std::chrono::steady_clock::now();
     const std::string key = tune_key(b);
+    // MMSP_GPU_BATCH_TILE="depth,shape" fixes the temporally blocked kernel's
+    // steps per launch and region shape (index into its shapes), "0,0" the
+    // per-step kernel, instead of tuning
+    if (const char* fix = getenv("MMSP_GPU_BATCH_TILE")) {
+        Tuning t;
+        t.rows = 16;
+        t.threads = 128;
+        if (sscanf(fix, "%d,%d", &t.ks, &t.shape) == 2 && t.shape >= 0 && t.shape < kTbShapeCount &&
+            (t.ks == 0 || std::find(std::begin(kTbDepths), std::end(kTbDepths), t.ks) != std::end(kTbDepths)) &&
+            4 * t.ks < std::min(kTbShapes[t.shape].ri, kTbShapes[t.shape].ci)) {
+            int rc = apply_tuning(b, t);
+            if (rc) return rc;
+            b->tuned = true;
+            b->tuned_from_cache = false;
+            b->tune_ms = 0.0;
+            return MMSP_GPU_OK;
+        }
+        return bfail(b, MMSP_GPU_EINVAL, "MMSP_GPU_BATCH_TILE: expected \"depth,shape\" with depth 0, 2, 4 or 8");
+    }
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         load_cache_file();

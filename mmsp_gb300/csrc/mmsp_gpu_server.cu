@@ -1,19 +1,29 @@
 // mmsp_gpu_server.cu -- the serving form (mmsp_gpu_server_*): a continuous
 // batching request loop over the single-grid handles.
 //
-// One scheduler thread owns the device work.  Each round it (1) admits
-// queued requests in arrival order while their footprint fits the HBM
-// budget, creating a handle and uploading the initial state, (2) queues up
-// to chunk_steps steps for every admitted request, each on its handle's own
-// stream so they run concurrently, and (3) waits for the round, retiring
-// requests that reached their step count: their mass and energy are
-// reduced, the state is copied to a host buffer and the handle's device
-// memory is freed before the next admission.  Clients only touch host
-// structures under the mutex.
+// Device memory: at start the server takes one block of the HBM budget and
+// carves every admitted request's buffers out of it (first fit, 256-byte
+// granules, freed blocks merge with their neighbours), so admission and
+// retirement never call cudaMalloc or cudaFree, which synchronise the
+// device.  Each admitted request gets a stream from a fixed set.
+//
+// One scheduler thread owns the device work and runs no rounds: it keeps up
+// to two chunks of at most chunk_steps steps queued on every running
+// request's stream, each followed by an event, and polls those events.
+// When a request's last chunk completes it is reduced (mass, energy),
+// copied to its host buffer and its block returned; queued requests are
+// admitted in arrival order as soon as their footprint fits the budget and
+// a block of that size is free.  Requests of different sizes therefore run
+// side by side on the GPU and finish independently.  Every request runs the
+// same kernels with the same step sequence as a lone mmsp_gpu_update (the
+// chunking does not change a step's result), so its result does not depend
+// on what else is running.  Clients only touch host structures under the
+// mutex.
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -24,9 +34,14 @@
 #include <string.h>
 
 #include "MMSP.gpu.h"
+#include "pf_handle.h"
 #include "pf_internal.h"
 
 namespace {
+
+constexpr int kStreams = 32;       // streams shared round-robin by running requests
+constexpr int kInFlight = 2;       // chunks queued ahead per request
+constexpr size_t kGranule = 256;
 
 struct Request {
     uint64_t id = 0;
@@ -35,11 +50,16 @@ struct Request {
     int steps = 0;
     std::atomic<int64_t> done{0};
     std::vector<unsigned char> host;   // initial state, then the result
-    size_t footprint = 0;
+    size_t footprint = 0;              // budget charge (mmsp_gpu_footprint)
+    size_t block_off = 0, block_bytes = 0;
     mmsp_gpu_handle* h = nullptr;
+    cudaStream_t stream = nullptr;
     int state = MMSP_GPU_REQ_QUEUED;
     std::atomic<bool> cancel{false};
-    int chunk = 0;                     // steps queued in the current round
+    int64_t queued = 0;                // steps queued on the device so far
+    std::deque<std::pair<cudaEvent_t, int>> inflight;   // (event after the chunk, its steps)
+    cudaEvent_t ev[kInFlight] = {nullptr, nullptr};
+    int next_ev = 0;
     double submit_s = 0, admit_s = 0, finish_s = 0, mass = 0, energy = 0;
     char message[160] = {0};
 };
@@ -51,6 +71,45 @@ static int note(Request* r, int rc, const char* what)
         snprintf(r->message, sizeof(r->message), "%s: %s", what, r->h ? mmsp_gpu_last_error(r->h) : mmsp_gpu_strerror(rc));
     return rc;
 }
+
+// First-fit sub-allocator over one device block.
+struct Pool {
+    char* base = nullptr;
+    size_t size = 0;
+    std::map<size_t, size_t> free;   // offset -> bytes
+
+    bool alloc(size_t bytes, size_t* off)
+    {
+        bytes = (bytes + kGranule - 1) / kGranule * kGranule;
+        for (auto it = free.begin(); it != free.end(); ++it)
+            if (it->second >= bytes) {
+                *off = it->first;
+                const size_t rest = it->second - bytes;
+                const size_t o = it->first + bytes;
+                free.erase(it);
+                if (rest) free[o] = rest;
+                return true;
+            }
+        return false;
+    }
+    void release(size_t off, size_t bytes)
+    {
+        bytes = (bytes + kGranule - 1) / kGranule * kGranule;
+        auto next = free.lower_bound(off);
+        if (next != free.end() && off + bytes == next->first) {   // merge with the following block
+            bytes += next->second;
+            next = free.erase(next);
+        }
+        if (next != free.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == off) {                // and with the preceding one
+                prev->second += bytes;
+                return;
+            }
+        }
+        free[off] = bytes;
+    }
+};
 
 using Clock = std::chrono::steady_clock;
 
@@ -70,6 +129,9 @@ struct mmsp_gpu_server {
     std::thread th;
     Clock::time_point t0;
     mmsp_gpu_server_stats st;
+    Pool pool;                    // the scheduler thread alone touches it
+    cudaStream_t streams[kStreams] = {};
+    int next_stream = 0;
 };
 
 static double since(const mmsp_gpu_server* s) { return std::chrono::duration<double>(Clock::now() - s->t0).count(); }
@@ -85,26 +147,74 @@ static void finish(mmsp_gpu_server* s, Request* r, int state)
     s->cv_done.notify_all();
 }
 
+// Scheduler thread: the request's device work is over (or never started);
+// give back its handle, events and block.
 static void release_request(mmsp_gpu_server* s, Request* r)
 {
+    if (r->stream) cudaStreamSynchronize(r->stream);
     if (r->h) {
         mmsp_gpu_destroy(r->h);
         r->h = nullptr;
     }
+    for (auto& e : r->ev)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    r->inflight.clear();
+    if (r->block_bytes) s->pool.release(r->block_off, r->block_bytes);
+    r->block_bytes = 0;
     std::lock_guard<std::mutex> lock(s->mu);
     s->in_use -= r->footprint;
+}
+
+// Scheduler thread: queue chunks until kInFlight are in flight or the steps are all queued.
+static int feed(mmsp_gpu_server* s, Request* r)
+{
+    while ((int)r->inflight.size() < kInFlight && r->queued < r->steps) {
+        const int n = (int)std::min<int64_t>(s->chunk, r->steps - r->queued);
+        int rc = note(r, mmsp_gpu_step(r->h, n), "step");
+        if (rc) return rc;
+        cudaEvent_t e = r->ev[r->next_ev];
+        r->next_ev = (r->next_ev + 1) % kInFlight;
+        if (cudaEventRecord(e, r->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return note(r, MMSP_GPU_ECUDA, "event");
+        }
+        r->inflight.emplace_back(e, n);
+        r->queued += n;
+    }
+    return MMSP_GPU_OK;
+}
+
+// Scheduler thread: device state for an admitted request (its block is set).
+static int start_request(mmsp_gpu_server* s, Request* r)
+{
+    r->stream = s->streams[s->next_stream];
+    s->next_stream = (s->next_stream + 1) % kStreams;
+    for (auto& e : r->ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return note(r, MMSP_GPU_ECUDA, "event");
+        }
+    int rc = note(r, pf::create_in(&r->h, &r->d, s->pool.base + r->block_off, r->stream), "create");
+    if (!rc) rc = note(r, mmsp_gpu_upload(r->h, r->host.data(), r->host.size(), r->layout), "upload");
+    if (!rc) rc = feed(s, r);
+    return rc;
 }
 
 static void scheduler(mmsp_gpu_server* s)
 {
     cudaSetDevice(s->device);
-    std::vector<Request*> admitted;
+    std::vector<Request*> admitted, running;
     while (true) {
         admitted.clear();
         {
             std::unique_lock<std::mutex> lock(s->mu);
-            s->cv_work.wait(lock, [&] { return s->stopping || !s->queue.empty() || !s->active.empty(); });
+            if (s->active.empty())
+                s->cv_work.wait(lock, [&] { return s->stopping || !s->queue.empty(); });
             if (s->stopping) break;
+            // admission, in arrival order, while the budget and a block allow
             while (!s->queue.empty()) {
                 Request* r = s->queue.front();
                 if (r->cancel) {
@@ -114,43 +224,52 @@ static void scheduler(mmsp_gpu_server* s)
                 }
                 if (s->max_active > 0 && (int)(s->active.size() + admitted.size()) >= s->max_active) break;
                 if (s->in_use + r->footprint > s->budget) break;   // arrival order: wait for memory
+                size_t off = 0;
+                const size_t bytes = pf::handle_block_bytes(r->d);
+                if (!s->pool.alloc(bytes, &off)) break;             // fragmented: wait for a block
+                r->block_off = off;
+                r->block_bytes = bytes;
                 s->queue.pop_front();
                 s->in_use += r->footprint;
                 admitted.push_back(r);
             }
         }
-        // admission: device state for the newly admitted requests
         for (Request* r : admitted) {
-            int rc = note(r, mmsp_gpu_create(&r->h, &r->d), "create");
-            if (!rc) rc = note(r, mmsp_gpu_upload(r->h, r->host.data(), r->host.size(), r->layout), "upload");
-            std::lock_guard<std::mutex> lock(s->mu);
+            int rc = start_request(s, r);
             if (rc) {
-                if (r->h) mmsp_gpu_destroy(r->h);
-                r->h = nullptr;
-                s->in_use -= r->footprint;
+                release_request(s, r);
+                std::lock_guard<std::mutex> lock(s->mu);
                 finish(s, r, rc);
                 continue;
             }
+            std::lock_guard<std::mutex> lock(s->mu);
             r->state = MMSP_GPU_REQ_RUNNING;
             r->admit_s = since(s);
             s->st.admitted++;
             s->active.push_back(r);
         }
-        std::vector<Request*> round;
         {
             std::lock_guard<std::mutex> lock(s->mu);
-            round = s->active;
+            running = s->active;
             s->st.rounds++;
         }
-        // one round: every active request advances up to `chunk` steps on its own stream
-        for (Request* r : round) {
-            r->chunk = (int)std::min<int64_t>(s->chunk, r->steps - r->done);
-            if (r->cancel || r->chunk <= 0) r->chunk = 0;
-            else if (note(r, mmsp_gpu_step(r->h, r->chunk), "step")) r->chunk = -1;
-        }
-        for (Request* r : round) {
-            int rc = (r->chunk < 0) ? MMSP_GPU_ECUDA : note(r, mmsp_gpu_synchronize(r->h), "synchronize");
-            if (r->chunk > 0 && !rc) r->done += r->chunk;
+        // progress of every running request: completed chunks, the next ones, retirement
+        bool progressed = !admitted.empty();
+        for (Request* r : running) {
+            int rc = MMSP_GPU_OK;
+            while (!r->inflight.empty()) {
+                cudaError_t q = cudaEventQuery(r->inflight.front().first);
+                if (q == cudaErrorNotReady) break;
+                if (q != cudaSuccess) {
+                    cudaGetLastError();
+                    rc = note(r, MMSP_GPU_ECUDA, "chunk");
+                    break;
+                }
+                r->done += r->inflight.front().second;
+                r->inflight.pop_front();
+                progressed = true;
+            }
+            if (!rc && !r->cancel && r->done < r->steps) rc = feed(s, r);
             int end_state = 0;
             bool end = false;
             if (rc) {
@@ -161,7 +280,8 @@ static void scheduler(mmsp_gpu_server* s)
                 end_state = MMSP_GPU_ECANCELED;
             } else if (r->done >= r->steps) {
                 mmsp_gpu_stats stt;
-                rc = note(r, mmsp_gpu_reduce(r->h, &stt), "reduce");
+                rc = note(r, mmsp_gpu_synchronize(r->h), "synchronize");
+                if (!rc) rc = note(r, mmsp_gpu_reduce(r->h, &stt), "reduce");
                 if (!rc) rc = note(r, mmsp_gpu_download(r->h, r->host.data(), r->host.size(), r->layout), "download");
                 r->mass = stt.mass;
                 r->energy = stt.energy;
@@ -169,6 +289,7 @@ static void scheduler(mmsp_gpu_server* s)
                 end_state = rc ? rc : MMSP_GPU_REQ_DONE;
             }
             if (end) {
+                progressed = true;
                 release_request(s, r);
                 std::lock_guard<std::mutex> lock(s->mu);
                 for (size_t i = 0; i < s->active.size(); i++)
@@ -179,16 +300,25 @@ static void scheduler(mmsp_gpu_server* s)
                 finish(s, r, end_state);
             }
         }
+        if (!progressed) {
+            // nothing finished: wait briefly for the GPU or a new submission
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv_work.wait_for(lock, std::chrono::microseconds(50));
+        }
     }
     // stopping: everything not finished ends with ESTOPPED
-    std::lock_guard<std::mutex> lock(s->mu);
-    for (Request* r : s->active) {
-        if (r->h) mmsp_gpu_destroy(r->h);
-        r->h = nullptr;
-        s->in_use -= r->footprint;
+    std::vector<Request*> left;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        left = s->active;
+        s->active.clear();
+    }
+    for (Request* r : left) {
+        release_request(s, r);
+        std::lock_guard<std::mutex> lock(s->mu);
         finish(s, r, MMSP_GPU_ESTOPPED);
     }
-    s->active.clear();
+    std::lock_guard<std::mutex> lock(s->mu);
     for (Request* r : s->queue) finish(s, r, MMSP_GPU_ESTOPPED);
     s->queue.clear();
 }
@@ -229,6 +359,29 @@ extern "C" int mmsp_gpu_server_start(mmsp_gpu_server** out, const mmsp_gpu_serve
     }
     s->budget = (cfg && cfg->hbm_budget_bytes) ? cfg->hbm_budget_bytes : (size_t)(0.8 * (double)free_b);
     if (s->budget > free_b) s->budget = free_b;
+    // the one device block requests are carved from (a little above the budget:
+    // blocks are 256-byte aligned per buffer); halve it until the device grants it
+    size_t want = s->budget + s->budget / 64 + (64u << 20);
+    while (want >= (64u << 20) && cudaMalloc((void**)&s->pool.base, want) != cudaSuccess) {
+        cudaGetLastError();
+        want /= 2;
+    }
+    if (!s->pool.base) {
+        delete s;
+        return MMSP_GPU_ENOMEM;
+    }
+    s->pool.size = want;
+    s->pool.free[0] = want;
+    if (s->budget > want) s->budget = want;
+    for (auto& st : s->streams)
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            for (auto& t : s->streams)
+                if (t) cudaStreamDestroy(t);
+            cudaFree(s->pool.base);
+            delete s;
+            return MMSP_GPU_ECUDA;
+        }
     if (cfg && cfg->chunk_steps > 0) s->chunk = cfg->chunk_steps;
     if (cfg && cfg->max_active > 0) s->max_active = cfg->max_active;
     s->st.device_bytes_budget = s->budget;
@@ -236,6 +389,9 @@ extern "C" int mmsp_gpu_server_start(mmsp_gpu_server** out, const mmsp_gpu_serve
     try {
         s->th = std::thread(scheduler, s);
     } catch (...) {
+        for (auto& t : s->streams)
+            if (t) cudaStreamDestroy(t);
+        cudaFree(s->pool.base);
         delete s;
         return MMSP_GPU_ENOMEM;
     }
@@ -365,6 +521,9 @@ extern "C" int mmsp_gpu_server_stop(mmsp_gpu_server* s)
     if (s->th.joinable()) s->th.join();
     for (auto& kv : s->all) delete kv.second;
     s->all.clear();
+    for (auto& t : s->streams)
+        if (t) cudaStreamDestroy(t);
+    if (s->pool.base) cudaFree(s->pool.base);
     delete s;
     return MMSP_GPU_OK;
 }

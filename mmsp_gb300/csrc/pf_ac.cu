@@ -189,10 +189,12 @@ cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, 
     int planes = p.planes, n = d.fields;
     if (d.dtype == MMSP_GPU_F64) {
         P<double> q = narrow<double>(c, g.dim);
+        if (noisy(d)) q.stepp = step_word(err);
         void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes, (void*)&n};
         return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);
     } else {
         P<float> q = narrow<float>(c, g.dim);
+        if (noisy(d)) q.stepp = step_word(err);
         void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes, (void*)&n};
         return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);
     }

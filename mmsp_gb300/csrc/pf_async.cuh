@@ -59,10 +59,10 @@ static __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t par
     return ok != 0;
 }
 
-// Bounded wait for phase `parity` of `bar` to complete.
-static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// Bounded wait for phase `parity` of `bar` to complete: at most `limit` polls.
+static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kSpinLimit)
 {
-    for (uint32_t i = 0; i < kSpinLimit; i++)
+    for (uint32_t i = 0; i < limit; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -83,6 +83,12 @@ static __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint
 static __device__ __forceinline__ void cp_async4(void* dst, const void* src)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// Wait until this thread's earlier cp.async copies have landed.
+static __device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // Arrive on `bar` once this thread's earlier cp.async copies have landed; the

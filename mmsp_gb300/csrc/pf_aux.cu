@@ -354,4 +354,12 @@ cudaError_t launch_transpose(int dtype, const void* in, void* out, long long cel
     return cudaGetLastError();
 }
 
+__global__ void advance_step_kernel(long long* step) { *step += 1; }
+
+cudaError_t launch_advance_step(int* err, cudaStream_t s)
+{
+    advance_step_kernel<<<1, 1, 0, s>>>(reinterpret_cast<long long*>(err + 4));
+    return cudaGetLastError();
+}
+
 }  // namespace pf

@@ -15,6 +15,7 @@
 //
 // FP64 instances use the reference's operation order (bit-identical to the
 // single-grid kernels and the oracle); FP32 instances use ordinary operators.
+#include "pf_async.cuh"
 #include "pf_batch.h"
 #include "pf_device.cuh"
 
@@ -275,11 +276,13 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
         const float w0 = (float)bi.w0, w1 = (float)bi.w1;
         const float* src = in + bi.off;
         // the region with periodic wraps (rows of axis 0, columns of axis 1)
+        // (4-byte asynchronous copies: every load of the region is in flight at once)
         if (col < cols) {
             const int gz = wrapi(it.z0 - H + col, bi.n1);
             for (int r = rg; r < rows; r += RG)
-                C[r * CI + col] = __ldg(src + (long long)wrapi(it.x0 - H + r, bi.n0) * bi.n1 + gz);
+                cp_async4(&C[r * CI + col], src + (long long)wrapi(it.x0 - H + r, bi.n0) * bi.n1 + gz);
         }
+        cp_async_wait_all();
         __syncthreads();
         for (int j = 0; j < KS; j++) {
             // mu on rows [2j+1, rows-2j-1) x cols [2j+1, cols-2j-1)

@@ -168,9 +168,9 @@ static const void* ch_pick(int dim, int model, int ty, bool unit)
 
 cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
-    // the stochastic forms take the tile kernel, which adds the noise term
+    // the stochastic forms take the rows kernel (or the tile kernel), which add the noise term
     if (!noisy(d) && ch3_stream_eligible(d, g)) return plan_ch3_stream(d, g, p);
-    if (!noisy(d) && ch_rows_eligible(d, g)) return plan_ch_rows(d, g, p);
+    if (ch_rows_eligible(d, g)) return plan_ch_rows(d, g, p);
     p->kind = 0;
     Coeffs c = make_coeffs(d);
     int ty = g.Y >= 16 ? 16 : 8;
@@ -213,14 +213,16 @@ cudaError_t launch_ch(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, 
                       const void* in, void* out, int* err, cudaStream_t s)
 {
     if (p.kind == 1) return launch_ch3_stream(p, g, c, in, out, err, s);
-    if (p.kind == 3) return launch_ch_rows(p, d, c, in, out, s);
+    if (p.kind == 3) return launch_ch_rows(p, d, c, in, out, err, s);
     int planes = p.planes;
     if (d.dtype == MMSP_GPU_F64) {
         P<double> q = narrow<double>(c, g.dim);
+        if (noisy(d)) q.stepp = step_word(err);
         void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes};
         return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);
     } else {
         P<float> q = narrow<float>(c, g.dim);
+        if (noisy(d)) q.stepp = step_word(err);
         void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes};
         return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);
     }

@@ -20,6 +20,9 @@
 // FP32 arithmetic is reassociated for throughput (six-neighbour sums and
 // Horner's form of f'(c)); the result is checked against the FP64 oracle
 // with a tolerance, not bitwise.
+#include <atomic>
+#include <stdlib.h>
+
 #include "pf_async.cuh"
 #include "pf_device.cuh"
 #include "pf_internal.h"
@@ -41,6 +44,12 @@ constexpr int kStreamR = PF_CH3_R;   // rows per block strip
 struct F32Coef {
     float wx, wy, wz, w2;   // Laplacian weights, w2 = 2(wx+wy+wz)
     float kappa, dtm, neg_r, u;
+    // Failure-detection test (0 in normal use): > 0 makes this launch's
+    // plane fills expect their bytes without issuing the copies and caps
+    // every wait at that many polls, so the waits run out with no copy in
+    // flight and the launch takes its timed-out exit (error word, drain,
+    // return).  Set from the host by MMSP_GPU_TEST_STALL_LAUNCHES only.
+    int stall;
 };
 
 // A thread's cells: float (one cell) or float2 (two adjacent cells).  float2
@@ -137,6 +146,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         constexpr uint32_t row = (uint32_t)Z * sizeof(float);
         fence_proxy_async();
         mbar_expect_tx(bar, RR * row);
+        if (q.stall) return;   // failure-detection test: the bytes never arrive
         const int a = y0 - 2, b = y0 + R + 2;
         if (a >= 0 && b <= g.Y) {
             bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
@@ -153,7 +163,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % kRing) * RR * Z; };
     auto wait_plane = [&](int pl) {
         const int k = pl - x_first;
-        if (!mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u)) {
+        if (!mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, q.stall ? (uint32_t)q.stall : kSpinLimit)) {
             s_err = 1;
             atomicExch(err, 1);
         }
@@ -262,7 +272,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         // leave no copy in flight: wait (bounded) for every issued fill
         for (int pl = max(x, x_first); pl <= min(x + kRing, x_last); pl++) {
             const int k = pl - x_first;
-            mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u);
+            mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, q.stall ? (uint32_t)q.stall : kSpinLimit);
         }
     }
 }
@@ -278,7 +288,26 @@ static F32Coef f32coef(const Coeffs& c)
     q.dtm = (float)c.dtm;
     q.neg_r = (float)c.neg_r;
     q.u = (float)c.u;
+    q.stall = 0;
     return q;
+}
+
+// MMSP_GPU_TEST_STALL_LAUNCHES=n: the next n launches of this kernel in the
+// process run the failure-detection test (F32Coef::stall) with waits of 4
+// polls.  Read once; unset in normal use.
+static std::atomic<int> g_stall_left{-1};
+static int take_stall()
+{
+    int left = g_stall_left.load();
+    if (left < 0) {
+        const char* v = getenv("MMSP_GPU_TEST_STALL_LAUNCHES");
+        int n = v ? atoi(v) : 0;
+        g_stall_left.compare_exchange_strong(left, n > 0 ? n : 0);
+    }
+    int cur = g_stall_left.load();
+    while (cur > 0 && !g_stall_left.compare_exchange_weak(cur, cur - 1)) {
+    }
+    return cur > 0 ? 4 : 0;
 }
 
 static bool row_ok(int Z) { return Z == 32 || Z == 64 || Z == 128 || Z == 256 || Z == 512; }
@@ -347,6 +376,7 @@ cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c,
                               int* err, cudaStream_t s)
 {
     F32Coef q = f32coef(c);
+    q.stall = take_stall();
     int planes = p.planes;
     void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes, (void*)&err};
     return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);

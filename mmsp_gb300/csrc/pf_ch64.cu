@@ -244,11 +244,12 @@ cudaError_t plan_ch64(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 }
 
 cudaError_t launch_ch64(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* in,
-                        void* out, void* work, cudaStream_t s)
+                        void* out, void* work, int* err, cudaStream_t s)
 {
     C64 q = c64_of(c, g.dim);
     q.poly0 = (d.model == MMSP_GPU_CH ? 2.0 : c.neg_r) + c.kappa * q.w2;
     P<double> pp = narrow<double>(c, g.dim);
+    if (noisy(d)) pp.stepp = step_word(err);
     int planes = p.planes;
     void* a1[] = {(void*)&in, (void*)&work, (void*)&g, (void*)&q, (void*)&pp, (void*)&planes};
     cudaError_t e = cudaLaunchKernel(p.fn, p.grid, p.block, a1, 0, s);

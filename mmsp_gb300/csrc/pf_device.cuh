@@ -48,8 +48,17 @@ template <typename T> struct P {
     T kappa, dtm, gamma2, neg_r, u;
     double noise;               // thermal noise standard deviation (0: none)
     unsigned long long seed;    // noise stream
-    long long step;             // step index within the stream
+    long long step;             // step index within the stream, when stepp is null
+    const long long* stepp;     // device word holding the step index (a handle's step counter)
 };
+
+// The step index of the noise stream: the handle's device counter, so that
+// graph replays of noisy steps draw each step's own deviates.
+template <typename T>
+static __device__ __forceinline__ long long step_of(const P<T>& p)
+{
+    return p.stepp ? *p.stepp : p.step;
+}
 
 // Value j of the SplitMix64 stream `seed` (Steele, Lea and Flood, OOPSLA
 // 2014): the same function as mmsp_gb300/inputs.py and the oracle use.
@@ -88,12 +97,12 @@ static __device__ __forceinline__ float gauss_at_f(unsigned long long seed, unsi
 // in the state type.
 static __device__ __forceinline__ double noise_at(const P<double>& p, long long cells, long long cell)
 {
-    const unsigned long long k = (unsigned long long)p.step * (unsigned long long)cells + (unsigned long long)cell;
+    const unsigned long long k = (unsigned long long)step_of(p) * (unsigned long long)cells + (unsigned long long)cell;
     return 0.0 + gauss_at(p.seed, k) * p.noise;
 }
 static __device__ __forceinline__ float noise_at(const P<float>& p, long long cells, long long cell)
 {
-    const unsigned long long k = (unsigned long long)p.step * (unsigned long long)cells + (unsigned long long)cell;
+    const unsigned long long k = (unsigned long long)step_of(p) * (unsigned long long)cells + (unsigned long long)cell;
     return gauss_at_f(p.seed, k) * (float)p.noise;
 }
 
@@ -221,6 +230,7 @@ static inline P<T> narrow(const Coeffs& c, int dim)
     p.noise = c.noise;
     p.seed = c.seed;
     p.step = c.step;
+    p.stepp = nullptr;
     return p;
 }
 

@@ -7,6 +7,14 @@
 #include "pf_internal.h"
 
 namespace pf {
+// Device bytes of one block holding a handle's buffers (two states, the
+// reduction partials, the error words, a model's work grid), each 256-byte
+// aligned, for create_in.
+size_t handle_block_bytes(const mmsp_gpu_desc& d);
+// A handle whose device buffers are carved from `block` (handle_block_bytes
+// long, 256-byte aligned) and whose work is ordered on `stream`: no device
+// allocation, no stream creation.  Destroying it frees neither.
+int create_in(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc, void* block, cudaStream_t stream);
 struct OutputState;
 // Wait for the handle's snapshots still being written, then free what the
 // output path allocated.
@@ -30,6 +38,7 @@ struct mmsp_gpu_handle {
     cudaStream_t stream;     // stream in use
     cudaEvent_t ev0, ev1;
     bool timed;              // ev0/ev1 bracket the last step call
+    bool external;           // buffers and stream belong to the caller (pf::create_in): not freed here
     int64_t steps;
     // CUDA graph of kGraphSteps steps starting from buf[0] (an even count ends in buf[0])
     cudaGraphExec_t graph;

@@ -104,19 +104,28 @@ cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c,
 bool ch64_eligible(const mmsp_gpu_desc& d, const Geom& g);
 cudaError_t plan_ch64(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ch64(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* in,
-                        void* out, void* work, cudaStream_t s);
+                        void* out, void* work, int* err, cudaStream_t s);
 
 // FP32 2D/3D Cahn-Hilliard for any row length up to 1024 (pf_rows.cu).
 bool ch_rows_eligible(const mmsp_gpu_desc& d, const Geom& g);
 cudaError_t plan_ch_rows(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ch_rows(const StepPlan& p, const mmsp_gpu_desc& d, const Coeffs& c, const void* in, void* out,
-                           cudaStream_t s);
+                           int* err, cudaStream_t s);
 
 // FP32 3D Allen-Cahn on whole rows (pf_ac3_stream.cu).
 bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g);
 cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ac3_stream(const StepPlan& p, const Geom& g, const Coeffs& c, const void* in, void* out,
                               int* err, cudaStream_t s);
+
+// A handle's device status block (256 bytes): int word 0 is set when a
+// kernel's bounded wait runs out, int word 1 when a sparse list overflows;
+// the 64-bit word at byte 16 counts the steps since the last upload, the
+// index of the noise stream of the stochastic forms.  Launchers get the
+// block as `err`.
+inline const long long* step_word(const int* err) { return reinterpret_cast<const long long*>(err + 4); }
+// Add one to the step word (after each noisy step, in stream order).
+cudaError_t launch_advance_step(int* err, cudaStream_t s);
 
 // One step in -> out on `s`.  `err` is a device word a kernel sets when a
 // bounded wait runs out.

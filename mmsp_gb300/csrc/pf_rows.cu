@@ -26,6 +26,10 @@ struct RowsGeom {
 struct RowsCoef {
     float wx, wy, wz, w2;   // weights of the streaming, row and cell axes; w2 = 2 * sum
     float kappa, dtm, neg_r, u;
+    float noise;                 // thermal noise standard deviation (NOISE kernels)
+    unsigned long long seed;     // its stream
+    long long cells;
+    const long long* stepp;      // the handle's step counter: the stream's step index
 };
 
 template <int MODEL>
@@ -43,7 +47,12 @@ struct RowsShape {
     static constexpr int OFF = H ? 1 : 0;         // index of row 0 in the mu arrays
 };
 
-template <int R, int H, int MODEL>
+// NOISE: the stochastic forms (model_B.cpp:100-101, spinodal.cpp:95-97) add
+// std * N(0,1) to mu, deviate step*cells + cell of the counter-based stream
+// (pf_device.cuh), so a halo mu recomputed in a neighbouring block draws the
+// same number; the step comes from the handle's device counter, so graph
+// replays advance it.
+template <int R, int H, int MODEL, bool NOISE>
 __global__ void __launch_bounds__(H ? 512 : 1024)
 ch_rows_f32(const float* __restrict__ cin, float* __restrict__ cout, RowsGeom g, RowsCoef q, int planes)
 {
@@ -72,6 +81,7 @@ ch_rows_f32(const float* __restrict__ cin, float* __restrict__ cout, RowsGeom g,
         for (int i = 0; i < RC; i++) d[i] = __ldg(base + rowoff[i]);
     };
 
+    const unsigned long long kstep = NOISE ? (unsigned long long)*q.stepp * (unsigned long long)q.cells : 0ull;
     float c0[RC], c1[RC], c2[RC], nx[RC];
     float m0[RM], m1[RM], m2[RM];
     load(c0, xs - 2);
@@ -103,6 +113,10 @@ ch_rows_f32(const float* __restrict__ cin, float* __restrict__ cout, RowsGeom g,
             if constexpr (H != 0) lap = fmaf(q.wx, sx, fmaf(q.wy, c1[i - 1] + c1[i + 1], fmaf(q.wz, sz, -q.w2 * cc)));
             else lap = fmaf(q.wx, sx, fmaf(q.wz, sz, -q.w2 * cc));
             m2[m] = rows_mu<MODEL>(cc, lap, q);
+            if (NOISE) {
+                const long long cell = (long long)wrapi(x + 1, g.NX) * g.plane + rowoff[i];
+                m2[m] += gauss_at_f(q.seed, kstep + (unsigned long long)cell) * q.noise;
+            }
         }
         // c'(x) from mu(x-1), mu(x), mu(x+1); Z neighbours of mu(x) from the buffer
         if (x >= xs) {
@@ -139,10 +153,11 @@ ch_rows_f32(const float* __restrict__ cin, float* __restrict__ cout, RowsGeom g,
 }
 
 template <int R, int H>
-static const void* rows_pick(int model)
+static const void* rows_pick(int model, bool noise)
 {
-    return model == MMSP_GPU_CH ? (const void*)&ch_rows_f32<R, H, MMSP_GPU_CH>
-                                : (const void*)&ch_rows_f32<R, H, MMSP_GPU_CH_POLY>;
+    if (noise) return (const void*)&ch_rows_f32<R, H, MMSP_GPU_CH_POLY, true>;   // only the shipped form is noisy
+    return model == MMSP_GPU_CH ? (const void*)&ch_rows_f32<R, H, MMSP_GPU_CH, false>
+                                : (const void*)&ch_rows_f32<R, H, MMSP_GPU_CH_POLY, false>;
 }
 
 static RowsGeom rows_geom(const mmsp_gpu_desc& d)
@@ -175,10 +190,11 @@ cudaError_t plan_ch_rows(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     const int R = rows_r(d);
     const int H = d.dim == 3 ? 2 : 0;
     const int RM = H ? R + 2 : R;
-    if (d.dim == 2) p->fn = rows_pick<1, 0>(d.model);
-    else if (R == 4) p->fn = rows_pick<4, 2>(d.model);
-    else if (R == 2) p->fn = rows_pick<2, 2>(d.model);
-    else p->fn = rows_pick<1, 2>(d.model);
+    const bool noise = noisy(d);
+    if (d.dim == 2) p->fn = rows_pick<1, 0>(d.model, noise);
+    else if (R == 4) p->fn = rows_pick<4, 2>(d.model, noise);
+    else if (R == 2) p->fn = rows_pick<2, 2>(d.model, noise);
+    else p->fn = rows_pick<1, 2>(d.model, noise);
     const int threads = (rg.Z + 31) / 32 * 32;
     p->smem = sizeof(float) * (size_t)(2 * RM + 2 * R) * rg.Z;
     p->block = dim3(threads, 1, 1);
@@ -206,7 +222,7 @@ cudaError_t plan_ch_rows(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 }
 
 cudaError_t launch_ch_rows(const StepPlan& p, const mmsp_gpu_desc& d, const Coeffs& c, const void* in, void* out,
-                           cudaStream_t s)
+                           int* err, cudaStream_t s)
 {
     RowsGeom rg = rows_geom(d);
     RowsCoef q;
@@ -224,6 +240,10 @@ cudaError_t launch_ch_rows(const StepPlan& p, const mmsp_gpu_desc& d, const Coef
     q.dtm = (float)c.dtm;
     q.neg_r = (float)c.neg_r;
     q.u = (float)c.u;
+    q.noise = (float)c.noise;
+    q.seed = c.seed;
+    q.cells = (long long)rg.NX * rg.plane;
+    q.stepp = noisy(d) ? step_word(err) : nullptr;
     int planes = p.planes;
     void* args[] = {(void*)&in, (void*)&out, (void*)&rg, (void*)&q, (void*)&planes};
     return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);

@@ -108,12 +108,15 @@ def test_autotune_cache(gpu, tmp_path, monkeypatch):
         first = b.info()
         assert first.tuned_from_cache == 0 and first.tune_ms > 0
     saved = json.loads(path.read_text())
-    assert any(v == [first.rows_per_item, first.threads_per_block] for v in saved.values())
+    assert any(v[:2] == [first.rows_per_item, first.threads_per_block] and v[2] in (0, first.temporal_depth)
+               for v in saved.values())
     with gpu.Batch(descs) as b:
         b.tune()
         again = b.info()
         assert again.tuned_from_cache == 1
         assert (again.rows_per_item, again.threads_per_block) == (first.rows_per_item, first.threads_per_block)
+        assert (again.temporal_depth, again.tile_rows, again.tile_cols) == \
+            (first.temporal_depth, first.tile_rows, first.tile_cols)
 
 
 def test_batch_rejects_mixed_dtypes(gpu):
@@ -122,3 +125,58 @@ def test_batch_rejects_mixed_dtypes(gpu):
     with pytest.raises(gpu.GpuError) as ei:
         gpu.Batch([d1, d2])
     assert ei.value.code == gpu.EINVAL
+
+
+TILINGS = [(2, 0), (4, 0), (8, 0), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2), (0, 0)]
+
+
+@pytest.mark.parametrize("ks,shape", TILINGS, ids=["depth%d-shape%d" % t for t in TILINGS])
+def test_batch_temporal_blocking(gpu, oracle, monkeypatch, ks, shape):
+    """The temporally blocked kernel on every region shape and depth: grids
+    smaller than a tile (rows and columns wrap more than once), ragged edge
+    tiles, non-unit spacing, both Cahn-Hilliard forms; step counts that are
+    not multiples of the depth; within 1e-5 of the FP64 oracle, and within
+    FP32 rounding of the per-step kernel."""
+    from mmsp_gb300 import inputs
+
+    monkeypatch.setenv("MMSP_GPU_BATCH_TILE", "%d,%d" % (ks, shape))
+    grids = [((3, 32), "ch", {}), ((64, 64), "ch", {}), ((40, 96), "ch", dict(kappa=1.9)),
+             ((130, 512), "ch", dict(kappa=0.5)), ((77, 224), "ch", dict(kappa=1.4)), ((200, 160), "ch", {}),
+             ((33, 64), "ch", dict(dx=[1.1, 0.9]))]
+    members = [(inputs.noisy_composition(sh, 0.45, 0.03, 700 + k), m, p) for k, (sh, m, p) in enumerate(grids)]
+    descs = [gpu.make_desc(x.shape, 1, np.float32, m, mobility=1.0, dt=0.004, **p) for x, m, p in members]
+    with gpu.Batch(descs) as b:
+        for i, (x, _, _) in enumerate(members):
+            b.upload(i, x.astype(np.float32))
+        b.step(3)
+        b.step(150)      # graph replay, then blocked launches and single steps
+        info = b.info()
+        assert info.temporal_depth == max(ks, 1)
+        if ks:
+            assert (info.tile_rows, info.tile_cols) == [(64, 128), (96, 128), (128, 64)][shape] and info.tiles > 0
+        for i, (x, _, p) in enumerate(members):
+            got = b.download(i).astype(np.float64)
+            want = oracle.ch_baseline(x, 153, p.get("kappa", 1.0), 1.0, 0.004, dx=p.get("dx"))
+            assert np.abs(got - want).max() <= TOL_F32, (i, np.abs(got - want).max())
+
+
+def test_batch_tuner_considers_temporal_blocking(gpu, monkeypatch):
+    """Tuning an all-FP32 2D batch scores the blocked kernel too; whatever
+    wins is reported, and a bad override is refused."""
+    from mmsp_gb300 import inputs
+
+    monkeypatch.delenv("MMSP_GPU_TUNE_CACHE", raising=False)
+    work = inputs.batched_cahn_hilliard(count=16, seed=5)
+    descs = [gpu.make_desc(c0.shape, 1, np.float32, "ch", kappa=k, dt=0.005) for c0, k in work]
+    with gpu.Batch(descs) as b:
+        for i, (c0, _) in enumerate(work):
+            b.upload(i, c0.astype(np.float32))
+        b.tune(force=True)
+        info = b.info()
+        assert info.temporal_depth in (1, 2, 4, 8)
+        assert (info.tile_rows > 0) == (info.temporal_depth > 1)
+    monkeypatch.setenv("MMSP_GPU_BATCH_TILE", "3,0")
+    with gpu.Batch(descs) as b:
+        with pytest.raises(gpu.GpuError) as ei:
+            b.tune(force=True)
+        assert ei.value.code == gpu.EINVAL
