@@ -302,17 +302,18 @@ def other_models(native, inputs, timed):
 
 def sparse_grain_growth(native, inputs):
     """Sparse phase-field grain growth (the sparsePF example's update, FP64)
-    on a 512^2 grid of 64 periodic Voronoi grains, 16 item slots per cell,
-    200 steps in one call, beside the oracle (the example's loops restated
-    in C, one thread) on 2 steps.  Algorithmic bytes of a step: every
-    cell's list read and the new list written once (int32 count, then
-    int32 index + float64 value per item), at the lists' mean length."""
+    on a 2048^2 grid of 32 periodic Voronoi grains, 16 item slots per
+    cell, 100 steps in one call, beside the oracle (the example's loops
+    restated in C, one thread) on 2 steps.  Algorithmic bytes of a step:
+    every cell's list read and the new list written once (int32 count, then
+    int32 index + float64 value per item), at the lists' mean length (about
+    190 MB per step: above the 129 MB L2)."""
     import torch
 
     from oracle import pf_oracle
 
-    shape, K, steps = (512, 512), 16, 200
-    c0, i0, v0 = inputs.sparse_grains(shape, 64, 21, K)
+    shape, K, steps = (2048, 2048), 16, 100
+    c0, i0, v0 = inputs.sparse_grains(shape, 32, 21, K)
     d = native.make_desc(shape, K, np.float64, "sparse_gg")
     with native.Stepper(d) as s:
         s.sparse_upload(c0, i0, v0)
@@ -335,7 +336,7 @@ def sparse_grain_growth(native, inputs):
     pf_oracle.sparse_gg(c0, i0, v0, 2, 0.01, 1e-8, threads=1)
     cpu_s = (time.perf_counter() - t0) / 2
     rate = cells * steps / (ms / 1e3)
-    return {"sparse2d_512_g64_200": {"f64_ms": ms, "cell_updates_per_s": rate, "mean_items_per_cell": mean_items,
+    return {"sparse2d_2048_g32_100": {"f64_ms": ms, "cell_updates_per_s": rate, "mean_items_per_cell": mean_items,
                                      "longest_list": int(cnt.max()),
                                      "roofline": {"bound": "hbm", "alg_bytes_per_step": alg,
                                                   "achieved_gbs": alg / (ms / 1e3 / steps) / 1e9, "peak": peak,
@@ -866,7 +867,7 @@ CASES = {
     "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ostwald3d_f32": ((256, 128, 64), 2, np.float32, "ostwald", {}),
     "convex2d_f64": ((400, 200), 2, np.float64, "ch_convex", {}),
-    "sparse2d_f64": ((512, 512), 16, np.float64, "sparse_gg", {}),
+    "sparse2d_f64": ((2048, 2048), 16, np.float64, "sparse_gg", {}),
 }
 
 
@@ -891,7 +892,7 @@ def run_case(name: str, steps: int):
     if model == "sparse_gg":
         d = native.make_desc(shape, fields, dtype, model, **params)
         with native.Stepper(d) as s:
-            s.sparse_upload(*inputs.sparse_grains(shape, 64, 21, fields))
+            s.sparse_upload(*inputs.sparse_grains(shape, 32, 21, fields))
             s.step(steps)
             cnt, _, _ = s.sparse_download()
         print("case %s: %d steps, mean items %.3f" % (name, steps, float(cnt.mean())))

@@ -168,9 +168,11 @@ static const void* ch_pick(int dim, int model, int ty, bool unit)
 
 cudaError_t plan_ch(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
-    // the stochastic forms take the rows kernel (or the tile kernel), which add the noise term
+    // the stochastic forms take the rows kernel in 3D and the tile kernel
+    // otherwise (a 2D rows block holds a whole row: 1024-thread blocks leave
+    // the noise arithmetic short of warps), both of which add the noise term
     if (!noisy(d) && ch3_stream_eligible(d, g)) return plan_ch3_stream(d, g, p);
-    if (ch_rows_eligible(d, g)) return plan_ch_rows(d, g, p);
+    if (ch_rows_eligible(d, g) && (!noisy(d) || g.dim == 3)) return plan_ch_rows(d, g, p);
     p->kind = 0;
     Coeffs c = make_coeffs(d);
     int ty = g.Y >= 16 ? 16 : 8;

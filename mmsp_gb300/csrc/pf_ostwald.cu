@@ -6,10 +6,10 @@
 // (:89-100), ghostswap, then the new composition from the Laplacian of that
 // grid and the new order parameters (fields 1..N-1) from their own
 // Laplacians (:103-120).  Here each pass is one kernel over all cells (a
-// block walks rows along axis Z, one thread per cell of a row, so a cell's
-// coordinates need no division), the work grid is a device buffer of the
-// handle, and the periodic halo is index arithmetic.  Neighbour values come
-// through the L1/L2 caches.
+// thread walks a (y, z) column plane by plane, so a cell's coordinates need
+// no division and its neighbour offsets are fixed per column), the work
+// grid is a device buffer of the handle, and the periodic halo is index
+// arithmetic.  Neighbour values come through the L1/L2 caches.
 //
 // FP64 follows the reference's operation order with separately rounded
 // operations (pow(x,3) as the compensated cube of pf_device.cuh, pow(x,2)
@@ -51,34 +51,35 @@ static OstP<T> ost_narrow(const Coeffs& c, int dim)
 }
 
 // Offsets of the six periodic neighbours of a cell (padded axes X, Y, Z).
-// The X and Y offsets are those of the cell's row; Z depends on the cell.
+// A thread owns one (y, z) column: its Y and Z offsets are fixed, the X
+// ones are taken per plane.
 struct Nb {
     long long xh, xl, yh, yl;
     int zh, zl;
 };
 
-static __device__ __forceinline__ Nb row_neighbours(const Geom& g, int x, int y)
+static __device__ __forceinline__ Nb column_neighbours(const Geom& g, int y, int z)
 {
     Nb n;
-    n.xh = (x + 1 == g.X ? -(long long)x : 1LL) * g.YZ;
-    n.xl = (x == 0 ? (long long)(g.X - 1) : -1LL) * g.YZ;
+    n.xh = n.xl = 0;
     n.yh = (y + 1 == g.Y ? -(long long)y : 1LL) * g.Z;
     n.yl = (y == 0 ? (long long)(g.Y - 1) : -1LL) * g.Z;
-    n.zh = n.zl = 0;
+    n.zh = z + 1 == g.Z ? -z : 1;
+    n.zl = z == 0 ? g.Z - 1 : -1;
     return n;
 }
 
-static __device__ __forceinline__ void cell_z(Nb& n, const Geom& g, int z)
+static __device__ __forceinline__ void plane_x(Nb& n, const Geom& g, int x)
 {
-    n.zh = z + 1 == g.Z ? -z : 1;
-    n.zl = z == 0 ? g.Z - 1 : -1;
+    n.xh = (x + 1 == g.X ? -(long long)x : 1LL) * g.YZ;
+    n.xl = (x == 0 ? (long long)(g.X - 1) : -1LL) * g.YZ;
 }
 
 template <typename T, int DIM, bool UNIT>
 static __device__ __forceinline__ T lap_at(const T* __restrict__ f, long long i, const Nb& n, const OstP<T>& p)
 {
-    return lap_ref<T, UNIT, DIM>(twice(f[i]), f[i + n.xh], f[i + n.xl], f[i + n.yh], f[i + n.yl], f[i + n.zh],
-                                 f[i + n.zl], p.wx, p.wy, p.wz);
+    return lap_ref<T, UNIT, DIM>(twice(__ldg(f + i)), __ldg(f + i + n.xh), __ldg(f + i + n.xl), __ldg(f + i + n.yh),
+                                 __ldg(f + i + n.yl), __ldg(f + i + n.zh), __ldg(f + i + n.zl), p.wx, p.wy, p.wz);
 }
 
 // sum_{j>=1} pow(e_j,2), ostwald.cpp:91-93 (0.0 + x == x for x >= 0).
@@ -93,37 +94,43 @@ static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long
 #pragma unroll(NF ? NF : 1)
     for (int j = 1; j < (NF ? NF : 64); j++) {
         if (!NF && j >= n) break;
-        const T e = s[(long long)j * cells + i];
+        const T e = __ldg(s + (long long)j * cells + i);
         sum = j == 1 ? A::mul(e, e) : A::add(sum, A::mul(e, e));
     }
     return sum;
 }
 
+// Both passes run on (y, z) columns: a block of kOstZ x kOstY threads over a
+// run of kOstPlanes X planes, a thread walking its column plane by plane
+// (coalesced rows, no per-cell division, neighbours through L1 with the
+// periodic offsets precomputed per column).
+constexpr int kOstZ = 32, kOstY = 4, kOstPlanes = 8;
+
 // Pass 1, ostwald.cpp:95-99:
 //   w = -A*(C-Cm) + B*pow(C-Cm,3) + Da*pow(C-Ca,3) + Db*pow(C-Cb,3) - g*(C-Ca)*sum - kappa*lap C
 template <typename T, int DIM, bool UNIT, int NF>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kOstZ * kOstY)
 ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
 {
     using A = Ar<T>;
-    const long long rows = (long long)g.X * g.Y;
-    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
-        const int x = (int)(row / g.Y), y = (int)(row - (long long)x * g.Y);
-        Nb n = row_neighbours(g, x, y);
-        for (int z = threadIdx.x; z < g.Z; z += blockDim.x) {
-            cell_z(n, g, z);
-            const long long i = row * g.Z + z;
-            const T sum = order_sum<T, NF>(s, i, g.cells, N);
-            const T C = s[i];
-            const T lap = lap_at<T, DIM, UNIT>(s, i, n, p);
-            const T dm = A::sub(C, p.Cm), da = A::sub(C, p.Ca), db = A::sub(C, p.Cb);
-            T v = A::mul(p.negA, dm);
-            v = A::add(v, A::mul(p.B, cube(dm)));
-            v = A::add(v, A::mul(p.Da, cube(da)));
-            v = A::add(v, A::mul(p.Db, cube(db)));
-            v = A::sub(v, A::mul(A::mul(p.g, da), sum));
-            w[i] = A::sub(v, kappa_times(p.kappa, lap));
-        }
+    const int z = blockIdx.x * kOstZ + threadIdx.x;
+    const int y = blockIdx.y * kOstY + threadIdx.y;
+    if (z >= g.Z || y >= g.Y) return;
+    Nb n = column_neighbours(g, y, z);
+    const int xs = blockIdx.z * kOstPlanes, xe = min(xs + kOstPlanes, g.X);
+    for (int x = xs; x < xe; x++) {
+        plane_x(n, g, x);
+        const long long i = (long long)x * g.YZ + (long long)y * g.Z + z;
+        const T sum = order_sum<T, NF>(s, i, g.cells, N);
+        const T C = __ldg(s + i);
+        const T lap = lap_at<T, DIM, UNIT>(s, i, n, p);
+        const T dm = A::sub(C, p.Cm), da = A::sub(C, p.Ca), db = A::sub(C, p.Cb);
+        T v = A::mul(p.negA, dm);
+        v = A::add(v, A::mul(p.B, cube(dm)));
+        v = A::add(v, A::mul(p.Da, cube(da)));
+        v = A::add(v, A::mul(p.Db, cube(db)));
+        v = A::sub(v, A::mul(A::mul(p.g, da), sum));
+        w[i] = A::sub(v, kappa_times(p.kappa, lap));
     }
 }
 
@@ -131,32 +138,32 @@ ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
 //   C'   = C + dt*D*lap w
 //   e_j' = e_j - dt*L*(-g*pow(C-Ca,2) + delta*pow(e_j,3) + eps*e_j*(sum - pow(e_j,2)) - kappa*lap e_j)
 template <typename T, int DIM, bool UNIT, int NF>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kOstZ * kOstY)
 ostwald_update(const T* __restrict__ s, const T* __restrict__ w, T* __restrict__ out, Geom g, OstP<T> p, int N)
 {
     using A = Ar<T>;
-    const long long rows = (long long)g.X * g.Y;
-    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
-        const int x = (int)(row / g.Y), y = (int)(row - (long long)x * g.Y);
-        Nb n = row_neighbours(g, x, y);
-        for (int z = threadIdx.x; z < g.Z; z += blockDim.x) {
-            cell_z(n, g, z);
-            const long long i = row * g.Z + z;
-            const T C = s[i];
-            out[i] = A::add(C, A::mul(p.dtD, lap_at<T, DIM, UNIT>(w, i, n, p)));
-            const T sum = order_sum<T, NF>(s, i, g.cells, N);
-            const T da = A::sub(C, p.Ca);
-            const T t1 = A::mul(p.neg_g, A::mul(da, da));
+    const int z = blockIdx.x * kOstZ + threadIdx.x;
+    const int y = blockIdx.y * kOstY + threadIdx.y;
+    if (z >= g.Z || y >= g.Y) return;
+    Nb n = column_neighbours(g, y, z);
+    const int xs = blockIdx.z * kOstPlanes, xe = min(xs + kOstPlanes, g.X);
+    for (int x = xs; x < xe; x++) {
+        plane_x(n, g, x);
+        const long long i = (long long)x * g.YZ + (long long)y * g.Z + z;
+        const T C = __ldg(s + i);
+        out[i] = A::add(C, A::mul(p.dtD, lap_at<T, DIM, UNIT>(w, i, n, p)));
+        const T sum = order_sum<T, NF>(s, i, g.cells, N);
+        const T da = A::sub(C, p.Ca);
+        const T t1 = A::mul(p.neg_g, A::mul(da, da));
 #pragma unroll(NF ? NF : 1)
-            for (int j = 1; j < (NF ? NF : 64); j++) {
-                if (!NF && j >= N) break;
-                const T* f = s + (long long)j * g.cells;
-                const T e = f[i];
-                T v = A::add(t1, A::mul(p.delta, cube(e)));
-                v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
-                v = A::sub(v, kappa_times(p.kappa, lap_at<T, DIM, UNIT>(f, i, n, p)));
-                out[(long long)j * g.cells + i] = A::sub(e, A::mul(p.dtL, v));
-            }
+        for (int j = 1; j < (NF ? NF : 64); j++) {
+            if (!NF && j >= N) break;
+            const T* f = s + (long long)j * g.cells;
+            const T e = __ldg(f + i);
+            T v = A::add(t1, A::mul(p.delta, cube(e)));
+            v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
+            v = A::sub(v, kappa_times(p.kappa, lap_at<T, DIM, UNIT>(f, i, n, p)));
+            out[(long long)j * g.cells + i] = A::sub(e, A::mul(p.dtL, v));
         }
     }
 }
@@ -191,14 +198,10 @@ cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     const void* up = nullptr;
     if (d.dtype == MMSP_GPU_F64) ost_pick<double>(g.dim, c.unit_w, d.fields, &p->fn, &up);
     else ost_pick<float>(g.dim, c.unit_w, d.fields, &p->fn, &up);
-    // one row (axis Z) per block iteration, threads along the row; blocks
-    // stride over the rows beyond 16 resident blocks per SM
-    const int threads = g.Z >= 256 ? 256 : (g.Z + 31) / 32 * 32;
-    long long blocks = (long long)g.X * g.Y;
-    const long long most = 16LL * sm_count() * (256 / threads);
-    if (blocks > most) blocks = most;
-    p->grid = dim3((unsigned)blocks, 1, 1);
-    p->block = dim3(threads, 1, 1);
+    // (y, z) columns of kOstZ x kOstY threads over runs of kOstPlanes planes
+    p->grid = dim3((g.Z + kOstZ - 1) / kOstZ, (g.Y + kOstY - 1) / kOstY, (g.X + kOstPlanes - 1) / kOstPlanes);
+    p->block = dim3(kOstZ, kOstY, 1);
+    if (p->grid.y > 65535 || p->grid.z > 65535) return cudaErrorInvalidConfiguration;
     p->smem = 0;
     p->planes = 1;
     p->fields = d.fields;

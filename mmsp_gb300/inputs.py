@@ -40,14 +40,11 @@ def noisy_composition(shape, mean: float, amplitude: float, seed: int) -> np.nda
     return (mean + amplitude * (2.0 * u - 1.0)).reshape(shape)
 
 
-def voronoi_grains(shape, points: int, fields: int, seed: int) -> np.ndarray:
-    """Order parameters of a periodic Voronoi tessellation.
-
-    ``points`` seeds are drawn uniformly in the box (one stream value per
-    coordinate).  Each cell belongs to the seed nearest by the periodic
-    minimum-image distance (lowest seed index on a tie); ``eta_k = 1`` for
-    ``k = grain % fields`` and 0 otherwise.  Returns shape ``shape + (fields,)``.
-    """
+def voronoi_grain_ids(shape, points: int, seed: int) -> np.ndarray:
+    """Grain index of every cell of a periodic Voronoi tessellation of
+    ``points`` seeds drawn uniformly in the box (one stream value per
+    coordinate): the seed nearest by the periodic minimum-image distance,
+    the lowest index on a tie.  Returns an int64 array of shape ``shape``."""
     shape = tuple(int(s) for s in shape)
     dim = len(shape)
     u = uniform(seed, points * dim).reshape(points, dim)
@@ -65,6 +62,20 @@ def voronoi_grains(shape, points: int, fields: int, seed: int) -> np.ndarray:
             d = np.minimum(d, L[a] - d)
             d2 += d * d
         grain[s:s + chunk] = np.argmin(d2, axis=1)
+    return grain.reshape(shape)
+
+
+def voronoi_grains(shape, points: int, fields: int, seed: int) -> np.ndarray:
+    """Order parameters of a periodic Voronoi tessellation.
+
+    ``points`` seeds are drawn uniformly in the box (one stream value per
+    coordinate).  Each cell belongs to the seed nearest by the periodic
+    minimum-image distance (lowest seed index on a tie); ``eta_k = 1`` for
+    ``k = grain % fields`` and 0 otherwise.  Returns shape ``shape + (fields,)``.
+    """
+    shape = tuple(int(s) for s in shape)
+    ncell = int(np.prod(shape))
+    grain = voronoi_grain_ids(shape, points, seed).ravel()
     eta = np.zeros((ncell, fields), dtype=np.float64)
     eta[np.arange(ncell), grain % fields] = 1.0
     return eta.reshape(shape + (fields,))
@@ -176,11 +187,10 @@ def sparse_grains(shape, points: int, seed: int, capacity: int):
     cells start with one set() each (sparsePF/graingrowth.cpp:14-56).
     Returns (count, index, value) with `capacity` slots per cell."""
     shape = tuple(int(s) for s in shape)
-    e = voronoi_grains(shape, points, points, seed)
     cnt = np.ones(shape, np.int32)
     idx = np.zeros(shape + (capacity,), np.int32)
     val = np.zeros(shape + (capacity,), np.float64)
-    idx[..., 0] = np.argmax(e, axis=-1)
+    idx[..., 0] = voronoi_grain_ids(shape, points, seed)
     val[..., 0] = 1.0
     return cnt, idx, val
 
