@@ -221,7 +221,6 @@ static void release(mmsp_gpu_handle* h)
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (int p = 0; p < 2; p++)
         if (h->cs_graph[p]) cudaGraphExecDestroy(h->cs_graph[p]);
-    if (h->cs_host) cudaFreeHost(h->cs_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->external) return;   // the caller's block and stream
@@ -530,86 +529,38 @@ static int build_graph(mmsp_gpu_handle* h)
 // (cahn-hilliard.cpp:311-388); then the guess becomes the state.
 static const unsigned kCsMaxIter = 10000;    // max_iter, cahn-hilliard.cpp:55
 static const unsigned kCsResidualStep = 5;   // residual_step, cahn-hilliard.cpp:54
-// After iteration kCsResidualStep the checks fall every kCsResidualStep
-// iterations: those chunks (sweeps, residual, read-back into pinned memory)
-// replay one CUDA graph per state buffer, built on first use.
-static int convex_chunk_graph(mmsp_gpu_handle* h, int p)
-{
-    if (h->cs_graph[p]) return MMSP_GPU_OK;
-    cudaError_t e;
-    if (!h->cs_host && (e = cudaHostAlloc((void**)&h->cs_host, 2 * sizeof(double), cudaHostAllocDefault)) != cudaSuccess)
-        return cuda_fail(h, e, "convex pinned buffer");
-    cudaStream_t cs;
-    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(h, e, "graph stream");
-    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
-        cudaStreamDestroy(cs);
-        return cuda_fail(h, e, "begin capture");
-    }
-    const void* old = h->buf[p];
-    void* nw = h->buf[p ^ 1];
-    cudaError_t le = cudaSuccess;
-    for (unsigned k = 0; k < kCsResidualStep && le == cudaSuccess; k++)
-        le = pf::launch_convex_sweeps(h->d, h->g, h->c, old, nw, cs);
-    if (le == cudaSuccess) le = pf::launch_convex_residual(h->d, h->g, h->c, old, nw, h->partials, cs);
-    if (le == cudaSuccess)
-        le = cudaMemcpyAsync(h->cs_host, h->partials + 4 * pf::kReduceBlocks, 2 * sizeof(double),
-                             cudaMemcpyDeviceToHost, cs);
-    cudaGraph_t graph = nullptr;
-    e = cudaStreamEndCapture(cs, &graph);
-    cudaStreamDestroy(cs);
-    if (le != cudaSuccess || e != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        return cuda_fail(h, le != cudaSuccess ? le : e, "convex capture");
-    }
-    e = cudaGraphInstantiate(&h->cs_graph[p], graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
-        h->cs_graph[p] = nullptr;
-        return cuda_fail(h, e, "convex instantiate");
-    }
-    return MMSP_GPU_OK;
-}
+// A step is one CUDA graph per state buffer (pf_convex.cu,
+// build_convex_step_graph): its conditional `while` nodes run the checked
+// iterations and decide on the device, so a call queues one graph launch per
+// step and reads the loop state back once at the end.  The loop state lives
+// in the handle's status block.
+static pf::CsLoop* convex_loop(mmsp_gpu_handle* h) { return reinterpret_cast<pf::CsLoop*>(h->flags + 16); }
 
 static int convex_steps(mmsp_gpu_handle* h, int steps)
 {
     cudaError_t e;
-    double host[2];
+    for (int p = 0; p < 2; p++)
+        if (!h->cs_graph[p] &&
+            (e = pf::build_convex_step_graph(h->d, h->g, h->c, h->buf[p], h->buf[p ^ 1], h->partials, convex_loop(h),
+                                             kCsMaxIter, kCsResidualStep, &h->cs_graph[p])) != cudaSuccess) {
+            h->cs_graph[p] = nullptr;
+            return cuda_fail(h, e, "convex step graph");
+        }
     for (int k = 0; k < steps; k++) {
-        const void* old = h->buf[h->cur];
-        void* nw = h->buf[h->cur ^ 1];
-        double residual = 1.0;
-        unsigned iter = 0;
-        while (iter < kCsMaxIter && residual > h->c.cs.tol) {
-            if (iter >= kCsResidualStep) {   // a whole chunk: iterations iter+1 .. iter+5, check at iter+5
-                int rc = convex_chunk_graph(h, h->cur);
-                if (rc) return rc;
-                if ((e = cudaGraphLaunch(h->cs_graph[h->cur], h->stream)) != cudaSuccess ||
-                    (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
-                    return cuda_fail(h, e, "convex chunk");
-                iter += kCsResidualStep;
-                residual = sqrt(h->cs_host[0] / h->cs_host[1]) / (2.0 * h->c.cs.cells);
-                continue;
-            }
-            if ((e = pf::launch_convex_sweeps(h->d, h->g, h->c, old, nw, h->stream)) != cudaSuccess)
-                return cuda_fail(h, e, "convex sweep");
-            iter++;
-            if (iter < kCsResidualStep || iter % kCsResidualStep == 0) {
-                if ((e = pf::launch_convex_residual(h->d, h->g, h->c, old, nw, h->partials, h->stream)) != cudaSuccess ||
-                    (e = cudaMemcpyAsync(host, h->partials + 4 * pf::kReduceBlocks, sizeof(host), cudaMemcpyDeviceToHost,
-                                         h->stream)) != cudaSuccess ||
-                    (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
-                    return cuda_fail(h, e, "convex residual");
-                residual = sqrt(host[0] / host[1]) / (2.0 * h->c.cs.cells);
-            }
-        }
-        h->last_iters = iter;
-        if (iter == kCsMaxIter) {
-            char msg[64];
-            snprintf(msg, sizeof(msg), "%u iterations, residual %.3g", iter, residual);
-            return fail(h, MMSP_GPU_ENOCONV, "convex splitting stagnated on step %s: %s",
-                        std::to_string(h->steps + k).c_str(), msg);
-        }
+        if ((e = cudaGraphLaunch(h->cs_graph[h->cur], h->stream)) != cudaSuccess) return cuda_fail(h, e, "convex step");
         h->cur ^= 1;   // swap(oldGrid, newGrid), cahn-hilliard.cpp:409
+    }
+    pf::CsLoop L;
+    if ((e = cudaMemcpyAsync(&L, convex_loop(h), sizeof(L), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+        return cuda_fail(h, e, "convex loop state");
+    h->last_iters = L.last_iters;
+    if (L.hit_max) {
+        cudaMemsetAsync(&convex_loop(h)->hit_max, 0, sizeof(int), h->stream);
+        char msg[64];
+        snprintf(msg, sizeof(msg), "%u iterations, residual %.3g", L.last_iters, L.residual);
+        return fail(h, MMSP_GPU_ENOCONV, "convex splitting stagnated within steps %s: %s",
+                    (std::to_string(h->steps) + ".." + std::to_string(h->steps + steps - 1)).c_str(), msg);
     }
     return MMSP_GPU_OK;
 }

@@ -230,23 +230,36 @@ cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchIns
 // steps later and goes back to HBM.  HBM traffic per step falls by about KS
 // times; the price is the halo work, which the autotuner weighs against it.
 //
-// The region is RI x CI floats (compile-time); a block of 256 threads sees it
-// as CI columns x (256 / CI) row groups, each thread walking a run of rows
-// of one column with the rows above and below in registers, so a cell-step
-// costs 3 shared loads and 1 store per pass.  Per cell the arithmetic is
-// the batched kernel's FP32 form.
+// The region is RI x CI floats (compile-time); in the passes a block of 256
+// threads sees it as CI/2 column pairs x (512 / CI) row groups, each thread
+// walking a run of rows of one pair with the pairs above and below in
+// registers, so a pair-step costs 3 shared loads and 1 store per pass, and
+// the arithmetic runs in packed FP32x2 instructions.  Per cell it is the
+// batched kernel's FP32 form.
+// Two adjacent cells per thread in packed FP32x2 arithmetic (one
+// instruction for both cells, and one 8-byte shared access for both).
+static __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+static __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+static __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+static __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+static __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 template <int MODEL>
-static __device__ __forceinline__ float tb_mu(float c, float lap, float kappa, float neg_r, float u)
+static __device__ __forceinline__ float2 tb_mu(float2 c, float2 lap, float kappa, float neg_r, float u)
 {
-    const float fp = MODEL == MMSP_GPU_CH ? c * fmaf(fmaf(4.0f, c, -6.0f), c, 2.0f) : c * fmaf(u, c * c, neg_r);
-    return fmaf(-kappa, lap, fp);
+    const float2 fp = MODEL == MMSP_GPU_CH ? mul2(c, fma2(fma2(f2(4.0f), c, f2(-6.0f)), c, f2(2.0f)))
+                                           : mul2(c, fma2(f2(u), mul2(c, c), f2(neg_r)));
+    return fma2(f2(-kappa), lap, fp);
 }
 
+// lap of cells (y.x, y.y) from the pairs above and below and the cells just
+// left (l) and right (r) of the pair
 template <bool UNIT>
-static __device__ __forceinline__ float tb_lap(float y, float up, float dn, float l, float r, float w0, float w1)
+static __device__ __forceinline__ float2 tb_lap(float2 y, float2 up, float2 dn, float l, float r, float w0, float w1)
 {
-    if (UNIT) return fmaf(-4.0f, y, (dn + up) + (r + l));
-    return fmaf(w0, dn + up, fmaf(w1, r + l, -2.0f * (w0 + w1) * y));
+    const float2 hz = add2(f2(l, y.x), f2(y.y, r));
+    if (UNIT) return fma2(f2(-4.0f), y, add2(add2(dn, up), hz));
+    return fma2(f2(w0), add2(dn, up), fma2(f2(w1), hz, mul2(f2(-2.0f * (w0 + w1)), y)));
 }
 
 template <int RI, int CI, int KS, int MODEL, bool UNIT>
@@ -255,14 +268,18 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
               const float* __restrict__ in, float* __restrict__ out, int* __restrict__ counters, int parity)
 {
     constexpr int H = 2 * KS;
-    constexpr int RG = 256 / CI;
+    constexpr int RG = 256 / CI;         // row groups of the loads and stores (one cell per thread)
+    constexpr int PG = 512 / CI;         // row groups of the passes (a pair of cells per thread)
     static_assert(CI % 32 == 0 && 256 % CI == 0 && RI > 2 * H && CI > 2 * H, "tile shape");
     extern __shared__ __align__(16) float tb_sm[];
     float* C = tb_sm;              // c, updated in place
     float* M = tb_sm + RI * CI;    // mu
     __shared__ int s_item;
     const int t = threadIdx.x;
-    const int col = t % CI, rg = t / CI;
+    const int col = t % CI, rg = t / CI;                    // loads and stores
+    const int pc = 2 * (t % (CI / 2)), pg = t / (CI / 2);  // passes: cells pc, pc+1
+    const int pl = pc == 0 ? 0 : pc - 1;                    // left of the pair (column 0 is never computed)
+    const int pr = pc + 2 == CI ? CI - 1 : pc + 2;          // right of the pair
     if (blockIdx.x == 0 && t == 0) counters[parity ^ 1] = 0;   // for the next launch
     while (true) {
         if (t == 0) s_item = atomicAdd(&counters[parity], 1);
@@ -279,23 +296,31 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
         // (4-byte asynchronous copies: every load of the region is in flight at once)
         if (col < cols) {
             const int gz = wrapi(it.z0 - H + col, bi.n1);
-            for (int r = rg; r < rows; r += RG)
-                cp_async4(&C[r * CI + col], src + (long long)wrapi(it.x0 - H + r, bi.n0) * bi.n1 + gz);
+            int gx = wrapi(it.x0 - H + rg, bi.n0);   // row of region row r, advanced without a division
+            for (int r = rg; r < rows; r += RG) {
+                cp_async4(&C[r * CI + col], src + (long long)gx * bi.n1 + gz);
+                gx += RG;
+                while (gx >= bi.n0) gx -= bi.n0;     // more than once only for grids smaller than a tile
+            }
         }
         cp_async_wait_all();
         __syncthreads();
+        // A pass computes both cells of every pair that meets its column
+        // range; a cell just outside it gets a value that no later cell of
+        // the range reads (the ranges shrink by one cell per pass).
         for (int j = 0; j < KS; j++) {
             // mu on rows [2j+1, rows-2j-1) x cols [2j+1, cols-2j-1)
             {
                 const int a = 2 * j + 1, b = rows - 2 * j - 1;
-                const int h = (b - a + RG - 1) / RG;
-                const int r0 = a + rg * h, r1 = min(b, r0 + h);
-                if (col >= a && col < cols - 2 * j - 1 && r0 < r1) {
-                    float up = C[(r0 - 1) * CI + col], cc = C[r0 * CI + col];
+                const int h = (b - a + PG - 1) / PG;
+                const int r0 = a + pg * h, r1 = min(b, r0 + h);
+                if (pc + 1 >= a && pc < cols - 2 * j - 1 && r0 < r1) {
+                    float2 up = *reinterpret_cast<const float2*>(&C[(r0 - 1) * CI + pc]);
+                    float2 cc = *reinterpret_cast<const float2*>(&C[r0 * CI + pc]);
                     for (int r = r0; r < r1; r++) {
-                        const float dn = C[(r + 1) * CI + col];
-                        const float lap = tb_lap<UNIT>(cc, up, dn, C[r * CI + col - 1], C[r * CI + col + 1], w0, w1);
-                        M[r * CI + col] = tb_mu<MODEL>(cc, lap, kappa, neg_r, u);
+                        const float2 dn = *reinterpret_cast<const float2*>(&C[(r + 1) * CI + pc]);
+                        const float2 lap = tb_lap<UNIT>(cc, up, dn, C[r * CI + pl], C[r * CI + pr], w0, w1);
+                        *reinterpret_cast<float2*>(&M[r * CI + pc]) = tb_mu<MODEL>(cc, lap, kappa, neg_r, u);
                         up = cc;
                         cc = dn;
                     }
@@ -305,14 +330,16 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
             // c' = c + dt*M*lap(mu) on rows [2j+2, rows-2j-2) x cols [2j+2, cols-2j-2), in place
             {
                 const int a = 2 * j + 2, b = rows - 2 * j - 2;
-                const int h = (b - a + RG - 1) / RG;
-                const int r0 = a + rg * h, r1 = min(b, r0 + h);
-                if (col >= a && col < cols - 2 * j - 2 && r0 < r1) {
-                    float up = M[(r0 - 1) * CI + col], mm = M[r0 * CI + col];
+                const int h = (b - a + PG - 1) / PG;
+                const int r0 = a + pg * h, r1 = min(b, r0 + h);
+                if (pc + 1 >= a && pc < cols - 2 * j - 2 && r0 < r1) {
+                    float2 up = *reinterpret_cast<const float2*>(&M[(r0 - 1) * CI + pc]);
+                    float2 mm = *reinterpret_cast<const float2*>(&M[r0 * CI + pc]);
                     for (int r = r0; r < r1; r++) {
-                        const float dn = M[(r + 1) * CI + col];
-                        const float lap = tb_lap<UNIT>(mm, up, dn, M[r * CI + col - 1], M[r * CI + col + 1], w0, w1);
-                        C[r * CI + col] = fmaf(dtm, lap, C[r * CI + col]);
+                        const float2 dn = *reinterpret_cast<const float2*>(&M[(r + 1) * CI + pc]);
+                        const float2 lap = tb_lap<UNIT>(mm, up, dn, M[r * CI + pl], M[r * CI + pr], w0, w1);
+                        float2* cp = reinterpret_cast<float2*>(&C[r * CI + pc]);
+                        *cp = fma2(f2(dtm), lap, *cp);
                         up = mm;
                         mm = dn;
                     }

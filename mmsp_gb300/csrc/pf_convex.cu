@@ -255,4 +255,139 @@ cudaError_t launch_convex_residual(const mmsp_gpu_desc& d, const Geom& g, const 
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// The solve's iteration loop on the device.  The example iterates
+// (cahn-hilliard.cpp:311-388) while iter < max_iter and the residual is above
+// the tolerance, checking the residual after iterations 1-4 and every 5th.
+// A step is one CUDA graph: begin, a `while` node of single iterations (each
+// checked) while iter < 5, a gate, a `while` node of 5-iteration chunks
+// (checked at the end of each), end.  The check kernels compute the same
+// residual expression as a host read-back would (correctly rounded sqrt and
+// division) and set the nodes' conditions, so no step waits on the host.
+
+__global__ void cs_loop_begin(CsLoop* L)
+{
+    L->iter = 0;
+    L->residual = 1.0;
+}
+
+// after `add` iterations: the residual of cs_residual_final's sums, and
+// whether the loop node goes on (iter < limit and residual > tol)
+__global__ void cs_loop_check(const double* __restrict__ partials, int nblocks, CsLoop* L, double tol, double cells,
+                              unsigned add, unsigned limit, cudaGraphConditionalHandle cond)
+{
+    L->iter += add;
+    const double r = sqrt(partials[nblocks * 4 + 0] / partials[nblocks * 4 + 1]) / (2.0 * cells);
+    L->residual = r;
+    cudaGraphSetConditional(cond, (L->iter < limit && r > tol) ? 1u : 0u);
+}
+
+__global__ void cs_loop_gate(const CsLoop* L, double tol, unsigned max_iter, cudaGraphConditionalHandle cond)
+{
+    cudaGraphSetConditional(cond, (L->iter < max_iter && L->residual > tol) ? 1u : 0u);
+}
+
+__global__ void cs_loop_end(CsLoop* L, unsigned max_iter)
+{
+    L->last_iters = L->iter;
+    if (L->iter >= max_iter) L->hit_max = 1;
+}
+
+namespace {
+
+// Append a `while` node on handle `h` after the capture's current
+// dependencies and return its body graph; the capture continues after the node.
+cudaError_t add_while(cudaStream_t cs, cudaGraphConditionalHandle h, cudaGraph_t* body)
+{
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t n = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(cs, &st, nullptr, &g, &deps, nullptr, &n);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams prm = {};
+    prm.type = cudaGraphNodeTypeConditional;
+    prm.conditional.handle = h;
+    prm.conditional.type = cudaGraphCondTypeWhile;
+    prm.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((e = cudaGraphAddNode(&node, g, deps, nullptr, n, &prm)) != cudaSuccess) return e;
+    *body = prm.conditional.phGraph_out[0];
+    return cudaStreamUpdateCaptureDependencies(cs, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+}  // namespace
+
+cudaError_t build_convex_step_graph(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* old, void* nw,
+                                    double* partials, CsLoop* L, unsigned max_iter, unsigned first_checks,
+                                    cudaGraphExec_t* exec)
+{
+    cudaStream_t cs = nullptr, bs = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    const double tol = c.cs.tol, cells = c.cs.cells;
+    bool capturing = e == cudaSuccess;
+    cudaGraphConditionalHandle ha = 0, hb = 0;
+    cudaGraph_t body = nullptr;
+    if (e == cudaSuccess) {
+        // both conditions belong to the graph being captured; the gate sets hb
+        cudaStreamCaptureStatus st;
+        cudaGraph_t top = nullptr;
+        e = cudaStreamGetCaptureInfo(cs, &st, nullptr, &top, nullptr, nullptr, nullptr);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&ha, top, 1, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hb, top, 0, cudaGraphCondAssignDefault);
+    }
+    if (e == cudaSuccess) {
+        cs_loop_begin<<<1, 1, 0, cs>>>(L);
+        e = cudaGetLastError();
+    }
+    // single checked iterations while iter < first_checks
+    if (e == cudaSuccess) e = add_while(cs, ha, &body);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        e = launch_convex_sweeps(d, g, c, old, nw, bs);
+        if (e == cudaSuccess) e = launch_convex_residual(d, g, c, old, nw, partials, bs);
+        if (e == cudaSuccess) {
+            cs_loop_check<<<1, 1, 0, bs>>>(partials, kReduceBlocks, L, tol, cells, 1u, first_checks, ha);
+            e = cudaGetLastError();
+        }
+        cudaGraph_t done = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(bs, &done);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) {
+        cs_loop_gate<<<1, 1, 0, cs>>>(L, tol, max_iter, hb);
+        e = cudaGetLastError();
+    }
+    // then chunks of first_checks iterations, checked at the end of each
+    if (e == cudaSuccess) e = add_while(cs, hb, &body);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (unsigned k = 0; k < first_checks && e == cudaSuccess; k++) e = launch_convex_sweeps(d, g, c, old, nw, bs);
+        if (e == cudaSuccess) e = launch_convex_residual(d, g, c, old, nw, partials, bs);
+        if (e == cudaSuccess) {
+            cs_loop_check<<<1, 1, 0, bs>>>(partials, kReduceBlocks, L, tol, cells, first_checks, max_iter, hb);
+            e = cudaGetLastError();
+        }
+        cudaGraph_t done = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(bs, &done);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) {
+        cs_loop_end<<<1, 1, 0, cs>>>(L, max_iter);
+        e = cudaGetLastError();
+    }
+    if (capturing) {
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (cs) cudaStreamDestroy(cs);
+    if (bs) cudaStreamDestroy(bs);
+    return e;
+}
+
 }  // namespace pf

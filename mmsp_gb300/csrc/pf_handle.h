@@ -44,7 +44,6 @@ struct mmsp_gpu_handle {
     cudaGraphExec_t graph;
     pf::OutputState* out;    // snapshot writer (mmsp_gpu_output), created on first use
     unsigned last_iters;     // MMSP_GPU_CH_CONVEX: solver iterations of the last step
-    cudaGraphExec_t cs_graph[2];   // MMSP_GPU_CH_CONVEX: 5 iterations + residual read-back, per buf[cur]
-    double* cs_host;               // pinned landing place of those read-backs (2 doubles)
+    cudaGraphExec_t cs_graph[2];   // MMSP_GPU_CH_CONVEX: one step (the solve's whole loop), per buf[cur]
     char err[512];
 };

@@ -148,6 +148,21 @@ cudaError_t launch_convex_sweeps(const mmsp_gpu_desc& d, const Geom& g, const Co
                                  void* nw, cudaStream_t s);
 cudaError_t launch_convex_residual(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* old,
                                    const void* nw, double* partials, cudaStream_t s);
+// The iteration loop of one convex-splitting step in device memory: the
+// iteration count and residual of the running solve, the count of the last
+// finished one, and a flag set when a solve reached max_iter.
+struct CsLoop {
+    double residual;
+    unsigned iter, last_iters;
+    int hit_max, pad;
+};
+// One step as a CUDA graph (old -> guess nw): single iterations checked
+// while iter < first_checks, then chunks of first_checks iterations checked
+// at their ends, while the residual is above the tolerance and iter <
+// max_iter; conditional `while` nodes decide on the device.
+cudaError_t build_convex_step_graph(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, const void* old, void* nw,
+                                    double* partials, CsLoop* L, unsigned max_iter, unsigned first_checks,
+                                    cudaGraphExec_t* exec);
 
 // Sparse phase-field grain growth (pf_sparse.cu).  A state buffer holds
 // count[cells] int32 at 0, index[K][cells] int32 at idx_off and
