@@ -39,7 +39,7 @@
 
 namespace {
 
-constexpr int kStreams = 32;       // streams shared round-robin by running requests
+constexpr int kStreams = 128;      // streams shared round-robin by running requests
 constexpr int kInFlight = 2;       // chunks queued ahead per request
 constexpr size_t kGranule = 256;
 

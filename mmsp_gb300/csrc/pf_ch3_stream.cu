@@ -44,12 +44,6 @@ constexpr int kStreamR = PF_CH3_R;   // rows per block strip
 struct F32Coef {
     float wx, wy, wz, w2;   // Laplacian weights, w2 = 2(wx+wy+wz)
     float kappa, dtm, neg_r, u;
-    // Failure-detection test (0 in normal use): > 0 makes this launch's
-    // plane fills expect their bytes without issuing the copies and caps
-    // every wait at that many polls, so the waits run out with no copy in
-    // flight and the launch takes its timed-out exit (error word, drain,
-    // return).  Set from the host by MMSP_GPU_TEST_STALL_LAUNCHES only.
-    int stall;
 };
 
 // A thread's cells: float (one cell) or float2 (two adjacent cells).  float2
@@ -109,7 +103,12 @@ static size_t ch3_smem(int R, int Z, int V)
            sizeof(uint64_t) * kRing;
 }
 
-template <int R, int Z, int V, int MODEL, bool UNIT>
+// STALL: the failure-detection test (never in normal use).  The plane fills
+// expect their bytes without issuing the copies and every wait is capped at
+// 4 polls, so the waits run out with no copy in flight and the launch takes
+// its timed-out exit (error word, bounded drain, return).  The host selects
+// it only through MMSP_GPU_TEST_STALL_LAUNCHES.
+template <int R, int Z, int V, int MODEL, bool UNIT, bool STALL>
 __global__ void __launch_bounds__(Z / V, (Z / V) <= 128 ? PF_CH3_MINB : 1)
 ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, F32Coef q, int planes,
                int* __restrict__ err)
@@ -146,7 +145,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         constexpr uint32_t row = (uint32_t)Z * sizeof(float);
         fence_proxy_async();
         mbar_expect_tx(bar, RR * row);
-        if (q.stall) return;   // failure-detection test: the bytes never arrive
+        if (STALL) return;   // failure-detection test: the bytes never arrive
         const int a = y0 - 2, b = y0 + R + 2;
         if (a >= 0 && b <= g.Y) {
             bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
@@ -163,7 +162,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % kRing) * RR * Z; };
     auto wait_plane = [&](int pl) {
         const int k = pl - x_first;
-        if (!mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, q.stall ? (uint32_t)q.stall : kSpinLimit)) {
+        if (!mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, STALL ? 4u : kSpinLimit)) {
             s_err = 1;
             atomicExch(err, 1);
         }
@@ -272,7 +271,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         // leave no copy in flight: wait (bounded) for every issued fill
         for (int pl = max(x, x_first); pl <= min(x + kRing, x_last); pl++) {
             const int k = pl - x_first;
-            mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, q.stall ? (uint32_t)q.stall : kSpinLimit);
+            mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, STALL ? 4u : kSpinLimit);
         }
     }
 }
@@ -288,13 +287,12 @@ static F32Coef f32coef(const Coeffs& c)
     q.dtm = (float)c.dtm;
     q.neg_r = (float)c.neg_r;
     q.u = (float)c.u;
-    q.stall = 0;
     return q;
 }
 
 // MMSP_GPU_TEST_STALL_LAUNCHES=n: the next n launches of this kernel in the
-// process run the failure-detection test (F32Coef::stall) with waits of 4
-// polls.  Read once; unset in normal use.
+// process run its STALL form (the failure-detection test).  Read once; unset
+// in normal use.
 static std::atomic<int> g_stall_left{-1};
 static int take_stall()
 {
@@ -307,7 +305,7 @@ static int take_stall()
     int cur = g_stall_left.load();
     while (cur > 0 && !g_stall_left.compare_exchange_weak(cur, cur - 1)) {
     }
-    return cur > 0 ? 4 : 0;
+    return cur > 0 ? 1 : 0;
 }
 
 static bool row_ok(int Z) { return Z == 32 || Z == 64 || Z == 128 || Z == 256 || Z == 512; }
@@ -319,27 +317,28 @@ bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
            (d.model == MMSP_GPU_CH || d.model == MMSP_GPU_CH_POLY);
 }
 
-template <int Z, int V, bool UNIT>
+template <int Z, int V, bool UNIT, bool STALL>
 static const void* pick_model(bool ch)
 {
-    return ch ? reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH, UNIT>)
-              : reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH_POLY, UNIT>);
+    return ch ? reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH, UNIT, STALL>)
+              : reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH_POLY, UNIT, STALL>);
 }
 
-template <int Z, int V>
+template <int Z, int V, bool STALL>
 static const void* pick_unit(bool ch, bool unit)
 {
-    return unit ? pick_model<Z, V, true>(ch) : pick_model<Z, V, false>(ch);
+    return unit ? pick_model<Z, V, true, STALL>(ch) : pick_model<Z, V, false, STALL>(ch);
 }
 
+template <bool STALL>
 static const void* pick_stream(int Z, bool ch, bool unit)
 {
     switch (Z) {
-    case 32: return pick_unit<32, 1>(ch, unit);
-    case 64: return pick_unit<64, 2>(ch, unit);
-    case 128: return pick_unit<128, 2>(ch, unit);
-    case 256: return pick_unit<256, 2>(ch, unit);
-    default: return pick_unit<512, 2>(ch, unit);
+    case 32: return pick_unit<32, 1, STALL>(ch, unit);
+    case 64: return pick_unit<64, 2, STALL>(ch, unit);
+    case 128: return pick_unit<128, 2, STALL>(ch, unit);
+    case 256: return pick_unit<256, 2, STALL>(ch, unit);
+    default: return pick_unit<512, 2, STALL>(ch, unit);
     }
 }
 
@@ -348,10 +347,12 @@ cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     const Coeffs c = make_coeffs(d);
     const int V = cells_per_thread(g.Z);
     const int threads = g.Z / V;
-    p->fn = pick_stream(g.Z, d.model == MMSP_GPU_CH, c.unit_w);
+    p->fn = pick_stream<false>(g.Z, d.model == MMSP_GPU_CH, c.unit_w);
+    p->fn2 = pick_stream<true>(g.Z, d.model == MMSP_GPU_CH, c.unit_w);   // the failure-detection test's form
     p->smem = ch3_smem(kStreamR, g.Z, V);
     p->block = dim3(threads, 1, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);
+    if (e == cudaSuccess) e = ensure_smem(p->fn2, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, threads, p->smem);
@@ -376,10 +377,9 @@ cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c,
                               int* err, cudaStream_t s)
 {
     F32Coef q = f32coef(c);
-    q.stall = take_stall();
     int planes = p.planes;
     void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes, (void*)&err};
-    return cudaLaunchKernel(p.fn, p.grid, p.block, args, p.smem, s);
+    return cudaLaunchKernel(take_stall() ? p.fn2 : p.fn, p.grid, p.block, args, p.smem, s);
 }
 
 }  // namespace pf
