@@ -195,7 +195,10 @@ static size_t state_bytes(const mmsp_gpu_desc* d)
 // its two passes (pf_ch64.cu).
 static bool two_pass_f64(const mmsp_gpu_desc* d)
 {
-    return d->dtype == MMSP_GPU_F64 && (d->dim == 2 || d->dim == 3) &&
+    // also the FP32 stochastic 3D Cahn-Hilliard form, whose deviates are drawn once per cell in the mu pass
+    // (in 2D the fused tile kernel, which redraws them on its halo, is faster)
+    const bool noisy32 = d->dtype == MMSP_GPU_F32 && d->model == MMSP_GPU_CH_POLY && d->dim == 3 && pf::noisy(*d);
+    return (d->dtype == MMSP_GPU_F64 || noisy32) && (d->dim == 2 || d->dim == 3) &&
            (d->model == MMSP_GPU_CH || d->model == MMSP_GPU_CH_POLY);
 }
 

@@ -364,7 +364,7 @@ static int set_tb(mmsp_gpu_batch* b, int shape, int ks)
     const size_t smem = tb_smem(shape);
     if ((e = ensure_smem(fn, smem)) != cudaSuccess) return bcuda(b, e, "tile kernel shared memory");
     int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTbShapes[shape].nt, smem)) != cudaSuccess)
         return bcuda(b, e, "occupancy");
     b->tb_blocks = std::max(1, per_sm) * sm_count();
     b->tb_nitems = (int)items.size();
@@ -382,8 +382,8 @@ static cudaError_t step_tb(mmsp_gpu_batch* b, cudaStream_t s, int in, int out)
 {
     const int parity = (int)(b->launches & 1);
     cudaError_t e = launch_tb(tb_kernel(b->tune.shape, b->tune.ks, b->persistent_model, b->unit), b->tb_blocks,
-                              tb_smem(b->tune.shape), b->d_insts, b->d_tb, b->tb_nitems, b->pool[in], b->pool[out],
-                              b->counters, parity, s);
+                              kTbShapes[b->tune.shape].nt, tb_smem(b->tune.shape), b->d_insts, b->d_tb, b->tb_nitems,
+                              b->pool[in], b->pool[out], b->counters, parity, s);
     b->launches++;
     return e;
 }

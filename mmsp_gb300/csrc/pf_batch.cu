@@ -230,8 +230,8 @@ cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchIns
 // steps later and goes back to HBM.  HBM traffic per step falls by about KS
 // times; the price is the halo work, which the autotuner weighs against it.
 //
-// The region is RI x CI floats (compile-time); in the passes a block of 256
-// threads sees it as CI/2 column pairs x (512 / CI) row groups, each thread
+// The region is RI x CI floats (compile-time); in the passes a block of NT
+// (256 or 512) threads sees it as CI/2 column pairs x (2 NT / CI) row groups, each thread
 // walking a run of rows of one pair with the pairs above and below in
 // registers, so a pair-step costs 3 shared loads and 1 store per pass, and
 // the arithmetic runs in packed FP32x2 instructions.  Per cell it is the
@@ -262,15 +262,15 @@ static __device__ __forceinline__ float2 tb_lap(float2 y, float2 up, float2 dn, 
     return fma2(f2(w0), add2(dn, up), fma2(f2(w1), hz, mul2(f2(-2.0f * (w0 + w1)), y)));
 }
 
-template <int RI, int CI, int KS, int MODEL, bool UNIT>
-__global__ void __launch_bounds__(256)
+template <int RI, int CI, int KS, int NT, int MODEL, bool UNIT>
+__global__ void __launch_bounds__(NT)
 ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ items, int nitems,
               const float* __restrict__ in, float* __restrict__ out, int* __restrict__ counters, int parity)
 {
     constexpr int H = 2 * KS;
-    constexpr int RG = 256 / CI;         // row groups of the loads and stores (one cell per thread)
-    constexpr int PG = 512 / CI;         // row groups of the passes (a pair of cells per thread)
-    static_assert(CI % 32 == 0 && 256 % CI == 0 && RI > 2 * H && CI > 2 * H, "tile shape");
+    constexpr int RG = NT / CI;          // row groups of the loads and stores (one cell per thread)
+    constexpr int PG = 2 * NT / CI;      // row groups of the passes (a pair of cells per thread)
+    static_assert(CI % 32 == 0 && NT % CI == 0 && RI > 2 * H && CI > 2 * H, "tile shape");
     extern __shared__ __align__(16) float tb_sm[];
     float* C = tb_sm;              // c, updated in place
     float* M = tb_sm + RI * CI;    // mu
@@ -357,48 +357,55 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
 }
 
 namespace {
-template <int RI, int CI, int KS, int MODEL>
+template <int RI, int CI, int KS, int NT, int MODEL>
 const void* tb_unit(bool unit)
 {
-    return unit ? (const void*)&ch2_tb_kernel<RI, CI, KS, MODEL, true> : (const void*)&ch2_tb_kernel<RI, CI, KS, MODEL, false>;
+    return unit ? (const void*)&ch2_tb_kernel<RI, CI, KS, NT, MODEL, true>
+                : (const void*)&ch2_tb_kernel<RI, CI, KS, NT, MODEL, false>;
 }
-template <int RI, int CI, int KS>
+template <int RI, int CI, int KS, int NT>
 const void* tb_model(int model, bool unit)
 {
-    return model == MMSP_GPU_CH ? tb_unit<RI, CI, KS, MMSP_GPU_CH>(unit) : tb_unit<RI, CI, KS, MMSP_GPU_CH_POLY>(unit);
+    return model == MMSP_GPU_CH ? tb_unit<RI, CI, KS, NT, MMSP_GPU_CH>(unit)
+                                : tb_unit<RI, CI, KS, NT, MMSP_GPU_CH_POLY>(unit);
 }
-template <int RI, int CI>
+template <int RI, int CI, int NT>
 const void* tb_depth(int ks, int model, bool unit)
 {
     switch (ks) {
-    case 2: return tb_model<RI, CI, 2>(model, unit);
-    case 4: return tb_model<RI, CI, 4>(model, unit);
-    case 8: return tb_model<RI, CI, 8>(model, unit);
+    case 2: return tb_model<RI, CI, 2, NT>(model, unit);
+    case 4: return tb_model<RI, CI, 4, NT>(model, unit);
+    case 8: return tb_model<RI, CI, 8, NT>(model, unit);
     default: return nullptr;
     }
 }
 }  // namespace
 
-const TbShape kTbShapes[kTbShapeCount] = {{64, 128}, {96, 128}, {128, 64}};
+const TbShape kTbShapes[kTbShapeCount] = {{64, 128, 256}, {96, 128, 256}, {128, 64, 256},
+                                          {64, 128, 512}, {96, 128, 512}, {128, 64, 512}};
 
 const void* tb_kernel(int shape, int ks, int model, bool unit)
 {
     switch (shape) {
-    case 0: return tb_depth<64, 128>(ks, model, unit);
-    case 1: return tb_depth<96, 128>(ks, model, unit);
-    case 2: return tb_depth<128, 64>(ks, model, unit);
+    case 0: return tb_depth<64, 128, 256>(ks, model, unit);
+    case 1: return tb_depth<96, 128, 256>(ks, model, unit);
+    case 2: return tb_depth<128, 64, 256>(ks, model, unit);
+    case 3: return tb_depth<64, 128, 512>(ks, model, unit);
+    case 4: return tb_depth<96, 128, 512>(ks, model, unit);
+    case 5: return tb_depth<128, 64, 512>(ks, model, unit);
     default: return nullptr;
     }
 }
 
 size_t tb_smem(int shape) { return sizeof(float) * 2 * (size_t)kTbShapes[shape].ri * kTbShapes[shape].ci; }
 
-cudaError_t launch_tb(const void* fn, int blocks, size_t smem, const BatchInst* insts, const TbItem* items, int nitems,
-                      const void* in, void* out, int* counters, int parity, cudaStream_t s)
+cudaError_t launch_tb(const void* fn, int blocks, int threads, size_t smem, const BatchInst* insts,
+                      const TbItem* items, int nitems, const void* in, void* out, int* counters, int parity,
+                      cudaStream_t s)
 {
     void* args[] = {(void*)&insts, (void*)&items, (void*)&nitems, (void*)&in, (void*)&out, (void*)&counters,
                     (void*)&parity};
-    return cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, smem, s);
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(threads), args, smem, s);
 }
 
 }  // namespace pf

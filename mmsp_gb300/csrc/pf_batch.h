@@ -37,19 +37,21 @@ struct TbItem {
     int inst, x0, z0, tx, tz;
 };
 
-// Region shapes (rows x columns, halo included) of the temporally blocked
-// kernel, and the depths (steps per launch) it is built for.
+// Region shapes (rows x columns, halo included, and block size) of the
+// temporally blocked kernel, and the depths (steps per launch) it is built for.
 struct TbShape {
-    int ri, ci;
+    int ri, ci;   // region rows and columns, halo included
+    int nt;       // threads per block
 };
-constexpr int kTbShapeCount = 3;
+constexpr int kTbShapeCount = 6;
 extern const TbShape kTbShapes[kTbShapeCount];
 constexpr int kTbDepths[] = {2, 4, 8};
 
 const void* tb_kernel(int shape, int ks, int model, bool unit);   // FP32 only
 size_t tb_smem(int shape);
-cudaError_t launch_tb(const void* fn, int blocks, size_t smem, const BatchInst* insts, const TbItem* items, int nitems,
-                      const void* in, void* out, int* counters, int parity, cudaStream_t s);
+cudaError_t launch_tb(const void* fn, int blocks, int threads, size_t smem, const BatchInst* insts,
+                      const TbItem* items, int nitems, const void* in, void* out, int* counters, int parity,
+                      cudaStream_t s);
 
 const void* batch_kernel(int dtype, int model, bool unit);
 cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchInst* insts, const BatchItem* items,
