@@ -654,14 +654,17 @@ def batched(native, inputs, stream, reps, flush):
             times.append(e0.elapsed_time(e1))
     ms = float(np.mean(times))
     out32 = [b.download(i).astype(np.float64) for i in range(len(work))]
+    # end to end: inputs from and results to pinned host memory
+    pin_in = [torch.from_numpy(h).pin_memory().numpy() for h in host]
+    pin_out = [torch.empty(h.shape, dtype=torch.float32).pin_memory().numpy() for h in host]
     e2e = []
     for _ in range(max(2, reps // 2)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for i, h in enumerate(host):
+        for i, h in enumerate(pin_in):
             b.upload(i, h)
         b.step(BATCH_STEPS)
-        res = [b.download(i) for i in range(len(work))]
+        res = [b.download(i, pin_out[i]) for i in range(len(work))]
         e2e.append(time.perf_counter() - t0)
     e2e_s = float(np.mean(e2e))
     b.close()
@@ -699,7 +702,7 @@ def batched(native, inputs, stream, reps, flush):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profile_traffic("ch2_tb_f32_256grids" if info.temporal_depth > 1
                                                 else "ch2_batch_f32_256grids"),
-                     "kernel": ("ch2_tb_kernel<%d,%d,%d,CH,unit> (%d steps per launch)" % (
+                     "kernel": ("ch2_tb_kernel<region %dx%d, KS=%d, CH, unit> (%d steps per launch)" % (
                          info.tile_rows, info.tile_cols, info.temporal_depth, info.temporal_depth)
                                 if info.temporal_depth > 1 else "ch2_batch_kernel<float,CH>"),
                      "peak_source": peak_kind, "alg_bytes_per_step": cells * 8,

@@ -321,10 +321,10 @@ int mmsp_gpu_output_wait(mmsp_gpu_handle* h);
  * and, when the environment variable MMSP_GPU_TUNE_CACHE names a file, in
  * that JSON file.  The environment variable MMSP_GPU_BATCH_TILE="depth,shape"
  * replaces the tuning: depth 2, 4 or 8 steps per blocked launch on region
- * shape 0 (64 x 128 cells), 1 (96 x 128) or 2 (128 x 64) with 256-thread
- * blocks, 3, 4 or 5 (the same regions with 512-thread blocks), or "0,0" for
- * the per-step kernel.  Results do not depend on the choice beyond FP32 rounding
- * (the blocked kernel contracts the update into one multiply-add). */
+ * shape 0 (64 x 128 cells, 4 warps), 1 (96 x 128, 4 warps), 2 (128 x 128,
+ * 8 warps) or 3 (128 x 128, 4 warps), or "0,0" for the per-step kernel.
+ * Results do not depend on the choice beyond FP32 rounding (the blocked
+ * kernel contracts the update into one multiply-add). */
 typedef struct mmsp_gpu_batch mmsp_gpu_batch;
 
 typedef struct mmsp_gpu_batch_info {

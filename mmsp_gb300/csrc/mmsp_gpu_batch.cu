@@ -336,7 +336,9 @@ static bool tb_possible(const mmsp_gpu_batch* b)
 static int set_tb(mmsp_gpu_batch* b, int shape, int ks)
 {
     const int H = 2 * ks;
-    const int TX = kTbShapes[shape].ri - 2 * H, TZ = kTbShapes[shape].ci - 2 * H;
+    const int TX = kTbShapes[shape].ri - 2 * H, TZ = kTbCols - 2 * H;
+    for (const auto& bi : b->insts)   // 16-byte groups: rows of a multiple of 4 cells at 16-byte aligned offsets
+        if (bi.n1 % 4 || bi.off % 4) return bfail(b, MMSP_GPU_EUNSUPPORTED, "tile kernel alignment");
     std::vector<TbItem> items;
     for (int i = 0; i < (int)b->insts.size(); i++) {
         const int n0 = b->insts[i].n0, n1 = b->insts[i].n1;
@@ -498,7 +500,7 @@ extern "C" int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force)
         t.threads = 128;
         if (sscanf(fix, "%d,%d", &t.ks, &t.shape) == 2 && t.shape >= 0 && t.shape < kTbShapeCount &&
             (t.ks == 0 || std::find(std::begin(kTbDepths), std::end(kTbDepths), t.ks) != std::end(kTbDepths)) &&
-            4 * t.ks < std::min(kTbShapes[t.shape].ri, kTbShapes[t.shape].ci)) {
+            4 * t.ks < std::min(kTbShapes[t.shape].ri, kTbCols)) {
             int rc = apply_tuning(b, t);
             if (rc) return rc;
             b->tuned = true;
@@ -566,7 +568,7 @@ extern "C" int mmsp_gpu_batch_tune(mmsp_gpu_batch* b, int force)
     if (tb_possible(b)) {
         for (int shape = 0; shape < kTbShapeCount; shape++)
             for (int ks : kTbDepths) {
-                if (2 * 2 * ks >= std::min(kTbShapes[shape].ri, kTbShapes[shape].ci)) continue;   // no interior
+                if (2 * 2 * ks >= std::min(kTbShapes[shape].ri, kTbCols)) continue;   // no interior
                 if ((rc = set_tb(b, shape, ks))) goto done;
                 float ms = 0;
                 e = time2([&] { return step_tb(b, b->stream, b->cur, b->cur ^ 1); }, &ms);
@@ -718,7 +720,7 @@ extern "C" int mmsp_gpu_batch_get_info(const mmsp_gpu_batch* b, mmsp_gpu_batch_i
     info->tune_ms = b->tune_ms;
     info->temporal_depth = b->tune.ks > 0 ? b->tune.ks : 1;
     info->tile_rows = b->tune.ks > 0 ? kTbShapes[b->tune.shape].ri : 0;
-    info->tile_cols = b->tune.ks > 0 ? kTbShapes[b->tune.shape].ci : 0;
+    info->tile_cols = b->tune.ks > 0 ? kTbCols : 0;
     info->tiles = b->tune.ks > 0 ? b->tb_nitems : 0;
     info->device_bytes = 2 * (size_t)b->pool_elems * b->esize + kPartialsBytes + 256 +
                          sizeof(BatchInst) * b->insts.size() + sizeof(BatchItem) * b->items_cap +

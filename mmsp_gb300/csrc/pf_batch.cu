@@ -224,20 +224,33 @@ cudaError_t launch_batch(const void* fn, int blocks, int threads, const BatchIns
 // A work item is a tile of one FP32 instance: an interior of tx x tz cells
 // whose region, widened by a halo of H = 2*KS cells on every side (the
 // Cahn-Hilliard step reads two cells deep: mu of the neighbours), is loaded
-// once into shared memory with periodic wraps.  Each of the KS steps then
-// computes mu on the region minus one more ring and the update on the region
-// minus two, in place, so after KS steps the interior holds the state KS
-// steps later and goes back to HBM.  HBM traffic per step falls by about KS
-// times; the price is the halo work, which the autotuner weighs against it.
+// once into shared memory with periodic wraps.  KS steps then run there in
+// place, each valid on two fewer rings of the region, so after KS steps the
+// interior holds the state KS steps later and goes back to HBM.  HBM traffic
+// per step falls by about KS times; the price is the halo work, which the
+// autotuner weighs against it.
 //
-// The region is RI x CI floats (compile-time); in the passes a block of NT
-// (256 or 512) threads sees it as CI/2 column pairs x (2 NT / CI) row groups, each thread
-// walking a run of rows of one pair with the pairs above and below in
-// registers, so a pair-step costs 3 shared loads and 1 store per pass, and
-// the arithmetic runs in packed FP32x2 instructions.  Per cell it is the
-// batched kernel's FP32 form.
-// Two adjacent cells per thread in packed FP32x2 arithmetic (one
-// instruction for both cells, and one 8-byte shared access for both).
+// The region is RI x 128 floats.  A warp spans a whole region row, 4 cells
+// per lane (16-byte shared accesses); its left and right neighbours come from
+// the adjacent lanes by shuffle.  The warps of a block split the rows of the
+// step's update range into bands; a warp walks its band downwards with c of
+// rows r, r+1 and mu of rows r-1, r in registers: per row it loads c(r+2),
+// computes mu(r+1) and writes c'(r) = c + dt*M*lap(mu) over c(r), so mu never
+// goes to shared memory and is computed twice only on the two rows that
+// border each band.  The two rows on either side of a band belong to the
+// neighbouring bands, which overwrite them, so each warp reads them into
+// registers before a barrier at the start of the step.  Columns are computed
+// over the full width: the outermost column of each side reads a neighbour
+// from the wrong side (lane 0's left, lane 31's right) or a column beyond the
+// tile, and like every cell of the halo this garbage moves inwards by two
+// cells per step, so after KS steps it has not reached the interior
+// [2*KS, cols - 2*KS).  Rows outside the shrinking update range are not
+// written and hold values of earlier steps or tiles, which again only halo
+// cells read.  Loads and stores are 16-byte: batched grids have rows of a
+// multiple of 32 cells at 256-byte aligned offsets, and tile columns start at
+// multiples of 4, so a group of 4 cells never straddles a periodic wrap.
+// Per cell the arithmetic is the batched kernel's FP32 form, in packed FP32x2
+// instructions (one instruction for two cells).
 static __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 static __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 static __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -252,34 +265,65 @@ static __device__ __forceinline__ float2 tb_mu(float2 c, float2 lap, float kappa
     return fma2(f2(-kappa), lap, fp);
 }
 
-// lap of cells (y.x, y.y) from the pairs above and below and the cells just
-// left (l) and right (r) of the pair
+// lap of a lane's 4 cells from the rows above and below; the horizontal
+// neighbour sums are formed by scalar adds (no register pairs to build), the
+// rest in packed FP32x2
 template <bool UNIT>
-static __device__ __forceinline__ float2 tb_lap(float2 y, float2 up, float2 dn, float l, float r, float w0, float w1)
+static __device__ __forceinline__ void tb_lap4(float4 up, float4 cc, float4 dn, float w0, float w1, float2& l01,
+                                               float2& l23)
 {
-    const float2 hz = add2(f2(l, y.x), f2(y.y, r));
-    if (UNIT) return fma2(f2(-4.0f), y, add2(add2(dn, up), hz));
-    return fma2(f2(w0), add2(dn, up), fma2(f2(w1), hz, mul2(f2(-2.0f * (w0 + w1)), y)));
+    const float left = __shfl_up_sync(0xffffffffu, cc.w, 1);
+    const float right = __shfl_down_sync(0xffffffffu, cc.x, 1);
+    const float2 h01 = f2(left + cc.y, cc.x + cc.z), h23 = f2(cc.y + cc.w, cc.z + right);
+    const float2 v01 = add2(f2(up.x, up.y), f2(dn.x, dn.y)), v23 = add2(f2(up.z, up.w), f2(dn.z, dn.w));
+    const float2 c01 = f2(cc.x, cc.y), c23 = f2(cc.z, cc.w);
+    if (UNIT) {
+        l01 = fma2(f2(-4.0f), c01, add2(v01, h01));
+        l23 = fma2(f2(-4.0f), c23, add2(v23, h23));
+    } else {
+        const float2 k = f2(-2.0f * (w0 + w1));
+        l01 = fma2(f2(w0), v01, fma2(f2(w1), h01, mul2(k, c01)));
+        l23 = fma2(f2(w0), v23, fma2(f2(w1), h23, mul2(k, c23)));
+    }
 }
 
-template <int RI, int CI, int KS, int NT, int MODEL, bool UNIT>
-__global__ void __launch_bounds__(NT)
+template <int MODEL, bool UNIT>
+static __device__ __forceinline__ float4 tb_mu4(float4 up, float4 cc, float4 dn, float w0, float w1, float kappa,
+                                                float neg_r, float u)
+{
+    float2 l01, l23;
+    tb_lap4<UNIT>(up, cc, dn, w0, w1, l01, l23);
+    const float2 m01 = tb_mu<MODEL>(f2(cc.x, cc.y), l01, kappa, neg_r, u);
+    const float2 m23 = tb_mu<MODEL>(f2(cc.z, cc.w), l23, kappa, neg_r, u);
+    return make_float4(m01.x, m01.y, m23.x, m23.y);
+}
+
+template <bool UNIT>
+static __device__ __forceinline__ float4 tb_update4(float4 c, float4 up, float4 mm, float4 dn, float w0, float w1,
+                                                    float dtm)
+{
+    float2 l01, l23;
+    tb_lap4<UNIT>(up, mm, dn, w0, w1, l01, l23);
+    const float2 n01 = fma2(f2(dtm), l01, f2(c.x, c.y)), n23 = fma2(f2(dtm), l23, f2(c.z, c.w));
+    return make_float4(n01.x, n01.y, n23.x, n23.y);
+}
+
+template <int RI, int KS, int NW, int MODEL, bool UNIT>
+__global__ void __launch_bounds__(NW * 32)
 ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ items, int nitems,
               const float* __restrict__ in, float* __restrict__ out, int* __restrict__ counters, int parity)
 {
+    constexpr int CI = kTbCols;          // 32 lanes x 4 cells
     constexpr int H = 2 * KS;
-    constexpr int RG = NT / CI;          // row groups of the loads and stores (one cell per thread)
-    constexpr int PG = 2 * NT / CI;      // row groups of the passes (a pair of cells per thread)
-    static_assert(CI % 32 == 0 && NT % CI == 0 && RI > 2 * H && CI > 2 * H, "tile shape");
+    constexpr int NT = NW * 32;
+    constexpr int RG = NT / (CI / 4);    // row groups of the 16-byte loads and stores
+    static_assert(RI > 2 * H && CI > 2 * H && NT % (CI / 4) == 0, "tile shape");
     extern __shared__ __align__(16) float tb_sm[];
-    float* C = tb_sm;              // c, updated in place
-    float* M = tb_sm + RI * CI;    // mu
+    float* C = tb_sm;
     __shared__ int s_item;
     const int t = threadIdx.x;
-    const int col = t % CI, rg = t / CI;                    // loads and stores
-    const int pc = 2 * (t % (CI / 2)), pg = t / (CI / 2);  // passes: cells pc, pc+1
-    const int pl = pc == 0 ? 0 : pc - 1;                    // left of the pair (column 0 is never computed)
-    const int pr = pc + 2 == CI ? CI - 1 : pc + 2;          // right of the pair
+    const int lane = t & 31, warp = t >> 5;
+    const int g = t % (CI / 4), rg = t / (CI / 4);   // loads and stores: cells 4g..4g+3 of rows rg + k*RG
     if (blockIdx.x == 0 && t == 0) counters[parity ^ 1] = 0;   // for the next launch
     while (true) {
         if (t == 0) s_item = atomicAdd(&counters[parity], 1);
@@ -292,112 +336,116 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
         const float kappa = (float)bi.kappa, dtm = (float)bi.dtm, neg_r = (float)bi.neg_r, u = (float)bi.u;
         const float w0 = (float)bi.w0, w1 = (float)bi.w1;
         const float* src = in + bi.off;
-        // the region with periodic wraps (rows of axis 0, columns of axis 1)
-        // (4-byte asynchronous copies: every load of the region is in flight at once)
-        if (col < cols) {
-            const int gz = wrapi(it.z0 - H + col, bi.n1);
+        // the region with periodic wraps (rows of axis 0, columns of axis 1),
+        // every copy in flight at once
+        if (4 * g < cols) {
+            const int gz = wrapi(it.z0 - H + 4 * g, bi.n1);
             int gx = wrapi(it.x0 - H + rg, bi.n0);   // row of region row r, advanced without a division
             for (int r = rg; r < rows; r += RG) {
-                cp_async4(&C[r * CI + col], src + (long long)gx * bi.n1 + gz);
+                cp_async16(&C[r * CI + 4 * g], src + (long long)gx * bi.n1 + gz);
                 gx += RG;
                 while (gx >= bi.n0) gx -= bi.n0;     // more than once only for grids smaller than a tile
             }
         }
         cp_async_wait_all();
         __syncthreads();
-        // A pass computes both cells of every pair that meets its column
-        // range; a cell just outside it gets a value that no later cell of
-        // the range reads (the ranges shrink by one cell per pass).
         for (int j = 0; j < KS; j++) {
-            // mu on rows [2j+1, rows-2j-1) x cols [2j+1, cols-2j-1)
-            {
-                const int a = 2 * j + 1, b = rows - 2 * j - 1;
-                const int h = (b - a + PG - 1) / PG;
-                const int r0 = a + pg * h, r1 = min(b, r0 + h);
-                if (pc + 1 >= a && pc < cols - 2 * j - 1 && r0 < r1) {
-                    float2 up = *reinterpret_cast<const float2*>(&C[(r0 - 1) * CI + pc]);
-                    float2 cc = *reinterpret_cast<const float2*>(&C[r0 * CI + pc]);
-                    for (int r = r0; r < r1; r++) {
-                        const float2 dn = *reinterpret_cast<const float2*>(&C[(r + 1) * CI + pc]);
-                        const float2 lap = tb_lap<UNIT>(cc, up, dn, C[r * CI + pl], C[r * CI + pr], w0, w1);
-                        *reinterpret_cast<float2*>(&M[r * CI + pc]) = tb_mu<MODEL>(cc, lap, kappa, neg_r, u);
-                        up = cc;
-                        cc = dn;
-                    }
-                }
+            const int a = 2 * j + 2, b = rows - 2 * j - 2;   // update rows of step j
+            const int h = (b - a + NW - 1) / NW;
+            const int r0 = a + warp * h, r1 = min(b, r0 + h);
+            auto ld = [&](int r) { return *reinterpret_cast<const float4*>(&C[r * CI + 4 * lane]); };
+            auto put = [&](int r, float4 v) { *reinterpret_cast<float4*>(&C[r * CI + 4 * lane]) = v; };
+            float4 ca, cb, f0, f1;   // c of the two rows above and the two rows below the band
+            if (r0 < r1) {
+                ca = ld(r0 - 2);
+                cb = ld(r0 - 1);
+                f0 = ld(r1);
+                f1 = ld(r1 + 1);
             }
             __syncthreads();
-            // c' = c + dt*M*lap(mu) on rows [2j+2, rows-2j-2) x cols [2j+2, cols-2j-2), in place
-            {
-                const int a = 2 * j + 2, b = rows - 2 * j - 2;
-                const int h = (b - a + PG - 1) / PG;
-                const int r0 = a + pg * h, r1 = min(b, r0 + h);
-                if (pc + 1 >= a && pc < cols - 2 * j - 2 && r0 < r1) {
-                    float2 up = *reinterpret_cast<const float2*>(&M[(r0 - 1) * CI + pc]);
-                    float2 mm = *reinterpret_cast<const float2*>(&M[r0 * CI + pc]);
-                    for (int r = r0; r < r1; r++) {
-                        const float2 dn = *reinterpret_cast<const float2*>(&M[(r + 1) * CI + pc]);
-                        const float2 lap = tb_lap<UNIT>(mm, up, dn, M[r * CI + pl], M[r * CI + pr], w0, w1);
-                        float2* cp = reinterpret_cast<float2*>(&C[r * CI + pc]);
-                        *cp = fma2(f2(dtm), lap, *cp);
-                        up = mm;
-                        mm = dn;
-                    }
+            if (r0 < r1) {   // warp-uniform: the shuffles see the whole warp
+                auto row = [&](int r) { return r < r1 ? ld(r) : r == r1 ? f0 : f1; };
+                // c(r), c(r+1), mu(r-1), mu(r) in registers at row r
+                float4 cA = row(r0), cB = row(r0 + 1);
+                float4 mA = tb_mu4<MODEL, UNIT>(ca, cb, cA, w0, w1, kappa, neg_r, u);
+                float4 mB = tb_mu4<MODEL, UNIT>(cb, cA, cB, w0, w1, kappa, neg_r, u);
+                int r = r0;
+                // three rows per iteration (the register roles come back to
+                // the same places, so no copies), while the rows read are in the band
+                for (; r + 5 <= r1; r += 3) {
+                    const float4 c2 = ld(r + 2);
+                    const float4 m2 = tb_mu4<MODEL, UNIT>(cA, cB, c2, w0, w1, kappa, neg_r, u);
+                    put(r, tb_update4<UNIT>(cA, mA, mB, m2, w0, w1, dtm));
+                    const float4 c3 = ld(r + 3);
+                    const float4 m3 = tb_mu4<MODEL, UNIT>(cB, c2, c3, w0, w1, kappa, neg_r, u);
+                    put(r + 1, tb_update4<UNIT>(cB, mB, m2, m3, w0, w1, dtm));
+                    const float4 c4 = ld(r + 4);
+                    const float4 m4 = tb_mu4<MODEL, UNIT>(c2, c3, c4, w0, w1, kappa, neg_r, u);
+                    put(r + 2, tb_update4<UNIT>(c2, m2, m3, m4, w0, w1, dtm));
+                    cA = c3;
+                    cB = c4;
+                    mA = m3;
+                    mB = m4;
+                }
+                for (; r < r1; r++) {   // the last rows: at most four
+                    const float4 c2 = row(r + 2);
+                    const float4 m2 = tb_mu4<MODEL, UNIT>(cA, cB, c2, w0, w1, kappa, neg_r, u);
+                    put(r, tb_update4<UNIT>(cA, mA, mB, m2, w0, w1, dtm));
+                    cA = cB;
+                    cB = c2;
+                    mA = mB;
+                    mB = m2;
                 }
             }
             __syncthreads();
         }
         // the interior back to HBM
-        if (col >= H && col < H + it.tz) {
-            float* dst = out + bi.off + (it.z0 - H + col);
-            for (int r = H + rg; r < H + it.tx; r += RG) dst[(long long)(it.x0 - H + r) * bi.n1] = C[r * CI + col];
+        if (4 * g >= H && 4 * g < H + it.tz) {
+            float* dst = out + bi.off + (it.z0 - H + 4 * g);
+            for (int r = H + rg; r < H + it.tx; r += RG)
+                *reinterpret_cast<float4*>(dst + (long long)(it.x0 - H + r) * bi.n1) =
+                    *reinterpret_cast<const float4*>(&C[r * CI + 4 * g]);
         }
         __syncthreads();   // the region is reloaded by the next item
     }
 }
 
 namespace {
-template <int RI, int CI, int KS, int NT, int MODEL>
-const void* tb_unit(bool unit)
-{
-    return unit ? (const void*)&ch2_tb_kernel<RI, CI, KS, NT, MODEL, true>
-                : (const void*)&ch2_tb_kernel<RI, CI, KS, NT, MODEL, false>;
-}
-template <int RI, int CI, int KS, int NT>
+template <int RI, int KS, int NW>
 const void* tb_model(int model, bool unit)
 {
-    return model == MMSP_GPU_CH ? tb_unit<RI, CI, KS, NT, MMSP_GPU_CH>(unit)
-                                : tb_unit<RI, CI, KS, NT, MMSP_GPU_CH_POLY>(unit);
+    if (model == MMSP_GPU_CH)
+        return unit ? (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH, true>
+                    : (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH, false>;
+    return unit ? (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH_POLY, true>
+                : (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH_POLY, false>;
 }
-template <int RI, int CI, int NT>
+template <int RI, int NW>
 const void* tb_depth(int ks, int model, bool unit)
 {
     switch (ks) {
-    case 2: return tb_model<RI, CI, 2, NT>(model, unit);
-    case 4: return tb_model<RI, CI, 4, NT>(model, unit);
-    case 8: return tb_model<RI, CI, 8, NT>(model, unit);
+    case 2: return tb_model<RI, 2, NW>(model, unit);
+    case 4: return tb_model<RI, 4, NW>(model, unit);
+    case 8: return tb_model<RI, 8, NW>(model, unit);
     default: return nullptr;
     }
 }
 }  // namespace
 
-const TbShape kTbShapes[kTbShapeCount] = {{64, 128, 256}, {96, 128, 256}, {128, 64, 256},
-                                          {64, 128, 512}, {96, 128, 512}, {128, 64, 512}};
+const TbShape kTbShapes[kTbShapeCount] = {{64, 128}, {96, 128}, {128, 256}, {128, 128}};
 
 const void* tb_kernel(int shape, int ks, int model, bool unit)
 {
     switch (shape) {
-    case 0: return tb_depth<64, 128, 256>(ks, model, unit);
-    case 1: return tb_depth<96, 128, 256>(ks, model, unit);
-    case 2: return tb_depth<128, 64, 256>(ks, model, unit);
-    case 3: return tb_depth<64, 128, 512>(ks, model, unit);
-    case 4: return tb_depth<96, 128, 512>(ks, model, unit);
-    case 5: return tb_depth<128, 64, 512>(ks, model, unit);
+    case 0: return tb_depth<64, 4>(ks, model, unit);
+    case 1: return tb_depth<96, 4>(ks, model, unit);
+    case 2: return tb_depth<128, 8>(ks, model, unit);
+    case 3: return tb_depth<128, 4>(ks, model, unit);
     default: return nullptr;
     }
 }
 
-size_t tb_smem(int shape) { return sizeof(float) * 2 * (size_t)kTbShapes[shape].ri * kTbShapes[shape].ci; }
+size_t tb_smem(int shape) { return sizeof(float) * (size_t)kTbShapes[shape].ri * kTbCols; }
 
 cudaError_t launch_tb(const void* fn, int blocks, int threads, size_t smem, const BatchInst* insts,
                       const TbItem* items, int nitems, const void* in, void* out, int* counters, int parity,

@@ -37,13 +37,16 @@ struct TbItem {
     int inst, x0, z0, tx, tz;
 };
 
-// Region shapes (rows x columns, halo included, and block size) of the
-// temporally blocked kernel, and the depths (steps per launch) it is built for.
+// Region shapes of the temporally blocked kernel (rows, halo included, of
+// kTbCols cells, and block size), and the depths (steps per launch) it is
+// built for.  Its 16-byte loads need rows of a multiple of 4 cells at 16-byte
+// aligned offsets, which batch_eligible grids in the pools have.
+constexpr int kTbCols = 128;
 struct TbShape {
-    int ri, ci;   // region rows and columns, halo included
-    int nt;       // threads per block
+    int ri;   // region rows, halo included
+    int nt;   // threads per block
 };
-constexpr int kTbShapeCount = 6;
+constexpr int kTbShapeCount = 4;
 extern const TbShape kTbShapes[kTbShapeCount];
 constexpr int kTbDepths[] = {2, 4, 8};
 

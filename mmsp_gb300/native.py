@@ -412,8 +412,13 @@ class Batch:
             raise ValueError("shape %s, expected %s" % (a.shape, self._shape(i)))
         _bcheck(self.L.mmsp_gpu_batch_upload(self.b, i, a.ctypes.data, a.nbytes, CELL_MAJOR), self.b, "upload")
 
-    def download(self, i: int) -> np.ndarray:
-        out = np.empty(self._shape(i), dtype=self.dtype)
+    def download(self, i: int, out: np.ndarray = None) -> np.ndarray:
+        """Grid i's state; into `out` (C-contiguous, the grid's shape and
+        dtype, e.g. a view of pinned memory) when given."""
+        if out is None:
+            out = np.empty(self._shape(i), dtype=self.dtype)
+        elif out.shape != self._shape(i) or out.dtype != self.dtype or not out.flags.c_contiguous:
+            raise ValueError("out: expected a C-contiguous %s array of shape %s" % (self.dtype, self._shape(i)))
         _bcheck(self.L.mmsp_gpu_batch_download(self.b, i, out.ctypes.data, out.nbytes, CELL_MAJOR), self.b,
                 "download")
         return out

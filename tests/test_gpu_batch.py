@@ -127,7 +127,8 @@ def test_batch_rejects_mixed_dtypes(gpu):
     assert ei.value.code == gpu.EINVAL
 
 
-TILINGS = [(2, 0), (4, 0), (8, 0), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2), (4, 3), (8, 4), (2, 5), (0, 0)]
+TILINGS = [(2, 0), (4, 0), (8, 0), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2), (8, 2), (2, 3), (4, 3), (8, 3), (0, 0)]
+TILE_SHAPES = [(64, 128), (96, 128), (128, 128), (128, 128)]
 
 
 @pytest.mark.parametrize("ks,shape", TILINGS, ids=["depth%d-shape%d" % t for t in TILINGS])
@@ -153,7 +154,7 @@ def test_batch_temporal_blocking(gpu, oracle, monkeypatch, ks, shape):
         info = b.info()
         assert info.temporal_depth == max(ks, 1)
         if ks:
-            assert (info.tile_rows, info.tile_cols) == [(64, 128), (96, 128), (128, 64)][shape % 3] and info.tiles > 0
+            assert (info.tile_rows, info.tile_cols) == TILE_SHAPES[shape] and info.tiles > 0
         for i, (x, _, p) in enumerate(members):
             got = b.download(i).astype(np.float64)
             want = oracle.ch_baseline(x, 153, p.get("kappa", 1.0), 1.0, 0.004, dx=p.get("dx"))
