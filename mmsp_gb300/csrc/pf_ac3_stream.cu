@@ -14,6 +14,10 @@
 // Laplacian; Y neighbours are registers, X and Z neighbours are read from
 // shared memory (Z wraps across the row).  There is no Z halo, and the Y
 // halo costs 2 extra rows per R-row strip in reads only.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
 #include "pf_async.cuh"
 #include "pf_device.cuh"
 #include "pf_internal.h"
@@ -195,6 +199,189 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
     }
 }
 
+// Rows of Z = 32*V cells (64, 128, 256): one warp per row, V adjacent cells
+// per lane.  The ring, its copies and the strip geometry are those of the
+// kernel above (bulk copies: such rows are 16-byte multiples), with TY rows
+// per strip and one warp each.  Shared reads are V-wide vectors, the Z
+// neighbours at a lane's ends come from the adjacent lanes by shuffle (lane 0
+// and lane 31 are neighbours: the periodic wrap of the row), and the
+// arithmetic runs on pairs of cells in packed FP32x2 instructions; the
+// in-row neighbour sums are scalar adds, which need no pairs built.
+static __device__ __forceinline__ float2 v2(float a, float b) { return make_float2(a, b); }
+static __device__ __forceinline__ float2 v2(float a) { return make_float2(a, a); }
+
+// The update of ac_new_f32 on a pair of cells, with the polynomial terms
+// regrouped into fewer multiply-adds (FP32 rounding differs in the last bits).
+template <int MODEL>
+static __device__ __forceinline__ float2 ac_new_f32x2(float2 c, float2 sum, float2 lap, const AcF32& q)
+{
+    const float2 c2 = __fmul2_rn(c, c);
+    if (MODEL == MMSP_GPU_AC) {
+        // c' = c - dt L (c (gamma2 sum + (1 - gamma2) c^2 - 1) - kappa lap)
+        const float2 df = __fmul2_rn(c, __ffma2_rn(v2(q.gamma2), sum, __ffma2_rn(v2(1.0f - q.gamma2), c2, v2(-1.0f))));
+        return __ffma2_rn(v2(-q.dtm), __ffma2_rn(v2(-q.kappa), lap, df), c);
+    } else if (MODEL == MMSP_GPU_GG || MODEL == MMSP_GPU_ZENER) {
+        // c' = c - dt L (2 (c sum - lap) - c (c^2 + 1))
+        const float2 t = __ffma2_rn(c, sum, __fmul2_rn(lap, v2(-1.0f)));
+        const float2 m = __fmul2_rn(c, __fadd2_rn(c2, v2(1.0f)));
+        return __ffma2_rn(v2(q.dtm), m, __ffma2_rn(v2(-2.0f * q.dtm), t, c));
+    } else {
+        // c' = c - dt L (c (u c^2 - r) - kappa lap)
+        const float2 e = __ffma2_rn(v2(-q.kappa), lap, __fmul2_rn(c, __ffma2_rn(v2(q.u), c2, v2(q.neg_r))));
+        return __ffma2_rn(v2(-q.dtm), e, c);
+    }
+}
+
+template <int V>
+static __device__ __forceinline__ void ldv(const float* p, float (&v)[V])
+{
+    if constexpr (V == 2) {
+        const float2 a = *reinterpret_cast<const float2*>(p);
+        v[0] = a.x;
+        v[1] = a.y;
+    } else {
+#pragma unroll
+        for (int k = 0; k < V; k += 4) {
+            const float4 a = *reinterpret_cast<const float4*>(p + k);
+            v[k] = a.x;
+            v[k + 1] = a.y;
+            v[k + 2] = a.z;
+            v[k + 3] = a.w;
+        }
+    }
+}
+
+template <int V>
+static __device__ __forceinline__ void stv(float* p, const float (&v)[V])
+{
+    if constexpr (V == 2) {
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < V; k += 4) *reinterpret_cast<float4*>(p + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+    }
+}
+
+template <int V, int TY, int MODEL>
+__global__ void __launch_bounds__(32 * TY)
+ac3_vec_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, AcF32 q, int planes, int N, int D,
+            int* __restrict__ err)
+{
+    constexpr int Z = 32 * V, R = TY, RR = R + 2;
+    const int lane = threadIdx.x, w = threadIdx.y;
+    const int tid = lane + 32 * w;
+    extern __shared__ __align__(128) unsigned char sm[];
+    float* slots = reinterpret_cast<float*>(sm);
+    const int chunk = RR * Z;   // floats of one field's rows in a slot
+    const int slot_elems = N * chunk;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(slots + ((D * slot_elems + 1) & ~1));
+
+    const int y0 = blockIdx.x * R;
+    const int xs = blockIdx.y * planes;
+    const int xe = min(xs + planes, g.X);
+    if (xs >= xe) return;
+    const int x_first = xs - 1, x_last = xe;   // planes read from global memory
+    const long long cells = g.cells;
+    const bool row_on = y0 + w < g.Y;           // this warp's row is inside the grid
+
+    auto fill = [&](int pl) {   // thread 0 only
+        const int k = pl - x_first, s = k % D;
+        uint64_t* bar = &bars[s];
+        float* dst0 = slots + s * slot_elems;
+        const long long plane = (long long)wrapi(pl, g.X) * g.YZ;
+        const uint32_t row = (uint32_t)Z * sizeof(float);
+        fence_proxy_async();
+        mbar_expect_tx(bar, (uint32_t)N * RR * row);
+        const int a = y0 - 1, b = y0 + R + 1;
+        for (int f = 0; f < N; f++) {
+            const float* base = ein + (long long)f * cells + plane;
+            float* dst = dst0 + f * chunk;
+            if (a >= 0 && b <= g.Y) {
+                bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
+            } else if (a < 0) {
+                bulk_g2s(dst, base + (long long)(g.Y - 1) * Z, row, bar);
+                bulk_g2s(dst + Z, base, (RR - 1) * row, bar);
+            } else {
+                const int n1 = g.Y - a;
+                bulk_g2s(dst, base + (long long)a * Z, n1 * row, bar);
+                bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
+            }
+        }
+    };
+    auto slot_of = [&](int pl) -> const float* { return slots + ((pl - x_first) % D) * slot_elems; };
+    auto arrived = [&](int pl) {
+        const int k = pl - x_first;
+        return mbar_wait(&bars[k % D], (uint32_t)(k / D) & 1u);
+    };
+
+    if (tid == 0) {
+        for (int s = 0; s < D; s++) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int issued = min(x_first + D - 1, x_last);   // last plane whose fill was issued
+    if (tid == 0)
+        for (int pl = x_first; pl <= issued; pl++) fill(pl);
+    bool bad = !arrived(x_first);
+    bad |= !arrived(x_first + 1);
+    bool stop = __syncthreads_or(bad);   // every thread leaves the loop at the same barrier
+
+    const int lo = (lane + 31) & 31, hi = (lane + 1) & 31;
+    for (int x = xs; x < xe && !stop; x++) {
+        bad = !arrived(x + 1);
+        const float* SL = slot_of(x - 1) + (w + 1) * Z + V * lane;   // own row of the plane below
+        const float* SH = slot_of(x + 1) + (w + 1) * Z + V * lane;   // and above
+        const float* SC = slot_of(x) + w * Z + V * lane;             // the row above the own row of plane x
+        float2 sum[V / 2];
+#pragma unroll
+        for (int k = 0; k < V / 2; k++) sum[k] = v2(0.0f);
+#pragma unroll 2
+        for (int f = 0; f < N; f++) {
+            float c[V];
+            ldv<V>(SC + f * chunk + Z, c);
+#pragma unroll
+            for (int k = 0; k < V / 2; k++) sum[k] = __ffma2_rn(v2(c[2 * k], c[2 * k + 1]), v2(c[2 * k], c[2 * k + 1]), sum[k]);
+        }
+        float* dst = eout + (long long)x * g.YZ + (long long)(y0 + w) * Z + V * lane;
+#pragma unroll 2
+        for (int f = 0; f < N; f++) {
+            const int fo = f * chunk;
+            float up[V], cc[V], dn[V], xl[V], xh[V], out[V];
+            ldv<V>(SC + fo, up);
+            ldv<V>(SC + fo + Z, cc);
+            ldv<V>(SC + fo + 2 * Z, dn);
+            ldv<V>(SL + fo, xl);
+            ldv<V>(SH + fo, xh);
+            const float left = __shfl_sync(0xffffffffu, cc[V - 1], lo);
+            const float right = __shfl_sync(0xffffffffu, cc[0], hi);
+#pragma unroll
+            for (int k = 0; k < V; k += 2) {
+                const float2 c2 = v2(cc[k], cc[k + 1]);
+                const float2 sz = v2((k == 0 ? left : cc[k - 1]) + cc[k + 1], cc[k] + (k + 2 == V ? right : cc[k + 2]));
+                const float2 sx = __fadd2_rn(v2(xl[k], xl[k + 1]), v2(xh[k], xh[k + 1]));
+                const float2 sy = __fadd2_rn(v2(up[k], up[k + 1]), v2(dn[k], dn[k + 1]));
+                const float2 lap = __ffma2_rn(v2(q.wx), sx, __ffma2_rn(v2(q.wy), sy,
+                                              __ffma2_rn(v2(q.wz), sz, __fmul2_rn(v2(-q.w2), c2))));
+                // Zener pinning: the particles (field 0) have zero mobility
+                const float2 nv = (MODEL == MMSP_GPU_ZENER && f == 0) ? c2 : ac_new_f32x2<MODEL>(c2, sum[k / 2], lap, q);
+                out[k] = nv.x;
+                out[k + 1] = nv.y;
+            }
+            if (row_on) stv<V>(dst + (long long)f * cells, out);
+        }
+        stop = __syncthreads_or(bad);
+        if (!stop && x - 1 + D <= x_last) {   // the slot of x-1 is free now
+            if (tid == 0) fill(x - 1 + D);
+            issued = x - 1 + D;
+        }
+    }
+    if (stop) {
+        if (tid == 0) atomicExch(err, 1);
+        // leave no copy in flight: wait (bounded) for the last fill of every slot
+        for (int pl = max(x_first, issued - D + 1); pl <= issued; pl++) arrived(pl);
+    }
+}
+
 // Thread rows per block for a strip of R rows of Z cells and N fields.
 // Measured on 128^3 grids: two thread rows (twice the warps at the same
 // shared memory) win from 8 fields up (47 -> 41 us per step at N = 8,
@@ -280,27 +467,87 @@ static bool ac3_shape(const Geom& g, int N, int* R, int* D)
     return false;
 }
 
+
+template <int V, int TY>
+static const void* acv_pick_model(int model)
+{
+    if (model == MMSP_GPU_AC) return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_AC>;
+    if (model == MMSP_GPU_GG) return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_GG>;
+    if (model == MMSP_GPU_ZENER) return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_ZENER>;
+    return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_AC_POLY>;
+}
+
+template <int V>
+static const void* acv_pick_ty(int ty, int model)
+{
+    if (ty == 4) return acv_pick_model<V, 4>(model);
+    if (ty == 2) return acv_pick_model<V, 2>(model);
+    return nullptr;
+}
+
+// The warp-per-row kernel for rows of 64, 128 or 256 cells: 4-row strips
+// (2 where 4 do not fit) and a ring of 3 slots, or 4 where the 3-slot ring
+// already limits an SM to 3 blocks or fewer and the fourth slot keeps 2
+// blocks, or loses none (measured on 128^3: 8 fields 35.2 -> 33.4 us per step
+// with 4 slots, 16 fields 119.5 -> 103.8; 3 fields 9.8 us with 3 slots
+// against 10.3 with 4).  MMSP_GPU_AC3_SHAPE="rows,depth" (rows 2 or 4, depth
+// 3 to 6) replaces the choice, "0,0" selects the kernel above.
+static const void* acv_plan(const mmsp_gpu_desc& d, const Geom& g, int* R, int* D)
+{
+    if (g.Z != 64 && g.Z != 128 && g.Z != 256) return nullptr;
+    int ty = 4, dd = 0;
+    if (const char* e = getenv("MMSP_GPU_AC3_SHAPE")) {
+        int a = 0, b = 0;
+        if (sscanf(e, "%d,%d", &a, &b) == 2) {
+            if (a == 0) return nullptr;
+            if ((a == 2 || a == 4) && b >= 3 && b <= 6) {
+                ty = a;
+                dd = b;
+            }
+        }
+    }
+    const int fix = dd;
+    if (!fix) dd = 3;
+    while (ty > 2 && (g.Y < ty + 2 || ac3_smem(ty, g.Z, d.fields, dd) > kAcSmemCap)) ty /= 2;
+    if (g.Y < ty + 2 || ac3_smem(ty, g.Z, d.fields, dd) > kAcSmemCap) return nullptr;
+    if (!fix && ac3_smem(ty, g.Z, d.fields, 4) <= kAcSmemCap) {
+        const int b3 = ac3_blocks_per_sm(ac3_smem(ty, g.Z, d.fields, 3));
+        const int b4 = ac3_blocks_per_sm(ac3_smem(ty, g.Z, d.fields, 4));
+        if (b3 <= 3 && (b4 >= 2 || b4 == b3)) dd = 4;
+    }
+    *R = ty;
+    *D = dd;
+    const int V = g.Z / 32;
+    return V == 2 ? acv_pick_ty<2>(ty, d.model) : V == 4 ? acv_pick_ty<4>(ty, d.model) : acv_pick_ty<8>(ty, d.model);
+}
+
 bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
     int R, D;
     return d.dtype == MMSP_GPU_F32 && g.dim == 3 && g.Z <= 256 &&
            (d.model == MMSP_GPU_AC || d.model == MMSP_GPU_GG || d.model == MMSP_GPU_AC_POLY ||
             d.model == MMSP_GPU_ZENER) &&
-           ac3_shape(g, d.fields, &R, &D);
+           (acv_plan(d, g, &R, &D) || ac3_shape(g, d.fields, &R, &D));
 }
 
 cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     int R = 4, D = 4;
-    ac3_shape(g, d.fields, &R, &D);
-    int RT, TY;
-    ac3_threads(R, g.Z, d.fields, &RT, &TY);
-    const int zt = (g.Z + 31) / 32 * 32;
-    const int threads = zt * TY;
-    p->fn = ac3_pick(RT, TY, g.Z, d.model);   // bulk copies when rows are 16-byte multiples
-    if (!p->fn) return cudaErrorInvalidConfiguration;
+    int threads;
+    if ((p->fn = acv_plan(d, g, &R, &D))) {
+        threads = 32 * R;
+        p->block = dim3(32, R, 1);
+    } else {
+        ac3_shape(g, d.fields, &R, &D);
+        int RT, TY;
+        ac3_threads(R, g.Z, d.fields, &RT, &TY);
+        const int zt = (g.Z + 31) / 32 * 32;
+        threads = zt * TY;
+        p->fn = ac3_pick(RT, TY, g.Z, d.model);   // bulk copies when rows are 16-byte multiples
+        if (!p->fn) return cudaErrorInvalidConfiguration;
+        p->block = dim3(zt, TY, 1);
+    }
     p->smem = ac3_smem(R, g.Z, d.fields, D);
-    p->block = dim3(zt, TY, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;

@@ -443,6 +443,22 @@ def test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, m
     assert np.abs(want - x).max() > 1e-3
 
 
+# Rows of 64, 128 and 256 cells take the warp-per-row form of the streaming
+# kernel; MMSP_GPU_AC3_SHAPE fixes its strip rows and ring depth ("0,0": the
+# per-cell form): 2- and 4-row strips (Y = 4, 5 fall back to 2 rows), rings of
+# 3 to 6 slots, partial strips and Y wraps, every model.
+AC_VEC = [("2,3", (7, 9, 64), 3, "ac"), ("2,5", (5, 11, 128), 8, "gg"), ("4,6", (6, 13, 128), 4, "zener"),
+          ("4,4", (4, 6, 256), 6, "ac"), ("0,0", (5, 9, 128), 8, "ac"), ("4,3", (3, 5, 128), 1, "ac_poly"),
+          ("4,4", (9, 4, 64), 16, "gg"), ("2,4", (4, 14, 256), 12, "ac")]
+
+
+@pytest.mark.parametrize("tile,shape,fields,model", AC_VEC,
+                         ids=["%s-%s-%d-%s" % (t, "x".join(map(str, s)), f, m) for t, s, f, m in AC_VEC])
+def test_fp32_ac_row_warp_kernel_shapes(gpu, oracle, monkeypatch, tile, shape, fields, model):
+    monkeypatch.setenv("MMSP_GPU_AC3_SHAPE", tile)
+    test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, model)
+
+
 # FP32 Cahn-Hilliard grids whose rows are not 32..512 cells in powers of two
 # take the row kernel (any row length, plain loads): 2D rows of odd lengths
 # up to 1024, 3D grids with few rows per plane and odd rows.
