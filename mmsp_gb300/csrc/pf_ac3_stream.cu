@@ -199,10 +199,13 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
     }
 }
 
-// Rows of Z = 32*V cells (64, 128, 256): one warp per row, V adjacent cells
+// Rows of Z = 32*V cells (64, 128, 256): a warp spans a row, V adjacent cells
 // per lane.  The ring, its copies and the strip geometry are those of the
 // kernel above (bulk copies: such rows are 16-byte multiples), with TY rows
-// per strip and one warp each.  Shared reads are V-wide vectors, the Z
+// per strip and FG warps per row that take every FG-th field (each sums the
+// squares of all fields of its cells): FG times the warps at the same shared
+// memory, to hide the latency of each warp's dependent loads and arithmetic.
+// Shared reads are V-wide vectors, the Z
 // neighbours at a lane's ends come from the adjacent lanes by shuffle (lane 0
 // and lane 31 are neighbours: the periodic wrap of the row), and the
 // arithmetic runs on pairs of cells in packed FP32x2 instructions; the
@@ -262,14 +265,14 @@ static __device__ __forceinline__ void stv(float* p, const float (&v)[V])
     }
 }
 
-template <int V, int TY, int MODEL>
-__global__ void __launch_bounds__(32 * TY)
+template <int V, int TY, int FG, int MODEL>
+__global__ void __launch_bounds__(32 * TY * FG)
 ac3_vec_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, AcF32 q, int planes, int N, int D,
             int* __restrict__ err)
 {
     constexpr int Z = 32 * V, R = TY, RR = R + 2;
-    const int lane = threadIdx.x, w = threadIdx.y;
-    const int tid = lane + 32 * w;
+    const int lane = threadIdx.x, w = threadIdx.y, fg = FG > 1 ? threadIdx.z : 0;
+    const int tid = lane + 32 * (w + TY * fg);
     extern __shared__ __align__(128) unsigned char sm[];
     float* slots = reinterpret_cast<float*>(sm);
     const int chunk = RR * Z;   // floats of one field's rows in a slot
@@ -332,19 +335,33 @@ ac3_vec_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, AcF
         const float* SL = slot_of(x - 1) + (w + 1) * Z + V * lane;   // own row of the plane below
         const float* SH = slot_of(x + 1) + (w + 1) * Z + V * lane;   // and above
         const float* SC = slot_of(x) + w * Z + V * lane;             // the row above the own row of plane x
-        float2 sum[V / 2];
+        // two accumulators (even and odd fields): two independent chains
+        float2 sum[V / 2], sum1[V / 2];
 #pragma unroll
-        for (int k = 0; k < V / 2; k++) sum[k] = v2(0.0f);
+        for (int k = 0; k < V / 2; k++) sum[k] = sum1[k] = v2(0.0f);
+        int f0 = 0;
 #pragma unroll 2
-        for (int f = 0; f < N; f++) {
+        for (; f0 + 1 < N; f0 += 2) {
+            float c[V], e[V];
+            ldv<V>(SC + f0 * chunk + Z, c);
+            ldv<V>(SC + (f0 + 1) * chunk + Z, e);
+#pragma unroll
+            for (int k = 0; k < V / 2; k++) {
+                sum[k] = __ffma2_rn(v2(c[2 * k], c[2 * k + 1]), v2(c[2 * k], c[2 * k + 1]), sum[k]);
+                sum1[k] = __ffma2_rn(v2(e[2 * k], e[2 * k + 1]), v2(e[2 * k], e[2 * k + 1]), sum1[k]);
+            }
+        }
+        if (f0 < N) {
             float c[V];
-            ldv<V>(SC + f * chunk + Z, c);
+            ldv<V>(SC + f0 * chunk + Z, c);
 #pragma unroll
             for (int k = 0; k < V / 2; k++) sum[k] = __ffma2_rn(v2(c[2 * k], c[2 * k + 1]), v2(c[2 * k], c[2 * k + 1]), sum[k]);
         }
+#pragma unroll
+        for (int k = 0; k < V / 2; k++) sum[k] = __fadd2_rn(sum[k], sum1[k]);
         float* dst = eout + (long long)x * g.YZ + (long long)(y0 + w) * Z + V * lane;
 #pragma unroll 2
-        for (int f = 0; f < N; f++) {
+        for (int f = fg; f < N; f += FG) {
             const int fo = f * chunk;
             float up[V], cc[V], dn[V], xl[V], xh[V], out[V];
             ldv<V>(SC + fo, up);
@@ -468,41 +485,53 @@ static bool ac3_shape(const Geom& g, int N, int* R, int* D)
 }
 
 
-template <int V, int TY>
+template <int V, int TY, int FG>
 static const void* acv_pick_model(int model)
 {
-    if (model == MMSP_GPU_AC) return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_AC>;
-    if (model == MMSP_GPU_GG) return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_GG>;
-    if (model == MMSP_GPU_ZENER) return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_ZENER>;
-    return (const void*)&ac3_vec_f32<V, TY, MMSP_GPU_AC_POLY>;
+    if (model == MMSP_GPU_AC) return (const void*)&ac3_vec_f32<V, TY, FG, MMSP_GPU_AC>;
+    if (model == MMSP_GPU_GG) return (const void*)&ac3_vec_f32<V, TY, FG, MMSP_GPU_GG>;
+    if (model == MMSP_GPU_ZENER) return (const void*)&ac3_vec_f32<V, TY, FG, MMSP_GPU_ZENER>;
+    return (const void*)&ac3_vec_f32<V, TY, FG, MMSP_GPU_AC_POLY>;
+}
+
+template <int V, int TY>
+static const void* acv_pick_fg(int fg, int model)
+{
+    if (fg == 4) return acv_pick_model<V, TY, 4>(model);
+    if (fg == 2) return acv_pick_model<V, TY, 2>(model);
+    return acv_pick_model<V, TY, 1>(model);
 }
 
 template <int V>
-static const void* acv_pick_ty(int ty, int model)
+static const void* acv_pick_ty(int ty, int fg, int model)
 {
-    if (ty == 4) return acv_pick_model<V, 4>(model);
-    if (ty == 2) return acv_pick_model<V, 2>(model);
+    if (ty == 4) return acv_pick_fg<V, 4>(fg, model);
+    if (ty == 2) return acv_pick_fg<V, 2>(fg, model);
     return nullptr;
 }
 
 // The warp-per-row kernel for rows of 64, 128 or 256 cells: 4-row strips
 // (2 where 4 do not fit) and a ring of 3 slots, or 4 where the 3-slot ring
 // already limits an SM to 3 blocks or fewer and the fourth slot keeps 2
-// blocks, or loses none (measured on 128^3: 8 fields 35.2 -> 33.4 us per step
-// with 4 slots, 16 fields 119.5 -> 103.8; 3 fields 9.8 us with 3 slots
-// against 10.3 with 4).  MMSP_GPU_AC3_SHAPE="rows,depth" (rows 2 or 4, depth
-// 3 to 6) replaces the choice, "0,0" selects the kernel above.
-static const void* acv_plan(const mmsp_gpu_desc& d, const Geom& g, int* R, int* D)
+// blocks, or loses none; two warps per row from 8 fields up.  Measured on
+// 128^3, us per step: 8 fields 35.1 (3 slots), 32.9 (4 slots), 31.9 (4 slots,
+// 2 warps per row); 16 fields 114.5, 100.7, 87.0; 3 fields 10.1 (3 slots),
+// 10.6 (4), 14.6 (3 slots, 2 warps per row).  MMSP_GPU_AC3_SHAPE=
+// "rows,depth[,warps per row]" (rows 2 or 4, depth 3 to 6, warps 1, 2 or 4)
+// replaces the choice, "0,0" selects the kernel above.
+static const void* acv_plan(const mmsp_gpu_desc& d, const Geom& g, int* R, int* D, int* FG)
 {
     if (g.Z != 64 && g.Z != 128 && g.Z != 256) return nullptr;
-    int ty = 4, dd = 0;
+    int ty = 4, dd = 0, fg = d.fields >= 8 ? 2 : 1;
     if (const char* e = getenv("MMSP_GPU_AC3_SHAPE")) {
-        int a = 0, b = 0;
-        if (sscanf(e, "%d,%d", &a, &b) == 2) {
+        int a = 0, b = 0, c = 0;
+        const int n = sscanf(e, "%d,%d,%d", &a, &b, &c);
+        if (n >= 2) {
             if (a == 0) return nullptr;
             if ((a == 2 || a == 4) && b >= 3 && b <= 6) {
                 ty = a;
                 dd = b;
+                fg = n == 3 && (c == 1 || c == 2 || c == 4) ? c : 1;
             }
         }
     }
@@ -518,25 +547,27 @@ static const void* acv_plan(const mmsp_gpu_desc& d, const Geom& g, int* R, int* 
     *R = ty;
     *D = dd;
     const int V = g.Z / 32;
-    return V == 2 ? acv_pick_ty<2>(ty, d.model) : V == 4 ? acv_pick_ty<4>(ty, d.model) : acv_pick_ty<8>(ty, d.model);
+    *FG = fg;
+    return V == 2 ? acv_pick_ty<2>(ty, fg, d.model) : V == 4 ? acv_pick_ty<4>(ty, fg, d.model)
+                  : acv_pick_ty<8>(ty, fg, d.model);
 }
 
 bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
-    int R, D;
+    int R, D, FG;
     return d.dtype == MMSP_GPU_F32 && g.dim == 3 && g.Z <= 256 &&
            (d.model == MMSP_GPU_AC || d.model == MMSP_GPU_GG || d.model == MMSP_GPU_AC_POLY ||
             d.model == MMSP_GPU_ZENER) &&
-           (acv_plan(d, g, &R, &D) || ac3_shape(g, d.fields, &R, &D));
+           (acv_plan(d, g, &R, &D, &FG) || ac3_shape(g, d.fields, &R, &D));
 }
 
 cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
-    int R = 4, D = 4;
+    int R = 4, D = 4, FG = 1;
     int threads;
-    if ((p->fn = acv_plan(d, g, &R, &D))) {
-        threads = 32 * R;
-        p->block = dim3(32, R, 1);
+    if ((p->fn = acv_plan(d, g, &R, &D, &FG))) {
+        threads = 32 * R * FG;
+        p->block = dim3(32, R, FG);
     } else {
         ac3_shape(g, d.fields, &R, &D);
         int RT, TY;
