@@ -85,6 +85,13 @@ static __device__ __forceinline__ void cp_async4(void* dst, const void* src)
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
 
+// Per-thread asynchronous 8-byte copy global -> shared (both addresses
+// 8-byte aligned).
+static __device__ __forceinline__ void cp_async8(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
 // Per-thread asynchronous 16-byte copy global -> shared (both addresses
 // 16-byte aligned), cached in L2 only.
 static __device__ __forceinline__ void cp_async16(void* dst, const void* src)

@@ -1,21 +1,26 @@
 // pf_ch3_stream.cu -- FP32 3D Cahn-Hilliard step, register streaming along X.
 //
-// The precision-form kernel for 3D grids whose rows (axis Z) hold 32, 64,
-// 128, 256 or 512 cells.  A block owns R consecutive rows (axis Y) of full
-// Z extent and a run of X planes; each thread owns V adjacent cells of a
-// row (V = 1 for 32-cell rows, else 2), so the block has Z/V threads.
+// The precision-form kernel for 3D grids whose rows (axis Z) hold an even
+// number of cells up to 512.  A block owns R consecutive rows (axis Y) of
+// full Z extent and a run of X planes; each thread owns V adjacent cells of
+// a row (V = 1 for 32-cell rows, else 2), so the block has Z/V threads,
+// rounded up to whole warps (the threads past the row's end compute on
+// copies of its last cells and store nothing).
 //
 // For every plane the block's R+4 rows (2 halo rows on each side, wrapped
-// periodically) arrive in shared memory through cp.async.bulk on an
-// mbarrier ring, several planes ahead of the one being computed.  Each
-// thread keeps its cells of c for planes x, x+1, x+2 and of mu for x-1, x,
-// x+1 in registers: Y neighbours are neighbouring registers, X neighbours
-// the neighbouring planes' registers, Z neighbours inside a thread are
-// registers, Z neighbours across threads come from shared memory (c) or
-// warp shuffles (mu), and the two cells at each warp's ends exchange mu
-// through a small shared array that wraps periodically across the row.
-// mu is recomputed only on the 2 halo rows of the strip; a block spans whole
-// rows, so there is no Z halo.
+// periodically) arrive in shared memory on an mbarrier ring, several planes
+// ahead of the one being computed: by cp.async.bulk where rows are 16-byte
+// multiples, by per-thread 8-byte cp.async otherwise.  Each thread keeps its
+// cells of c for planes x, x+1, x+2 and of mu for x-1, x, x+1 in registers:
+// Y neighbours are neighbouring registers, X neighbours the neighbouring
+// planes' registers, Z neighbours inside a thread are registers, Z
+// neighbours across threads come from shared memory (c) or warp shuffles
+// (mu), and the first and last cells of each warp exchange mu through a small
+// shared array that wraps periodically across the row (the last warp's last
+// cell is the row's last cell, wherever the row ends in that warp).  mu is
+// recomputed only on the 2 halo rows of the strip; a block spans whole rows,
+// so there is no Z halo.  Rows of 32..512 cells in powers of two have
+// compile-time instances (row offsets become immediates).
 //
 // FP32 arithmetic is reassociated for throughput (six-neighbour sums and
 // Horner's form of f'(c)); the result is checked against the FP64 oracle
@@ -94,11 +99,14 @@ static __device__ __forceinline__ VT lap_v(VT sx, VT sy, VT sz, VT c, const F32C
     return vfma(vset<VT>(q.wx), sx, vfma(vset<VT>(q.wy), sy, vfma(vset<VT>(q.wz), sz, vmul(vset<VT>(-q.w2), c))));
 }
 
+// Threads of a block for rows of Z cells, V per thread: whole warps.
+static int ch3_threads(int Z, int V) { return (Z / V + 31) / 32 * 32; }
+
 // Shared memory: kRing slots of (R+4) x Z floats, the warp-end mu buffers
 // [parity][warp][side][R], then kRing mbarriers.
 static size_t ch3_smem(int R, int Z, int V)
 {
-    int warps = Z / V / 32;
+    const int warps = ch3_threads(Z, V) / 32;
     return sizeof(float) * (size_t)kRing * (R + 4) * Z + sizeof(float) * 2 * warps * 2 * R +
            sizeof(uint64_t) * kRing;
 }
@@ -108,18 +116,28 @@ static size_t ch3_smem(int R, int Z, int V)
 // 4 polls, so the waits run out with no copy in flight and the launch takes
 // its timed-out exit (error word, bounded drain, return).  The host selects
 // it only through MMSP_GPU_TEST_STALL_LAUNCHES.
-template <int R, int Z, int V, int MODEL, bool UNIT, bool STALL>
-__global__ void __launch_bounds__(Z / V, (Z / V) <= 128 ? PF_CH3_MINB : 1)
+// ZT: the row length when it is a compile-time constant (32..512 in powers
+// of two, ZT / V = TM threads), 0 when it is taken from the grid (a multiple
+// of V; blockDim.x = ch3_threads(Z, V) <= TM).  BULK: rows are 16-byte
+// multiples and thread 0 stages each plane with cp.async.bulk (one arrival,
+// transaction-counted); otherwise every thread copies its cells with 4- or
+// 8-byte cp.async and arrives when they land.
+template <int R, int ZT, int TM, int V, int MODEL, bool UNIT, bool STALL, bool BULK>
+__global__ void __launch_bounds__(TM, TM <= 128 ? PF_CH3_MINB : (V == 1 && TM == 256 ? 2 : 1))
 ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, F32Coef q, int planes,
                int* __restrict__ err)
 {
     constexpr int RR = R + 4;
-    constexpr int T = Z / V;             // threads per block
-    constexpr int W = T / 32;            // warps per block (one row)
-    static_assert(T % 32 == 0 && R % 4 == 0, "row split");
+    static_assert(TM % 32 == 0 && R % 4 == 0 && (!ZT || ZT == TM * V), "row split");
+    const int Z = ZT ? ZT : g.Z;
+    const int W = ZT ? TM / 32 : (int)(blockDim.x >> 5);   // warps per block
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
-    const int z0 = t * V;                // first cell of this thread
+    const int tl = Z / V - 1;            // the thread holding the row's last cells
+    const bool real = ZT || t <= tl;     // past the row's end: compute on the last cells, store nothing
+    const int z0 = (real ? t : tl) * V;  // first cell of this thread
+    const int wlast = W - 1;             // (whole warps: the last warp holds the row's last cells)
+    const int lane_last = warp == wlast ? (ZT ? 31 : tl & 31) : 31;   // this warp's last real lane
     extern __shared__ __align__(128) unsigned char sm[];
     float* slots = reinterpret_cast<float*>(sm);
     float* edges = slots + (size_t)kRing * RR * Z;
@@ -132,31 +150,42 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     if (xs >= xe) return;
     const int zl = z0 == 0 ? Z - 1 : z0 - 1;            // cell left of this thread's first
     const int zh = z0 + V == Z ? 0 : z0 + V;            // cell right of this thread's last
-    const int wl = warp == 0 ? W - 1 : warp - 1;
-    const int wh = warp == W - 1 ? 0 : warp + 1;
+    const int wl = warp == 0 ? wlast : warp - 1;
+    const int wh = warp == wlast ? 0 : warp + 1;
     const int x_first = xs - 2, x_last = xe + 1;        // planes read from global memory
 
-    // producer (thread 0): stage plane pl (wrapped) into its ring slot
+    // stage plane pl (wrapped) into its ring slot: thread 0 (BULK) or every thread
     auto fill = [&](int pl) {
         const int k = pl - x_first, s = k % kRing;
         uint64_t* bar = &bars[s];
         float* dst = slots + (size_t)s * RR * Z;
         const float* base = cin + (long long)wrapi(pl, g.X) * g.YZ;
-        constexpr uint32_t row = (uint32_t)Z * sizeof(float);
-        fence_proxy_async();
-        mbar_expect_tx(bar, RR * row);
-        if (STALL) return;   // failure-detection test: the bytes never arrive
-        const int a = y0 - 2, b = y0 + R + 2;
-        if (a >= 0 && b <= g.Y) {
-            bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
-        } else if (a < 0) {
-            const int n1 = -a;   // rows Y-n1 .. Y-1 first, then 0 ..
-            bulk_g2s(dst, base + (long long)(g.Y - n1) * Z, n1 * row, bar);
-            bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
+        if constexpr (BULK) {
+            const uint32_t row = (uint32_t)Z * sizeof(float);
+            fence_proxy_async();
+            mbar_expect_tx(bar, RR * row);
+            if (STALL) return;   // failure-detection test: the bytes never arrive
+            const int a = y0 - 2, b = y0 + R + 2;
+            if (a >= 0 && b <= g.Y) {
+                bulk_g2s(dst, base + (long long)a * Z, RR * row, bar);
+            } else if (a < 0) {
+                const int n1 = -a;   // rows Y-n1 .. Y-1 first, then 0 ..
+                bulk_g2s(dst, base + (long long)(g.Y - n1) * Z, n1 * row, bar);
+                bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
+            } else {
+                const int n1 = g.Y - a;   // rows a .. Y-1, then 0 ..
+                bulk_g2s(dst, base + (long long)a * Z, n1 * row, bar);
+                bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
+            }
         } else {
-            const int n1 = g.Y - a;   // rows a .. Y-1, then 0 ..
-            bulk_g2s(dst, base + (long long)a * Z, n1 * row, bar);
-            bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, bar);
+            if (STALL) return;   // no copies and no arrivals: the waits run out
+            if (real)
+                for (int i = 0; i < RR; i++) {
+                    const float* src = base + (long long)wrapi(y0 - 2 + i, g.Y) * Z + z0;
+                    if (V == 2) cp_async8(dst + i * Z + z0, src);
+                    else cp_async4(dst + i * Z + z0, src);
+                }
+            cp_async_arrive(bar);
         }
     };
     auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % kRing) * RR * Z; };
@@ -169,12 +198,12 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     };
 
     if (t == 0) {
-        for (int s = 0; s < kRing; s++) mbar_init(&bars[s], 1);
+        for (int s = 0; s < kRing; s++) mbar_init(&bars[s], BULK ? 1 : (int)blockDim.x);
         mbar_fence_init();
         s_err = 0;
     }
     __syncthreads();
-    if (t == 0)
+    if (!BULK || t == 0)   // (evaluated where used: a flag held across the loop costs registers)
         for (int pl = x_first; pl < x_first + kRing && pl <= x_last; pl++) fill(pl);
 
     using VT = typename Cells<V>::type;
@@ -194,7 +223,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
 #pragma unroll
     for (int i = 0; i < R + 2; i++) mA[i] = mB[i] = vset<VT>(0.0f);
     __syncthreads();
-    if (t == 0 && !s_err && x_first + kRing <= x_last) fill(x_first + kRing);   // slot of x_first is free
+    if ((!BULK || t == 0) && !s_err && x_first + kRing <= x_last) fill(x_first + kRing);   // slot of x_first is free
 
     // One plane: a = c(x), b = c(x+1), c = c(x+2) (loaded here); ma = mu(x-1),
     // mb = mu(x), mc = mu(x+1) (computed here); writes c'(x) when x >= xs.
@@ -214,17 +243,31 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
             const VT lap = lap_v<UNIT>(vadd(a[i], c[i]), vadd(b[i - 1], b[i + 1]), vzsum(cc, left, right), cc, q);
             mc[r + 1] = mu_v<MODEL>(cc, lap, q);
         }
-        // warp ends publish mu(x+1) of rows 0..R-1 for the neighbouring warps
+        // warp ends publish mu(x+1) of rows 0..R-1 for the neighbouring warps:
+        // lane 0 its first cell, the warp's last real lane its last
         float* e1 = edges + (((x + 1) & 1) * W + warp) * 2 * R;
-        if (lane == 0 || lane == 31) {
-            // lane 0 publishes its first cell, lane 31 its last (selects keep mc in registers)
-            const bool first = lane == 0;
-            float* dst = e1 + (first ? 0 : R);
+        if (ZT) {
+            if (lane == 0 || lane == 31) {
+                // (selects keep mc in registers)
+                const bool first = lane == 0;
+                float* dst = e1 + (first ? 0 : R);
 #pragma unroll
-            for (int r = 0; r < R; r += 4)
-                *reinterpret_cast<float4*>(dst + r) = make_float4(
-                    first ? vfirst(mc[r + 1]) : vlast(mc[r + 1]), first ? vfirst(mc[r + 2]) : vlast(mc[r + 2]),
-                    first ? vfirst(mc[r + 3]) : vlast(mc[r + 3]), first ? vfirst(mc[r + 4]) : vlast(mc[r + 4]));
+                for (int r = 0; r < R; r += 4)
+                    *reinterpret_cast<float4*>(dst + r) = make_float4(
+                        first ? vfirst(mc[r + 1]) : vlast(mc[r + 1]), first ? vfirst(mc[r + 2]) : vlast(mc[r + 2]),
+                        first ? vfirst(mc[r + 3]) : vlast(mc[r + 3]), first ? vfirst(mc[r + 4]) : vlast(mc[r + 4]));
+            }
+        } else {
+            if (lane == 0)
+#pragma unroll
+                for (int r = 0; r < R; r += 4)
+                    *reinterpret_cast<float4*>(e1 + r) = make_float4(vfirst(mc[r + 1]), vfirst(mc[r + 2]),
+                                                                     vfirst(mc[r + 3]), vfirst(mc[r + 4]));
+            if (lane == lane_last)
+#pragma unroll
+                for (int r = 0; r < R; r += 4)
+                    *reinterpret_cast<float4*>(e1 + R + r) = make_float4(vlast(mc[r + 1]), vlast(mc[r + 2]),
+                                                                         vlast(mc[r + 3]), vlast(mc[r + 4]));
         }
         if (x >= xs) {
             // the neighbouring warps' end cells: every lane reads the same
@@ -245,16 +288,16 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
                 const float up = __shfl_up_sync(0xffffffffu, vlast(mb[r + 1]), 1);
                 const float down = __shfl_down_sync(0xffffffffu, vfirst(mb[r + 1]), 1);
                 const float left = lane == 0 ? el[r] : up;
-                const float right = lane == 31 ? eh[r] : down;
+                const float right = lane == lane_last ? eh[r] : down;
                 const VT m = mb[r + 1];
                 const VT lap = lap_v<UNIT>(vadd(ma[r + 1], mc[r + 1]), vadd(mb[r], mb[r + 2]), vzsum(m, left, right), m, q);
                 const VT o = vfma(vset<VT>(q.dtm), lap, a[r + 2]);
-                if (r < rows) *reinterpret_cast<VT*>(dst + (long long)r * Z) = o;
+                if (r < rows && real) *reinterpret_cast<VT*>(dst + (long long)r * Z) = o;
             }
         }
         __syncthreads();
         if (s_err) return false;
-        if (t == 0 && x + 1 + kRing <= x_last) fill(x + 1 + kRing);   // slot of x+1 is free now
+        if ((!BULK || t == 0) && x + 1 + kRing <= x_last) fill(x + 1 + kRing);   // slot of x+1 is free now
         return true;
     };
 
@@ -267,8 +310,10 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         if (x >= xe || !iter(x, cC, cA, cB, mC, mA, mB)) break;
         x++;
     }
-    if (s_err && t == 0) {
+    if (s_err && (!BULK || t == 0)) {
         // leave no copy in flight: wait (bounded) for every issued fill
+        // (per-thread copies: every thread waits for its own)
+        if (!BULK) cp_async_wait_all();
         for (int pl = max(x, x_first); pl <= min(x + kRing, x_last); pl++) {
             const int k = pl - x_first;
             mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, STALL ? 4u : kSpinLimit);
@@ -308,51 +353,62 @@ static int take_stall()
     return cur > 0 ? 1 : 0;
 }
 
-static bool row_ok(int Z) { return Z == 32 || Z == 64 || Z == 128 || Z == 256 || Z == 512; }
-static int cells_per_thread(int Z) { return Z == 32 ? 1 : 2; }
+// cells per thread: 2 (packed FP32x2) for even rows, 1 for odd rows and 32-cell rows
+static int cells_per_thread(int Z) { return Z == 32 || Z % 2 ? 1 : 2; }
 
 bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
-    return d.dtype == MMSP_GPU_F32 && g.dim == 3 && row_ok(g.Z) && g.Y >= kStreamR + 4 &&
+    return d.dtype == MMSP_GPU_F32 && g.dim == 3 && g.Z >= 32 && g.Z <= 512 && g.Y >= kStreamR + 4 &&
            (d.model == MMSP_GPU_CH || d.model == MMSP_GPU_CH_POLY);
 }
 
-template <int Z, int V, bool UNIT, bool STALL>
-static const void* pick_model(bool ch)
+template <int ZT, int TM, int V, bool STALL, bool BULK>
+static const void* pick_mu(bool ch, bool unit)
 {
-    return ch ? reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH, UNIT, STALL>)
-              : reinterpret_cast<const void*>(&ch3_stream_f32<kStreamR, Z, V, MMSP_GPU_CH_POLY, UNIT, STALL>);
+    if (ch)
+        return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, true, STALL, BULK>
+                    : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, false, STALL, BULK>;
+    return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, true, STALL, BULK>
+                : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, false, STALL, BULK>;
 }
 
-template <int Z, int V, bool STALL>
-static const void* pick_unit(bool ch, bool unit)
-{
-    return unit ? pick_model<Z, V, true, STALL>(ch) : pick_model<Z, V, false, STALL>(ch);
-}
-
+// The kernel for rows of Z cells: a compile-time instance for rows of
+// 32..512 cells in powers of two (with its STALL form), else the runtime-row
+// instance whose thread bound covers Z / V (no STALL form: nullptr).
 template <bool STALL>
 static const void* pick_stream(int Z, bool ch, bool unit)
 {
     switch (Z) {
-    case 32: return pick_unit<32, 1, STALL>(ch, unit);
-    case 64: return pick_unit<64, 2, STALL>(ch, unit);
-    case 128: return pick_unit<128, 2, STALL>(ch, unit);
-    case 256: return pick_unit<256, 2, STALL>(ch, unit);
-    default: return pick_unit<512, 2, STALL>(ch, unit);
+    case 32: return pick_mu<32, 32, 1, STALL, true>(ch, unit);
+    case 64: return pick_mu<64, 32, 2, STALL, true>(ch, unit);
+    case 128: return pick_mu<128, 64, 2, STALL, true>(ch, unit);
+    case 256: return pick_mu<256, 128, 2, STALL, true>(ch, unit);
+    case 512: return pick_mu<512, 256, 2, STALL, true>(ch, unit);
+    default: break;
     }
+    if (STALL) return nullptr;
+    const int V = cells_per_thread(Z), T = ch3_threads(Z, V);
+    if (V == 2) {
+        const bool bulk = Z % 4 == 0;
+        if (T <= 128) return bulk ? pick_mu<0, 128, 2, false, true>(ch, unit) : pick_mu<0, 128, 2, false, false>(ch, unit);
+        return bulk ? pick_mu<0, 256, 2, false, true>(ch, unit) : pick_mu<0, 256, 2, false, false>(ch, unit);
+    }
+    if (T <= 128) return pick_mu<0, 128, 1, false, false>(ch, unit);
+    if (T <= 256) return pick_mu<0, 256, 1, false, false>(ch, unit);
+    return pick_mu<0, 512, 1, false, false>(ch, unit);
 }
 
 cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     const Coeffs c = make_coeffs(d);
     const int V = cells_per_thread(g.Z);
-    const int threads = g.Z / V;
+    const int threads = ch3_threads(g.Z, V);
     p->fn = pick_stream<false>(g.Z, d.model == MMSP_GPU_CH, c.unit_w);
     p->fn2 = pick_stream<true>(g.Z, d.model == MMSP_GPU_CH, c.unit_w);   // the failure-detection test's form
     p->smem = ch3_smem(kStreamR, g.Z, V);
     p->block = dim3(threads, 1, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);
-    if (e == cudaSuccess) e = ensure_smem(p->fn2, p->smem);
+    if (e == cudaSuccess && p->fn2) e = ensure_smem(p->fn2, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, threads, p->smem);
@@ -379,7 +435,7 @@ cudaError_t launch_ch3_stream(const StepPlan& p, const Geom& g, const Coeffs& c,
     F32Coef q = f32coef(c);
     int planes = p.planes;
     void* args[] = {(void*)&in, (void*)&out, (void*)&g, (void*)&q, (void*)&planes, (void*)&err};
-    return cudaLaunchKernel(take_stall() ? p.fn2 : p.fn, p.grid, p.block, args, p.smem, s);
+    return cudaLaunchKernel(p.fn2 && take_stall() ? p.fn2 : p.fn, p.grid, p.block, args, p.smem, s);
 }
 
 }  // namespace pf

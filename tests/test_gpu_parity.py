@@ -357,11 +357,17 @@ def test_full_3d_ac_128_n8(gpu):
     assert first_bad == div["first_nonfinite_step"]
 
 
-# FP32 3D grids whose rows are a multiple of 32 cells (up to 256) take the
-# register-streaming kernel with bulk-copy staging; cover its strip/segment
-# edge cases: partial last strip, periodic Y wrap at both ends, the smallest
-# allowed Y (strip + 4 halo rows), a single warp per row, few X planes.
-STREAM_SHAPES = [(16, 24, 64), (20, 13, 32), (5, 12, 96), (3, 40, 256), (33, 17, 128), (1, 16, 32)]
+# FP32 3D grids with rows of 32 to 512 cells and at least 12 rows per plane
+# take the register-streaming kernel; cover its strip/segment edge cases
+# (partial last strip, periodic Y wrap at both ends, the smallest allowed Y,
+# a single warp per row, few X planes) and its row forms: compile-time rows
+# of 32..512 in powers of two; runtime rows with bulk copies (multiples of 4
+# cells), with per-thread 8-byte copies (even rows), with one cell per thread
+# (odd rows); a last warp that the row fills only in part (the warp-end mu
+# exchange and the periodic wrap from its last real lane).
+STREAM_SHAPES = [(16, 24, 64), (20, 13, 32), (5, 12, 96), (3, 40, 256), (33, 17, 128), (1, 16, 32),
+                 (7, 13, 243), (4, 12, 33), (6, 20, 50), (3, 14, 198), (2, 12, 300), (2, 12, 301), (3, 17, 190),
+                 (4, 12, 36)]
 
 
 @pytest.mark.parametrize("shape", STREAM_SHAPES, ids=["x".join(map(str, s)) for s in STREAM_SHAPES])
@@ -461,9 +467,9 @@ def test_fp32_ac_row_warp_kernel_shapes(gpu, oracle, monkeypatch, tile, shape, f
     test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, model)
 
 
-# FP32 Cahn-Hilliard grids whose rows are not 32..512 cells in powers of two
-# take the row kernel (any row length, plain loads): 2D rows of odd lengths
-# up to 1024, 3D grids with few rows per plane and odd rows.
+# FP32 Cahn-Hilliard grids that the streaming kernel does not take use the row
+# kernel (any row length, plain loads): 2D rows up to 1024 cells, 3D grids
+# with fewer than 12 rows per plane or rows shorter than 32 cells.
 ROWS = [(50, 77), (7, 1024), (3, 33), (1, 100), (20, 9, 45), (6, 3, 70), (11, 1, 33), (5, 40, 500), (9, 30, 1)]
 
 
