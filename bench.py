@@ -40,6 +40,11 @@ import time
 
 import numpy as np
 
+# The request loop runs each admitted request on its own stream (128 of
+# them); more hardware work queues than the default 8 let their kernels start
+# independently.  Read when the process creates its CUDA context.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -875,6 +880,7 @@ CASES = {
     "ch3d_f32": (SHAPE, 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
     "ch3d_f64": (SHAPE, 1, np.float64, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
     "ch3d_f64c": (SHAPE, 1, np.float64, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB, contract=True)),
+    "ch3d208_f32": ((208, 208, 208), 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
     "ch2d_f64": ((256, 256), 1, np.float64, "ch", dict(dt=0.005, kappa=1.0, mobility=1.0)),
     "ac3d_f32": ((128, 128, 128), 8, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),

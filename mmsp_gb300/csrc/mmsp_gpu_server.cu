@@ -5,7 +5,9 @@
 // carves every admitted request's buffers out of it (first fit, 256-byte
 // granules, freed blocks merge with their neighbours), so admission and
 // retirement never call cudaMalloc or cudaFree, which synchronise the
-// device.  Each admitted request gets a stream from a fixed set.
+// device.  Each admitted request gets a stream from a fixed set: requests of
+// at most 2^21 values from the high-priority half (CUDA stream priorities),
+// the rest from the low-priority half.
 //
 // One scheduler thread owns the device work and runs no rounds: it keeps up
 // to two chunks of at most chunk_steps steps queued on every running
@@ -39,7 +41,8 @@
 
 namespace {
 
-constexpr int kStreams = 128;      // streams shared round-robin by running requests
+constexpr int kStreams = 128;      // streams shared round-robin by running requests (half high priority)
+constexpr long long kSmallValues = 1ll << 21;   // requests of at most this many values take high-priority streams
 constexpr int kInFlight = 2;       // chunks queued ahead per request
 constexpr size_t kGranule = 256;
 
@@ -130,8 +133,8 @@ struct mmsp_gpu_server {
     Clock::time_point t0;
     mmsp_gpu_server_stats st;
     Pool pool;                    // the scheduler thread alone touches it
-    cudaStream_t streams[kStreams] = {};
-    int next_stream = 0;
+    cudaStream_t streams[kStreams] = {};   // [0, kStreams/2): high priority; the rest: low
+    int next_stream[2] = {0, 0};
 };
 
 static double since(const mmsp_gpu_server* s) { return std::chrono::duration<double>(Clock::now() - s->t0).count(); }
@@ -190,8 +193,15 @@ static int feed(mmsp_gpu_server* s, Request* r)
 // Scheduler thread: device state for an admitted request (its block is set).
 static int start_request(mmsp_gpu_server* s, Request* r)
 {
-    r->stream = s->streams[s->next_stream];
-    s->next_stream = (s->next_stream + 1) % kStreams;
+    // Small grids run long chains of short steps; on high-priority streams the
+    // block scheduler starts their kernels first whenever SMs free up, instead
+    // of behind the large grids' full-GPU kernels.
+    const long long values = (long long)r->d.n[0] * (r->d.dim > 1 ? r->d.n[1] : 1) * (r->d.dim > 2 ? r->d.n[2] : 1) *
+                             r->d.fields;
+    const int pri = values <= kSmallValues ? 0 : 1;
+    int& next = s->next_stream[pri];
+    r->stream = s->streams[pri * (kStreams / 2) + next];
+    next = (next + 1) % (kStreams / 2);
     for (auto& e : r->ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
@@ -373,8 +383,14 @@ extern "C" int mmsp_gpu_server_start(mmsp_gpu_server** out, const mmsp_gpu_serve
     s->pool.size = want;
     s->pool.free[0] = want;
     if (s->budget > want) s->budget = want;
-    for (auto& st : s->streams)
-        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    int lo_pri = 0, hi_pri = 0;
+    if (cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri) != cudaSuccess) {
+        cudaGetLastError();
+        lo_pri = hi_pri = 0;
+    }
+    for (int i = 0; i < kStreams; i++)
+        if (cudaStreamCreateWithPriority(&s->streams[i], cudaStreamNonBlocking, i < kStreams / 2 ? hi_pri : lo_pri) !=
+            cudaSuccess) {
             cudaGetLastError();
             for (auto& t : s->streams)
                 if (t) cudaStreamDestroy(t);
