@@ -50,43 +50,41 @@ static OstP<T> ost_narrow(const Coeffs& c, int dim)
     return p;
 }
 
-// Offsets of the six periodic neighbours of a cell (padded axes X, Y, Z).
-// A thread owns one (y, z) column: its Y and Z offsets are fixed, the X
-// ones are taken per plane.
-struct Nb {
-    long long xh, xl, yh, yl;
-    int zh, zl;
+// A thread owns one (y, z) column of the padded axes X, Y, Z and walks it
+// plane by plane.  In-plane offsets are 32-bit (a plane holds fewer than
+// 2^31 cells) and fixed per column, the plane pointers advance once per
+// plane, and the values of the planes either side along X roll through
+// registers, so each Laplacian reads 5 values per cell instead of 7.
+struct Col {
+    int o, yh, yl, zh, zl;   // offsets in a plane: the cell and its four in-plane neighbours
 };
 
-static __device__ __forceinline__ Nb column_neighbours(const Geom& g, int y, int z)
+static __device__ __forceinline__ Col column_of(const Geom& g, int y, int z)
 {
-    Nb n;
-    n.xh = n.xl = 0;
-    n.yh = (y + 1 == g.Y ? -(long long)y : 1LL) * g.Z;
-    n.yl = (y == 0 ? (long long)(g.Y - 1) : -1LL) * g.Z;
-    n.zh = z + 1 == g.Z ? -z : 1;
-    n.zl = z == 0 ? g.Z - 1 : -1;
-    return n;
+    Col c;
+    const int ry = y * g.Z;
+    c.o = ry + z;
+    c.yh = (y + 1 == g.Y ? 0 : y + 1) * g.Z + z;
+    c.yl = (y == 0 ? g.Y - 1 : y - 1) * g.Z + z;
+    c.zh = ry + (z + 1 == g.Z ? 0 : z + 1);
+    c.zl = ry + (z == 0 ? g.Z - 1 : z - 1);
+    return c;
 }
 
-static __device__ __forceinline__ void plane_x(Nb& n, const Geom& g, int x)
-{
-    n.xh = (x + 1 == g.X ? -(long long)x : 1LL) * g.YZ;
-    n.xl = (x == 0 ? (long long)(g.X - 1) : -1LL) * g.YZ;
-}
-
+// The Laplacian at plane pointer pc from the rolled X neighbours xh, xl
+// (the reference's operand order: lap_ref).
 template <typename T, int DIM, bool UNIT>
-static __device__ __forceinline__ T lap_at(const T* __restrict__ f, long long i, const Nb& n, const OstP<T>& p)
+static __device__ __forceinline__ T lap_col(const T* __restrict__ pc, T c, T xh, T xl, const Col& k, const OstP<T>& p)
 {
-    return lap_ref<T, UNIT, DIM>(twice(__ldg(f + i)), __ldg(f + i + n.xh), __ldg(f + i + n.xl), __ldg(f + i + n.yh),
-                                 __ldg(f + i + n.yl), __ldg(f + i + n.zh), __ldg(f + i + n.zl), p.wx, p.wy, p.wz);
+    return lap_ref<T, UNIT, DIM>(twice(c), xh, xl, __ldg(pc + k.yh), __ldg(pc + k.yl), __ldg(pc + k.zh),
+                                 __ldg(pc + k.zl), p.wx, p.wy, p.wz);
 }
 
-// sum_{j>=1} pow(e_j,2), ostwald.cpp:91-93 (0.0 + x == x for x >= 0).
-// NF: the field count when it is a compile-time constant (loops unroll), 0
-// when it is taken from N.
+// sum_{j>=1} pow(e_j,2), ostwald.cpp:91-93 (0.0 + x == x for x >= 0), at
+// offset o of plane offset xo.  NF: the field count when it is a
+// compile-time constant (loops unroll), 0 when it is taken from N.
 template <typename T, int NF>
-static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long i, long long cells, int N)
+static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long xo, int o, long long cells, int N)
 {
     using A = Ar<T>;
     const int n = NF ? NF : N;
@@ -94,17 +92,15 @@ static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long
 #pragma unroll(NF ? NF : 1)
     for (int j = 1; j < (NF ? NF : 64); j++) {
         if (!NF && j >= n) break;
-        const T e = __ldg(s + (long long)j * cells + i);
+        const T e = __ldg(s + (long long)j * cells + xo + o);
         sum = j == 1 ? A::mul(e, e) : A::add(sum, A::mul(e, e));
     }
     return sum;
 }
 
 // Both passes run on (y, z) columns: a block of kOstZ x kOstY threads over a
-// run of kOstPlanes X planes, a thread walking its column plane by plane
-// (coalesced rows, no per-cell division, neighbours through L1 with the
-// periodic offsets precomputed per column).
-constexpr int kOstZ = 32, kOstY = 4, kOstPlanes = 8;
+// run of kOstPlanes X planes (coalesced rows, no per-cell division).
+constexpr int kOstZ = 32, kOstY = 4, kOstPlanes = 16;
 
 // Pass 1, ostwald.cpp:95-99:
 //   w = -A*(C-Cm) + B*pow(C-Cm,3) + Da*pow(C-Ca,3) + Db*pow(C-Cb,3) - g*(C-Ca)*sum - kappa*lap C
@@ -116,55 +112,97 @@ ostwald_mu(const T* __restrict__ s, T* __restrict__ w, Geom g, OstP<T> p, int N)
     const int z = blockIdx.x * kOstZ + threadIdx.x;
     const int y = blockIdx.y * kOstY + threadIdx.y;
     if (z >= g.Z || y >= g.Y) return;
-    Nb n = column_neighbours(g, y, z);
+    const Col k = column_of(g, y, z);
     const int xs = blockIdx.z * kOstPlanes, xe = min(xs + kOstPlanes, g.X);
+    const long long YZ = g.YZ;
+    const T* pc = s + (long long)xs * YZ;
+    T cl = __ldg(s + (long long)(xs == 0 ? g.X - 1 : xs - 1) * YZ + k.o);   // C(x-1)
+    T cc = __ldg(pc + k.o);                                                  // C(x)
     for (int x = xs; x < xe; x++) {
-        plane_x(n, g, x);
-        const long long i = (long long)x * g.YZ + (long long)y * g.Z + z;
-        const T sum = order_sum<T, NF>(s, i, g.cells, N);
-        const T C = __ldg(s + i);
-        const T lap = lap_at<T, DIM, UNIT>(s, i, n, p);
+        const T* ph = s + (long long)(x + 1 == g.X ? 0 : x + 1) * YZ;
+        const T ch = __ldg(ph + k.o);
+        const long long xo = (long long)x * YZ;
+        const T sum = order_sum<T, NF>(s, xo, k.o, g.cells, N);
+        const T C = cc;
+        const T lap = lap_col<T, DIM, UNIT>(pc, cc, ch, cl, k, p);
         const T dm = A::sub(C, p.Cm), da = A::sub(C, p.Ca), db = A::sub(C, p.Cb);
         T v = A::mul(p.negA, dm);
         v = A::add(v, A::mul(p.B, cube(dm)));
         v = A::add(v, A::mul(p.Da, cube(da)));
         v = A::add(v, A::mul(p.Db, cube(db)));
         v = A::sub(v, A::mul(A::mul(p.g, da), sum));
-        w[i] = A::sub(v, kappa_times(p.kappa, lap));
+        w[xo + k.o] = A::sub(v, kappa_times(p.kappa, lap));
+        cl = cc;
+        cc = ch;
+        pc = ph;
     }
 }
 
 // Pass 2, ostwald.cpp:103-120:
 //   C'   = C + dt*D*lap w
 //   e_j' = e_j - dt*L*(-g*pow(C-Ca,2) + delta*pow(e_j,3) + eps*e_j*(sum - pow(e_j,2)) - kappa*lap e_j)
+// The work grid and, for a compile-time field count, every order parameter
+// roll their X neighbours through registers.
 template <typename T, int DIM, bool UNIT, int NF>
 __global__ void __launch_bounds__(kOstZ * kOstY)
 ostwald_update(const T* __restrict__ s, const T* __restrict__ w, T* __restrict__ out, Geom g, OstP<T> p, int N)
 {
     using A = Ar<T>;
+    constexpr int NE = NF ? NF - 1 : 1;   // order parameters rolled (none when NF is 0)
     const int z = blockIdx.x * kOstZ + threadIdx.x;
     const int y = blockIdx.y * kOstY + threadIdx.y;
     if (z >= g.Z || y >= g.Y) return;
-    Nb n = column_neighbours(g, y, z);
+    const Col k = column_of(g, y, z);
     const int xs = blockIdx.z * kOstPlanes, xe = min(xs + kOstPlanes, g.X);
+    const long long YZ = g.YZ, cells = g.cells;
+    const long long xlo = (long long)(xs == 0 ? g.X - 1 : xs - 1) * YZ;
+    const T* wc_p = w + (long long)xs * YZ;
+    T wl = __ldg(w + xlo + k.o), wc = __ldg(wc_p + k.o);
+    T el[NE], ec[NE];
+    if (NF) {
+#pragma unroll
+        for (int j = 0; j < NE; j++) {
+            el[j] = __ldg(s + (long long)(j + 1) * cells + xlo + k.o);
+            ec[j] = __ldg(s + (long long)(j + 1) * cells + (long long)xs * YZ + k.o);
+        }
+    }
     for (int x = xs; x < xe; x++) {
-        plane_x(n, g, x);
-        const long long i = (long long)x * g.YZ + (long long)y * g.Z + z;
-        const T C = __ldg(s + i);
-        out[i] = A::add(C, A::mul(p.dtD, lap_at<T, DIM, UNIT>(w, i, n, p)));
-        const T sum = order_sum<T, NF>(s, i, g.cells, N);
+        const long long xo = (long long)x * YZ;
+        const long long xho = (long long)(x + 1 == g.X ? 0 : x + 1) * YZ;
+        const T wh = __ldg(w + xho + k.o);
+        const T C = __ldg(s + xo + k.o);
+        out[xo + k.o] = A::add(C, A::mul(p.dtD, lap_col<T, DIM, UNIT>(wc_p, wc, wh, wl, k, p)));
+        const T sum = order_sum<T, NF>(s, xo, k.o, cells, N);
         const T da = A::sub(C, p.Ca);
         const T t1 = A::mul(p.neg_g, A::mul(da, da));
-#pragma unroll(NF ? NF : 1)
-        for (int j = 1; j < (NF ? NF : 64); j++) {
-            if (!NF && j >= N) break;
-            const T* f = s + (long long)j * g.cells;
-            const T e = __ldg(f + i);
-            T v = A::add(t1, A::mul(p.delta, cube(e)));
-            v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
-            v = A::sub(v, kappa_times(p.kappa, lap_at<T, DIM, UNIT>(f, i, n, p)));
-            out[(long long)j * g.cells + i] = A::sub(e, A::mul(p.dtL, v));
+        if (NF) {
+#pragma unroll
+            for (int j = 0; j < NE; j++) {
+                const T* f = s + (long long)(j + 1) * cells;
+                const T e = ec[j];
+                const T eh = __ldg(f + xho + k.o);
+                T v = A::add(t1, A::mul(p.delta, cube(e)));
+                v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
+                v = A::sub(v, kappa_times(p.kappa, lap_col<T, DIM, UNIT>(f + xo, e, eh, el[j], k, p)));
+                out[(long long)(j + 1) * cells + xo + k.o] = A::sub(e, A::mul(p.dtL, v));
+                el[j] = e;
+                ec[j] = eh;
+            }
+        } else {
+            const long long xlo2 = (long long)(x == 0 ? g.X - 1 : x - 1) * YZ;
+            for (int j = 1; j < N; j++) {
+                const T* f = s + (long long)j * cells;
+                const T e = __ldg(f + xo + k.o);
+                T v = A::add(t1, A::mul(p.delta, cube(e)));
+                v = A::add(v, A::mul(A::mul(p.eps, e), A::sub(sum, A::mul(e, e))));
+                v = A::sub(v, kappa_times(p.kappa, lap_col<T, DIM, UNIT>(f + xo, e, __ldg(f + xho + k.o),
+                                                                        __ldg(f + xlo2 + k.o), k, p)));
+                out[(long long)j * cells + xo + k.o] = A::sub(e, A::mul(p.dtL, v));
+            }
         }
+        wl = wc;
+        wc = wh;
+        wc_p = w + xho;
     }
 }
 
