@@ -399,6 +399,157 @@ ac3_vec_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, AcF
     }
 }
 
+// The same computation with the ring run as a producer/consumer pipeline
+// and no block-wide barrier in the plane loop: warp TY*FG (lane 0) issues
+// the plane copies, each slot with a "full" barrier (the copy's bytes) and
+// an "empty" barrier on which every computing warp arrives once it is done
+// with the plane; the producer refills a slot when its "empty" phase
+// completes.  A computing warp that finishes a plane goes on to the next as
+// soon as that plane has arrived, instead of waiting for the slowest warp.
+// Every wait is bounded; a warp whose wait runs out sets the error word and
+// leaves, the others then run out too, and the producer waits (bounded) for
+// its last copies before it leaves.
+template <int V, int TY, int FG, int MODEL>
+__global__ void __launch_bounds__(32 * (TY * FG + 1))
+ac3_ws_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, AcF32 q, int planes, int N, int D,
+           int* __restrict__ err)
+{
+    constexpr int Z = 32 * V, R = TY, RR = R + 2, CW = TY * FG;   // CW computing warps
+    const int lane = threadIdx.x, cw = threadIdx.y;
+    const int w = cw % TY, fg = cw / TY;
+    extern __shared__ __align__(128) unsigned char sm[];
+    float* slots = reinterpret_cast<float*>(sm);
+    const int chunk = RR * Z;
+    const int slot_elems = N * chunk;
+    uint64_t* full = reinterpret_cast<uint64_t*>(slots + ((D * slot_elems + 1) & ~1));
+    uint64_t* empty = full + D;
+
+    const int y0 = blockIdx.x * R;
+    const int xs = blockIdx.y * planes;
+    const int xe = min(xs + planes, g.X);
+    if (xs >= xe) return;
+    const int x_first = xs - 1, x_last = xe;
+    const long long cells = g.cells;
+
+    if (cw == 0 && lane == 0) {
+        for (int s = 0; s < D; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], CW);
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();   // the only block-wide barrier
+
+    if (cw == CW) {   // the producer warp
+        if (lane != 0) return;
+        const uint32_t row = (uint32_t)Z * sizeof(float);
+        int pl = x_first;
+        for (; pl <= x_last; pl++) {
+            const int k = pl - x_first, s = k % D;
+            if (k >= D && !mbar_wait(&empty[s], (uint32_t)(k / D - 1) & 1u)) {
+                atomicExch(err, 1);
+                break;
+            }
+            float* dst0 = slots + s * slot_elems;
+            const long long plane = (long long)wrapi(pl, g.X) * g.YZ;
+            fence_proxy_async();
+            mbar_expect_tx(&full[s], (uint32_t)N * RR * row);
+            const int a = y0 - 1, b = y0 + R + 1;
+            for (int f = 0; f < N; f++) {
+                const float* base = ein + (long long)f * cells + plane;
+                float* dst = dst0 + f * chunk;
+                if (a >= 0 && b <= g.Y) {
+                    bulk_g2s(dst, base + (long long)a * Z, RR * row, &full[s]);
+                } else if (a < 0) {
+                    bulk_g2s(dst, base + (long long)(g.Y - 1) * Z, row, &full[s]);
+                    bulk_g2s(dst + Z, base, (RR - 1) * row, &full[s]);
+                } else {
+                    const int n1 = g.Y - a;
+                    bulk_g2s(dst, base + (long long)a * Z, n1 * row, &full[s]);
+                    bulk_g2s(dst + n1 * Z, base, (RR - n1) * row, &full[s]);
+                }
+            }
+        }
+        // leave no copy in flight: wait (bounded) for the last fill of every slot
+        for (int p2 = max(x_first, pl - D); p2 < pl; p2++) {
+            const int k = p2 - x_first;
+            mbar_wait(&full[k % D], (uint32_t)(k / D) & 1u);
+        }
+        return;
+    }
+
+    auto slot_of = [&](int pl) -> const float* { return slots + ((pl - x_first) % D) * slot_elems; };
+    auto arrived = [&](int pl) {
+        const int k = pl - x_first;
+        return mbar_wait(&full[k % D], (uint32_t)(k / D) & 1u);
+    };
+    const bool row_on = y0 + w < g.Y;
+    const int lo = (lane + 31) & 31, hi = (lane + 1) & 31;
+    bool ok = arrived(x_first) && arrived(x_first + 1);
+    for (int x = xs; x < xe && ok; x++) {
+        if (!arrived(x + 1)) {
+            ok = false;
+            break;
+        }
+        const float* SL = slot_of(x - 1) + (w + 1) * Z + V * lane;
+        const float* SH = slot_of(x + 1) + (w + 1) * Z + V * lane;
+        const float* SC = slot_of(x) + w * Z + V * lane;
+        float2 sum[V / 2], sum1[V / 2];
+#pragma unroll
+        for (int k = 0; k < V / 2; k++) sum[k] = sum1[k] = v2(0.0f);
+        int f0 = 0;
+#pragma unroll 2
+        for (; f0 + 1 < N; f0 += 2) {
+            float c[V], e[V];
+            ldv<V>(SC + f0 * chunk + Z, c);
+            ldv<V>(SC + (f0 + 1) * chunk + Z, e);
+#pragma unroll
+            for (int k = 0; k < V / 2; k++) {
+                sum[k] = __ffma2_rn(v2(c[2 * k], c[2 * k + 1]), v2(c[2 * k], c[2 * k + 1]), sum[k]);
+                sum1[k] = __ffma2_rn(v2(e[2 * k], e[2 * k + 1]), v2(e[2 * k], e[2 * k + 1]), sum1[k]);
+            }
+        }
+        if (f0 < N) {
+            float c[V];
+            ldv<V>(SC + f0 * chunk + Z, c);
+#pragma unroll
+            for (int k = 0; k < V / 2; k++) sum[k] = __ffma2_rn(v2(c[2 * k], c[2 * k + 1]), v2(c[2 * k], c[2 * k + 1]), sum[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < V / 2; k++) sum[k] = __fadd2_rn(sum[k], sum1[k]);
+        float* dst = eout + (long long)x * g.YZ + (long long)(y0 + w) * Z + V * lane;
+#pragma unroll 2
+        for (int f = fg; f < N; f += FG) {
+            const int fo = f * chunk;
+            float up[V], cc[V], dn[V], xl[V], xh[V], out[V];
+            ldv<V>(SC + fo, up);
+            ldv<V>(SC + fo + Z, cc);
+            ldv<V>(SC + fo + 2 * Z, dn);
+            ldv<V>(SL + fo, xl);
+            ldv<V>(SH + fo, xh);
+            const float left = __shfl_sync(0xffffffffu, cc[V - 1], lo);
+            const float right = __shfl_sync(0xffffffffu, cc[0], hi);
+#pragma unroll
+            for (int k = 0; k < V; k += 2) {
+                const float2 c2 = v2(cc[k], cc[k + 1]);
+                const float2 sz = v2((k == 0 ? left : cc[k - 1]) + cc[k + 1], cc[k] + (k + 2 == V ? right : cc[k + 2]));
+                const float2 sx = __fadd2_rn(v2(xl[k], xl[k + 1]), v2(xh[k], xh[k + 1]));
+                const float2 sy = __fadd2_rn(v2(up[k], up[k + 1]), v2(dn[k], dn[k + 1]));
+                const float2 lap = __ffma2_rn(v2(q.wx), sx, __ffma2_rn(v2(q.wy), sy,
+                                              __ffma2_rn(v2(q.wz), sz, __fmul2_rn(v2(-q.w2), c2))));
+                const float2 nv = (MODEL == MMSP_GPU_ZENER && f == 0) ? c2 : ac_new_f32x2<MODEL>(c2, sum[k / 2], lap, q);
+                out[k] = nv.x;
+                out[k + 1] = nv.y;
+            }
+            if (row_on) stv<V>(dst + (long long)f * cells, out);
+        }
+        // this warp is done with plane x-1
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[(x - 1 - x_first) % D]);
+    }
+    if (!ok && lane == 0) atomicExch(err, 1);
+}
+
 // Thread rows per block for a strip of R rows of Z cells and N fields.
 // Measured on 128^3 grids: two thread rows (twice the warps at the same
 // shared memory) win from 8 fields up (47 -> 41 us per step at N = 8,
@@ -486,6 +637,15 @@ static bool ac3_shape(const Geom& g, int N, int* R, int* D)
 
 
 template <int V, int TY, int FG>
+static const void* acw_pick_model(int model)
+{
+    if (model == MMSP_GPU_AC) return (const void*)&ac3_ws_f32<V, TY, FG, MMSP_GPU_AC>;
+    if (model == MMSP_GPU_GG) return (const void*)&ac3_ws_f32<V, TY, FG, MMSP_GPU_GG>;
+    if (model == MMSP_GPU_ZENER) return (const void*)&ac3_ws_f32<V, TY, FG, MMSP_GPU_ZENER>;
+    return (const void*)&ac3_ws_f32<V, TY, FG, MMSP_GPU_AC_POLY>;
+}
+
+template <int V, int TY, int FG>
 static const void* acv_pick_model(int model)
 {
     if (model == MMSP_GPU_AC) return (const void*)&ac3_vec_f32<V, TY, FG, MMSP_GPU_AC>;
@@ -495,79 +655,97 @@ static const void* acv_pick_model(int model)
 }
 
 template <int V, int TY>
-static const void* acv_pick_fg(int fg, int model)
+static const void* acv_pick_fg(int fg, bool ws, int model)
 {
+    if (ws) return fg == 4 ? acw_pick_model<V, TY, 4>(model) : fg == 2 ? acw_pick_model<V, TY, 2>(model)
+                                                              : acw_pick_model<V, TY, 1>(model);
     if (fg == 4) return acv_pick_model<V, TY, 4>(model);
     if (fg == 2) return acv_pick_model<V, TY, 2>(model);
     return acv_pick_model<V, TY, 1>(model);
 }
 
 template <int V>
-static const void* acv_pick_ty(int ty, int fg, int model)
+static const void* acv_pick_ty(int ty, int fg, bool ws, int model)
 {
-    if (ty == 4) return acv_pick_fg<V, 4>(fg, model);
-    if (ty == 2) return acv_pick_fg<V, 2>(fg, model);
+    if (ty == 4) return acv_pick_fg<V, 4>(fg, ws, model);
+    if (ty == 2) return acv_pick_fg<V, 2>(fg, ws, model);
     return nullptr;
 }
 
 // The warp-per-row kernel for rows of 64, 128 or 256 cells: 4-row strips
 // (2 where 4 do not fit) and a ring of 3 slots, or 4 where the 3-slot ring
 // already limits an SM to 3 blocks or fewer and the fourth slot keeps 2
-// blocks, or loses none; two warps per row from 8 fields up.  Measured on
-// 128^3, us per step: 8 fields 35.1 (3 slots), 32.9 (4 slots), 31.9 (4 slots,
-// 2 warps per row); 16 fields 114.5, 100.7, 87.0; 3 fields 10.1 (3 slots),
-// 10.6 (4), 14.6 (3 slots, 2 warps per row).  MMSP_GPU_AC3_SHAPE=
-// "rows,depth[,warps per row]" (rows 2 or 4, depth 3 to 6, warps 1, 2 or 4)
-// replaces the choice, "0,0" selects the kernel above.
-static const void* acv_plan(const mmsp_gpu_desc& d, const Geom& g, int* R, int* D, int* FG)
+// blocks, or loses none; two warps per row from 8 fields up; the
+// producer/consumer form (4 slots) from 12 fields up and for 256-cell rows.
+// Measured, us per step: 128^3 x 8 fields 35.1 (3 slots), 32.9 (4 slots),
+// 31.9 (4 slots, 2 warps per row), 32.2 (the same, producer/consumer);
+// 128^3 x 16: 114.5, 100.7, 87.0, 75.7; 128^3 x 3: 10.1 (3 slots), 10.6 (4),
+// 14.6 (3 slots, 2 warps per row), 12.7 (producer/consumer); 96x64x256 x 6:
+// 28.1 against 24.4 (producer/consumer).  MMSP_GPU_AC3_SHAPE=
+// "rows,depth[,warps per row[,1]]" (rows 2 or 4, depth 3 to 6, warps 1, 2
+// or 4, 1: the producer/consumer form) replaces the choice, "0,0" selects
+// the kernel above.
+static const void* acv_plan(const mmsp_gpu_desc& d, const Geom& g, int* R, int* D, int* FG, bool* WS)
 {
     if (g.Z != 64 && g.Z != 128 && g.Z != 256) return nullptr;
     int ty = 4, dd = 0, fg = d.fields >= 8 ? 2 : 1;
+    bool ws = false;
     if (const char* e = getenv("MMSP_GPU_AC3_SHAPE")) {
-        int a = 0, b = 0, c = 0;
-        const int n = sscanf(e, "%d,%d,%d", &a, &b, &c);
+        int a = 0, b = 0, c = 0, w = 0;
+        const int n = sscanf(e, "%d,%d,%d,%d", &a, &b, &c, &w);
         if (n >= 2) {
             if (a == 0) return nullptr;
             if ((a == 2 || a == 4) && b >= 3 && b <= 6) {
                 ty = a;
                 dd = b;
-                fg = n == 3 && (c == 1 || c == 2 || c == 4) ? c : 1;
+                fg = n >= 3 && (c == 1 || c == 2 || c == 4) ? c : 1;
+                ws = n == 4 && w == 1;
             }
         }
     }
     const int fix = dd;
+    // large slots (many fields, or 256-cell rows): the producer/consumer form
+    // with two warps per row on a 4-slot ring
+    if (!fix && (d.fields >= 12 || g.Z == 256)) {
+        ws = true;
+        fg = d.fields >= 2 ? 2 : 1;
+    }
     if (!fix) dd = 3;
     while (ty > 2 && (g.Y < ty + 2 || ac3_smem(ty, g.Z, d.fields, dd) > kAcSmemCap)) ty /= 2;
     if (g.Y < ty + 2 || ac3_smem(ty, g.Z, d.fields, dd) > kAcSmemCap) return nullptr;
     if (!fix && ac3_smem(ty, g.Z, d.fields, 4) <= kAcSmemCap) {
         const int b3 = ac3_blocks_per_sm(ac3_smem(ty, g.Z, d.fields, 3));
         const int b4 = ac3_blocks_per_sm(ac3_smem(ty, g.Z, d.fields, 4));
-        if (b3 <= 3 && (b4 >= 2 || b4 == b3)) dd = 4;
+        if (ws || (b3 <= 3 && (b4 >= 2 || b4 == b3))) dd = 4;
     }
     *R = ty;
     *D = dd;
     const int V = g.Z / 32;
     *FG = fg;
-    return V == 2 ? acv_pick_ty<2>(ty, fg, d.model) : V == 4 ? acv_pick_ty<4>(ty, fg, d.model)
-                  : acv_pick_ty<8>(ty, fg, d.model);
+    *WS = ws;
+    return V == 2 ? acv_pick_ty<2>(ty, fg, ws, d.model) : V == 4 ? acv_pick_ty<4>(ty, fg, ws, d.model)
+                  : acv_pick_ty<8>(ty, fg, ws, d.model);
 }
 
 bool ac3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
     int R, D, FG;
+    bool WS;
     return d.dtype == MMSP_GPU_F32 && g.dim == 3 && g.Z <= 256 &&
            (d.model == MMSP_GPU_AC || d.model == MMSP_GPU_GG || d.model == MMSP_GPU_AC_POLY ||
             d.model == MMSP_GPU_ZENER) &&
-           (acv_plan(d, g, &R, &D, &FG) || ac3_shape(g, d.fields, &R, &D));
+           (acv_plan(d, g, &R, &D, &FG, &WS) || ac3_shape(g, d.fields, &R, &D));
 }
 
 cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     int R = 4, D = 4, FG = 1;
+    bool WS = false;
     int threads;
-    if ((p->fn = acv_plan(d, g, &R, &D, &FG))) {
-        threads = 32 * R * FG;
-        p->block = dim3(32, R, FG);
+    if ((p->fn = acv_plan(d, g, &R, &D, &FG, &WS))) {
+        // the pipelined form: computing warps along y, then the producer warp
+        threads = WS ? 32 * (R * FG + 1) : 32 * R * FG;
+        p->block = WS ? dim3(32, R * FG + 1, 1) : dim3(32, R, FG);
     } else {
         ac3_shape(g, d.fields, &R, &D);
         int RT, TY;
@@ -578,7 +756,7 @@ cudaError_t plan_ac3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
         if (!p->fn) return cudaErrorInvalidConfiguration;
         p->block = dim3(zt, TY, 1);
     }
-    p->smem = ac3_smem(R, g.Z, d.fields, D);
+    p->smem = ac3_smem(R, g.Z, d.fields, D) + (WS ? sizeof(uint64_t) * D : 0);   // + the "empty" barriers
     cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;

@@ -25,6 +25,13 @@ static __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
 
+// Arrive on `bar` (release: this thread's earlier shared-memory accesses
+// are ordered before the phase completes).
+static __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Make initialised barriers visible to the asynchronous proxy.
 static __device__ __forceinline__ void mbar_fence_init()
 {

@@ -450,14 +450,17 @@ def test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, m
 
 
 # Rows of 64, 128 and 256 cells take the warp-per-row form of the streaming
-# kernel; MMSP_GPU_AC3_SHAPE fixes its strip rows, ring depth and warps per
-# row ("0,0": the per-cell form): 2- and 4-row strips (Y = 4, 5 fall back to
-# 2 rows), rings of 3 to 6 slots, 1, 2 and 4 warps per row (uneven field
-# shares, a warp with none), partial strips and Y wraps, every model.
+# kernel; MMSP_GPU_AC3_SHAPE fixes its strip rows, ring depth, warps per row
+# and (fourth value 1) the producer/consumer form ("0,0": the per-cell
+# form): 2- and 4-row strips (Y = 4, 5 fall back to 2 rows), rings of 3 to 6
+# slots, 1, 2 and 4 warps per row (uneven field shares, a warp with none),
+# partial strips and Y wraps, a single X plane, every model.
 AC_VEC = [("2,3", (7, 9, 64), 3, "ac"), ("2,5", (5, 11, 128), 8, "gg"), ("4,6", (6, 13, 128), 4, "zener"),
           ("4,4", (4, 6, 256), 6, "ac"), ("0,0", (5, 9, 128), 8, "ac"), ("4,3", (3, 5, 128), 1, "ac_poly"),
           ("4,4", (9, 4, 64), 16, "gg"), ("2,4", (4, 14, 256), 12, "ac"), ("4,4,2", (6, 9, 128), 8, "ac"),
-          ("2,3,4", (5, 7, 64), 5, "gg"), ("4,4,4", (4, 6, 128), 3, "zener"), ("4,3,2", (5, 10, 256), 7, "ac")]
+          ("2,3,4", (5, 7, 64), 5, "gg"), ("4,4,4", (4, 6, 128), 3, "zener"), ("4,3,2", (5, 10, 256), 7, "ac"),
+          ("4,4,2,1", (6, 9, 128), 8, "ac"), ("4,3,1,1", (5, 7, 64), 5, "gg"), ("2,4,2,1", (4, 14, 256), 12, "ac"),
+          ("4,5,4,1", (4, 6, 128), 3, "zener"), ("4,3,1,1", (1, 7, 128), 2, "ac")]
 
 
 @pytest.mark.parametrize("tile,shape,fields,model", AC_VEC,
