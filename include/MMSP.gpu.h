@@ -209,7 +209,11 @@ int mmsp_gpu_upload_device(mmsp_gpu_handle* h, const void* dev, size_t bytes, in
 int mmsp_gpu_download_device(mmsp_gpu_handle* h, void* dev, size_t bytes, int layout);
 
 /* Advance the state by `steps` explicit-Euler steps (asynchronous; CUDA
- * graphs replay long runs).  steps == 0 is a no-op. */
+ * graphs replay long runs).  steps == 0 is a no-op.  2D FP32 Cahn-Hilliard
+ * grids (noise-free) take whole blocks of 4 steps per launch of a
+ * temporally blocked kernel and the call's last steps % 4 steps one launch
+ * each; the two round differently in FP32, so runs split into calls of
+ * multiples of 4 steps equal one call, bit for bit. */
 int mmsp_gpu_step(mmsp_gpu_handle* h, int steps);
 
 /* Wait for the handle's queued work. */
@@ -366,18 +370,22 @@ const char* mmsp_gpu_batch_last_error(const mmsp_gpu_batch* b);
  *
  * Clients submit (descriptor, initial state, steps) from any thread.  A
  * scheduler thread admits queued requests in arrival order while their
- * device footprint (mmsp_gpu_footprint) fits the HBM budget, keeps admitted
- * state on the device, and advances every admitted request by up to
- * chunk_steps steps per round on its own stream, so requests overlap on the
- * GPU.  New requests join at round boundaries; finished ones are reduced
- * (mass, energy), copied to the host and their device memory freed at once.
- * Each request runs the same kernels with the same step sequence as a lone
- * mmsp_gpu_update, so its result does not depend on what else is running. */
+ * device footprint (mmsp_gpu_footprint) fits the HBM budget, carving their
+ * buffers from one device block taken at start, and keeps two chunks of at
+ * most chunk_steps steps (rounded down to a multiple of 4) queued on every
+ * admitted request's stream, so requests overlap on the GPU and finish
+ * independently; small grids run on high-priority streams.  Finished
+ * requests are reduced (mass, energy), copied to the host and their block
+ * returned at once.  Each request runs the same kernels with the same step
+ * sequence as a lone mmsp_gpu_update, so its result does not depend on what
+ * else is running.  A serving process should set CUDA_DEVICE_MAX_CONNECTIONS
+ * to 32 before it creates its CUDA context (the requests' streams then do
+ * not share the default 8 hardware work queues). */
 typedef struct mmsp_gpu_server mmsp_gpu_server;
 
 typedef struct mmsp_gpu_server_config {
     size_t hbm_budget_bytes;   /* device bytes for request state (0: 80% of free memory) */
-    int chunk_steps;           /* steps per round (0: 200) */
+    int chunk_steps;           /* steps per queued chunk, a multiple of 4 (0: 200) */
     int max_active;            /* requests resident at once (0: no limit but the budget) */
 } mmsp_gpu_server_config;
 

@@ -4,10 +4,13 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "MMSP.gpu.h"
+#include "pf_batch.h"
 #include "pf_handle.h"
 #include "pf_internal.h"
 
@@ -202,8 +205,33 @@ static bool two_pass_f64(const mmsp_gpu_desc* d)
            (d->model == MMSP_GPU_CH || d->model == MMSP_GPU_CH_POLY);
 }
 
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+// 2D FP32 Cahn-Hilliard grids step in blocks of pf::kTbAnyDepth steps, each
+// one launch of the temporally blocked kernel of the batched form
+// (pf_batch.cu) over the grid's 64 x 128 regions: a quarter of the launches
+// and of the HBM traffic of one kernel per step.  The leftover steps of a
+// call (fewer than kTbAnyDepth) take the plan's per-step kernel, so a run
+// split into calls of multiples of kTbAnyDepth steps equals one call.
+static bool tb_handle(const mmsp_gpu_desc* d)
+{
+    return d->dtype == MMSP_GPU_F32 && d->dim == 2 && (d->model == MMSP_GPU_CH || d->model == MMSP_GPU_CH_POLY) &&
+           !pf::noisy(*d);
+}
+
+static int tb_tile_rows() { return pf::kTbShapes[0].ri - 4 * pf::kTbAnyDepth; }
+static int tb_tile_cols() { return pf::kTbCols - 4 * pf::kTbAnyDepth; }
+
+static size_t tb_meta_bytes(const mmsp_gpu_desc* d)
+{
+    const long long tiles = (long long)((d->n[0] + tb_tile_rows() - 1) / tb_tile_rows()) *
+                            ((d->n[1] + tb_tile_cols() - 1) / tb_tile_cols());
+    return align256(sizeof(pf::BatchInst)) + align256(sizeof(pf::TbItem) * (size_t)tiles) + 256;
+}
+
 static size_t work_bytes(const mmsp_gpu_desc* d)
 {
+    if (tb_handle(d)) return tb_meta_bytes(d);   // the blocked kernel's instance, tiles and counters
     if (d->model == MMSP_GPU_CH_CONVEX) return state_bytes(d);   // download staging (the guess stays put)
     if (d->model != MMSP_GPU_OSTWALD && !two_pass_f64(d)) return 0;
     return state_bytes(d) / (size_t)d->fields;
@@ -235,14 +263,13 @@ static void release(mmsp_gpu_handle* h)
     if (h->own) cudaStreamDestroy(h->own);
 }
 
-static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
-
 size_t pf::handle_block_bytes(const mmsp_gpu_desc& d)
 {
     return 2 * align256(state_bytes(&d)) + align256(pf::kPartialsBytes) + 256 + align256(work_bytes(&d));
 }
 
 static int make_plan(mmsp_gpu_handle* h);
+static int setup_tb(mmsp_gpu_handle* h);
 
 int pf::create_in(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc, void* block, cudaStream_t stream)
 {
@@ -283,6 +310,7 @@ int pf::create_in(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc, void* block,
         return MMSP_GPU_ECUDA;
     }
     rc = make_plan(h);
+    if (!rc) rc = setup_tb(h);
     if (rc) {
         release(h);
         delete h;
@@ -313,6 +341,65 @@ static int make_plan(mmsp_gpu_handle* h)
         return cuda_fail(h, e, "plan");
     }
     return MMSP_GPU_OK;
+}
+
+// The blocked kernel's instance and tile list, in the handle's work buffer.
+static int setup_tb(mmsp_gpu_handle* h)
+{
+    if (!tb_handle(&h->d)) return MMSP_GPU_OK;
+    const int n0 = h->d.n[0], n1 = h->d.n[1], TX = tb_tile_rows(), TZ = tb_tile_cols();
+    std::vector<pf::TbItem> items;
+    for (int x0 = 0; x0 < n0; x0 += TX)
+        for (int z0 = 0; z0 < n1; z0 += TZ)
+            items.push_back(pf::TbItem{0, x0, z0, std::min(TX, n0 - x0), std::min(TZ, n1 - z0)});
+    pf::BatchInst bi;
+    memset(&bi, 0, sizeof(bi));
+    bi.off = 0;
+    bi.n0 = n0;
+    bi.n1 = n1;
+    bi.w0 = h->c.w[0];
+    bi.w1 = h->c.w[1];
+    bi.kappa = h->c.kappa;
+    bi.dtm = h->c.dtm;
+    bi.neg_r = h->c.neg_r;
+    bi.u = h->c.u;
+    char* p = static_cast<char*>(h->work);
+    h->tb_inst = reinterpret_cast<pf::BatchInst*>(p);
+    p += align256(sizeof(pf::BatchInst));
+    h->tb_list = reinterpret_cast<pf::TbItem*>(p);
+    p += align256(sizeof(pf::TbItem) * items.size());
+    h->tb_counters = reinterpret_cast<int*>(p);
+    h->tb_items = (int)items.size();
+    const bool aligned = n1 % 4 == 0;   // 16-byte row groups
+    h->tb_fn = aligned ? pf::tb_kernel(0, pf::kTbAnyDepth, h->d.model, h->c.unit_w)
+                       : pf::tb_kernel_any(h->d.model, h->c.unit_w);
+    h->tb_smem = pf::tb_smem(0);
+    cudaError_t e = cudaMemcpyAsync(h->tb_inst, &bi, sizeof(bi), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->tb_list, items.data(), sizeof(pf::TbItem) * items.size(), cudaMemcpyHostToDevice,
+                            h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->tb_counters, 0, 256, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);   // the host arrays go out of scope
+    if (e == cudaSuccess) e = pf::ensure_smem(h->tb_fn, h->tb_smem);
+    int per_sm = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->tb_fn, pf::kTbShapes[0].nt, h->tb_smem);
+    if (e != cudaSuccess) return cuda_fail(h, e, "blocked kernel setup");
+    h->tb_blocks = std::max(1, std::min(per_sm * pf::sm_count(), h->tb_items));
+    h->tb_launches = 0;
+    h->tb = true;
+    return MMSP_GPU_OK;
+}
+
+// kTbAnyDepth steps from buf[cur] in one launch of the blocked kernel.
+static cudaError_t tb_launch(mmsp_gpu_handle* h, cudaStream_t s)
+{
+    const cudaError_t e =
+        pf::launch_tb(h->tb_fn, h->tb_blocks, pf::kTbShapes[0].nt, h->tb_smem, h->tb_inst, h->tb_list, h->tb_items,
+                      h->buf[h->cur], h->buf[h->cur ^ 1], h->tb_counters, (int)(h->tb_launches & 1), s);
+    h->cur ^= 1;
+    h->tb_launches++;
+    return e;
 }
 
 extern "C" int mmsp_gpu_create(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc)
@@ -352,6 +439,7 @@ extern "C" int mmsp_gpu_create(mmsp_gpu_handle** out, const mmsp_gpu_desc* desc)
         return MMSP_GPU_ENOMEM;
     }
     rc = make_plan(h);
+    if (!rc) rc = setup_tb(h);
     if (rc) {
         release(h);
         delete h;
@@ -504,11 +592,17 @@ static int build_graph(mmsp_gpu_handle* h)
         cudaStreamDestroy(cs);
         return cuda_fail(h, e, "begin capture");
     }
-    int saved = h->cur;
+    const int saved = h->cur;
+    const int64_t saved_launches = h->tb_launches;
     h->cur = 0;
+    h->tb_launches = 0;
     cudaError_t le = cudaSuccess;
-    for (int i = 0; i < kGraphSteps && le == cudaSuccess; i++) le = one_step(h, cs);
+    if (h->tb)
+        for (int i = 0; i < kGraphSteps / pf::kTbAnyDepth && le == cudaSuccess; i++) le = tb_launch(h, cs);
+    else
+        for (int i = 0; i < kGraphSteps && le == cudaSuccess; i++) le = one_step(h, cs);
     h->cur = saved;
+    h->tb_launches = saved_launches;
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(cs, &graph);
     cudaStreamDestroy(cs);
@@ -585,6 +679,29 @@ extern "C" int mmsp_gpu_step(mmsp_gpu_handle* h, int steps)
         int rc = convex_steps(h, steps);
         if (rc) return rc;
         left = 0;
+    } else if (h->tb) {
+        constexpr int kTbGraph = kGraphSteps / pf::kTbAnyDepth;   // launches per graph replay (even)
+        int nt = left / pf::kTbAnyDepth;
+        left -= nt * pf::kTbAnyDepth;
+        if (nt >= 2 * kTbGraph) {
+            int rc = build_graph(h);
+            if (rc) return rc;
+            // the graph starts from buf[0] at an even launch count
+            if (h->cur == 1 && (h->tb_launches & 1) == 1) {
+                if ((e = tb_launch(h, h->stream)) != cudaSuccess) return cuda_fail(h, e, "blocked step");
+                nt--;
+            }
+            if (h->cur == 0 && (h->tb_launches & 1) == 0)
+                while (nt >= kTbGraph) {
+                    if ((e = cudaGraphLaunch(h->graph, h->stream)) != cudaSuccess) return cuda_fail(h, e, "graph launch");
+                    nt -= kTbGraph;
+                    h->tb_launches += kTbGraph;
+                }
+        }
+        while (nt > 0) {
+            if ((e = tb_launch(h, h->stream)) != cudaSuccess) return cuda_fail(h, e, "blocked step");
+            nt--;
+        }
     } else if (steps >= kGraphMin) {
         int rc = build_graph(h);
         if (rc) return rc;

@@ -21,6 +21,7 @@
 // chunking does not change a step's result), so its result does not depend
 // on what else is running.  Clients only touch host structures under the
 // mutex.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -398,7 +399,9 @@ extern "C" int mmsp_gpu_server_start(mmsp_gpu_server** out, const mmsp_gpu_serve
             delete s;
             return MMSP_GPU_ECUDA;
         }
-    if (cfg && cfg->chunk_steps > 0) s->chunk = cfg->chunk_steps;
+    // multiples of 4: 2D FP32 Cahn-Hilliard handles run 4 steps per launch, and
+    // chunks of whole blocks give the same launches as one call of all steps
+    if (cfg && cfg->chunk_steps > 0) s->chunk = std::max(4, cfg->chunk_steps / 4 * 4);
     if (cfg && cfg->max_active > 0) s->max_active = cfg->max_active;
     s->st.device_bytes_budget = s->budget;
     s->t0 = Clock::now();

@@ -308,7 +308,7 @@ static __device__ __forceinline__ float4 tb_update4(float4 c, float4 up, float4 
     return make_float4(n01.x, n01.y, n23.x, n23.y);
 }
 
-template <int RI, int KS, int NW, int MODEL, bool UNIT>
+template <int RI, int KS, int NW, int MODEL, bool UNIT, bool ALIGNED>
 __global__ void __launch_bounds__(NW * 32)
 ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ items, int nitems,
               const float* __restrict__ in, float* __restrict__ out, int* __restrict__ counters, int parity)
@@ -337,14 +337,28 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
         const float w0 = (float)bi.w0, w1 = (float)bi.w1;
         const float* src = in + bi.off;
         // the region with periodic wraps (rows of axis 0, columns of axis 1),
-        // every copy in flight at once
+        // every copy in flight at once: 16-byte groups (ALIGNED), else cell by cell
         if (4 * g < cols) {
-            const int gz = wrapi(it.z0 - H + 4 * g, bi.n1);
             int gx = wrapi(it.x0 - H + rg, bi.n0);   // row of region row r, advanced without a division
-            for (int r = rg; r < rows; r += RG) {
-                cp_async16(&C[r * CI + 4 * g], src + (long long)gx * bi.n1 + gz);
-                gx += RG;
-                while (gx >= bi.n0) gx -= bi.n0;     // more than once only for grids smaller than a tile
+            if (ALIGNED) {
+                const int gz = wrapi(it.z0 - H + 4 * g, bi.n1);
+                for (int r = rg; r < rows; r += RG) {
+                    cp_async16(&C[r * CI + 4 * g], src + (long long)gx * bi.n1 + gz);
+                    gx += RG;
+                    while (gx >= bi.n0) gx -= bi.n0;     // more than once only for grids smaller than a tile
+                }
+            } else {
+                int gz[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) gz[q] = wrapi(it.z0 - H + 4 * g + q, bi.n1);
+                for (int r = rg; r < rows; r += RG) {
+                    const float* row = src + (long long)gx * bi.n1;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (4 * g + q < cols) cp_async4(&C[r * CI + 4 * g + q], row + gz[q]);
+                    gx += RG;
+                    while (gx >= bi.n0) gx -= bi.n0;
+                }
             }
         }
         cp_async_wait_all();
@@ -400,25 +414,40 @@ ch2_tb_kernel(const BatchInst* __restrict__ insts, const TbItem* __restrict__ it
             __syncthreads();
         }
         // the interior back to HBM
-        if (4 * g >= H && 4 * g < H + it.tz) {
+        if (ALIGNED) {
+            if (4 * g >= H && 4 * g < H + it.tz) {
+                float* dst = out + bi.off + (it.z0 - H + 4 * g);
+                for (int r = H + rg; r < H + it.tx; r += RG)
+                    *reinterpret_cast<float4*>(dst + (long long)(it.x0 - H + r) * bi.n1) =
+                        *reinterpret_cast<const float4*>(&C[r * CI + 4 * g]);
+            }
+        } else if (4 * g + 3 >= H && 4 * g < H + it.tz) {
             float* dst = out + bi.off + (it.z0 - H + 4 * g);
-            for (int r = H + rg; r < H + it.tx; r += RG)
-                *reinterpret_cast<float4*>(dst + (long long)(it.x0 - H + r) * bi.n1) =
-                    *reinterpret_cast<const float4*>(&C[r * CI + 4 * g]);
+            for (int r = H + rg; r < H + it.tx; r += RG) {
+                float* drow = dst + (long long)(it.x0 - H + r) * bi.n1;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (4 * g + q >= H && 4 * g + q < H + it.tz) drow[q] = C[r * CI + 4 * g + q];
+            }
         }
         __syncthreads();   // the region is reloaded by the next item
     }
 }
 
 namespace {
+template <int RI, int KS, int NW, bool AL>
+const void* tb_model_al(int model, bool unit)
+{
+    if (model == MMSP_GPU_CH)
+        return unit ? (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH, true, AL>
+                    : (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH, false, AL>;
+    return unit ? (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH_POLY, true, AL>
+                : (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH_POLY, false, AL>;
+}
 template <int RI, int KS, int NW>
 const void* tb_model(int model, bool unit)
 {
-    if (model == MMSP_GPU_CH)
-        return unit ? (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH, true>
-                    : (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH, false>;
-    return unit ? (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH_POLY, true>
-                : (const void*)&ch2_tb_kernel<RI, KS, NW, MMSP_GPU_CH_POLY, false>;
+    return tb_model_al<RI, KS, NW, true>(model, unit);
 }
 template <int RI, int NW>
 const void* tb_depth(int ks, int model, bool unit)
@@ -446,6 +475,8 @@ const void* tb_kernel(int shape, int ks, int model, bool unit)
 }
 
 size_t tb_smem(int shape) { return sizeof(float) * (size_t)kTbShapes[shape].ri * kTbCols; }
+
+const void* tb_kernel_any(int model, bool unit) { return tb_model_al<64, kTbAnyDepth, 4, false>(model, unit); }
 
 cudaError_t launch_tb(const void* fn, int blocks, int threads, size_t smem, const BatchInst* insts,
                       const TbItem* items, int nitems, const void* in, void* out, int* counters, int parity,

@@ -52,6 +52,11 @@ constexpr int kTbDepths[] = {2, 4, 8};
 
 const void* tb_kernel(int shape, int ks, int model, bool unit);   // FP32 only
 size_t tb_smem(int shape);
+// Single 2D FP32 Cahn-Hilliard grids of any row length (handles): region
+// shape 0 (64 x 128 cells, 4 warps) at depth kTbAnyDepth, loads and stores
+// cell by cell where rows are not a multiple of 4 cells.
+constexpr int kTbAnyDepth = 4;
+const void* tb_kernel_any(int model, bool unit);
 cudaError_t launch_tb(const void* fn, int blocks, int threads, size_t smem, const BatchInst* insts,
                       const TbItem* items, int nitems, const void* in, void* out, int* counters, int parity,
                       cudaStream_t s);

@@ -7,6 +7,8 @@
 #include "pf_internal.h"
 
 namespace pf {
+struct BatchInst;
+struct TbItem;
 // Device bytes of one block holding a handle's buffers (two states, the
 // reduction partials, the error words, a model's work grid), each 256-byte
 // aligned, for create_in.
@@ -40,10 +42,21 @@ struct mmsp_gpu_handle {
     bool timed;              // ev0/ev1 bracket the last step call
     bool external;           // buffers and stream belong to the caller (pf::create_in): not freed here
     int64_t steps;
-    // CUDA graph of kGraphSteps steps starting from buf[0] (an even count ends in buf[0])
+    // CUDA graph of kGraphSteps steps starting from buf[0] (an even count ends in buf[0]); for
+    // blocked handles, kGraphSteps / pf::kTbAnyDepth launches from buf[0] at an even launch count
     cudaGraphExec_t graph;
     pf::OutputState* out;    // snapshot writer (mmsp_gpu_output), created on first use
     unsigned last_iters;     // MMSP_GPU_CH_CONVEX: solver iterations of the last step
     cudaGraphExec_t cs_graph[2];   // MMSP_GPU_CH_CONVEX: one step (the solve's whole loop), per buf[cur]
+    // 2D FP32 Cahn-Hilliard: blocks of pf::kTbAnyDepth steps per launch of the
+    // temporally blocked kernel (its instance, tile list and work counters in `work`)
+    bool tb;
+    const void* tb_fn;
+    size_t tb_smem;
+    int tb_blocks, tb_items;
+    int64_t tb_launches;     // launches so far: their parity picks the work counter
+    pf::BatchInst* tb_inst;
+    pf::TbItem* tb_list;
+    int* tb_counters;
     char err[512];
 };

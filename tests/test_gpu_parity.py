@@ -470,6 +470,58 @@ def test_fp32_ac_row_warp_kernel_shapes(gpu, oracle, monkeypatch, tile, shape, f
     test_fp32_ac_stream_kernel_against_fp64_oracle(gpu, oracle, shape, fields, model)
 
 
+# 2D FP32 Cahn-Hilliard handles step in blocks of 4 steps per launch of the
+# temporally blocked kernel (64 x 128 regions), the leftover steps of a call
+# one per launch: rows of a multiple of 4 cells (16-byte copies) and not,
+# grids smaller than a region (wraps inside it), ragged edge tiles, a single
+# row, non-unit spacing, both models; graph replays, a start from the second
+# buffer at an even launch count (no graph), and calls of multiples of 4
+# steps equal one call bit for bit.
+TB_HANDLE = [(50, 77), (64, 64), (130, 512), (3, 33), (200, 1024), (97, 100), (1, 40), (33, 130)]
+
+
+@pytest.mark.parametrize("shape", TB_HANDLE, ids=["x".join(map(str, s)) for s in TB_HANDLE])
+def test_fp32_2d_blocked_handle(gpu, oracle, shape):
+    from mmsp_gb300 import inputs
+
+    poly = shape[0] % 2 == 1
+    x = inputs.noisy_composition(shape, 0.0 if poly else 0.45, 0.5 if poly else 0.05, 900 + shape[0])
+    if poly:
+        d = gpu.make_desc(shape, 1, np.float32, "ch_poly", r=1.0, u=1.0, kappa=1.0, mobility=1.0, dt=0.004)
+    else:
+        d = gpu.make_desc(shape, 1, np.float32, "ch", kappa=0.8, mobility=1.2, dt=0.003, dx=[1.0, 1.1])
+    x32 = x.astype(np.float32)
+    with gpu.Stepper(d) as s:
+        s.upload(x32)
+        for n in (8, 16, 13):          # 9 blocked launches, then one single step
+            s.step(n)
+        a = s.download()
+        s.upload(x32)
+        s.step(24)
+        s.step(13)
+        b = s.download()
+        s.upload(x32)
+        s.step(3)                      # three single steps: buffer 1 at an even launch count
+        s.step(300)                    # 75 blocked launches without the graph
+        c = s.download()
+        s.upload(x32)
+        s.step(300)                    # graph replays
+        s.step(3)
+        e = s.download()
+    assert np.array_equal(a, b)
+    if poly:
+        want37 = oracle.ch_shipped(x, 37, 1.0, 1.0, 1.0, 1.0, 0.004)
+        want303 = oracle.ch_shipped(x, 303, 1.0, 1.0, 1.0, 1.0, 0.004)
+    else:
+        want37 = oracle.ch_baseline(x, 37, 0.8, 1.2, 0.003, dx=[1.0, 1.1])
+        want303 = oracle.ch_baseline(x, 303, 0.8, 1.2, 0.003, dx=[1.0, 1.1])
+    scale = max(1.0, np.abs(want303).max())
+    assert np.abs(a.astype(np.float64) - want37).max() <= TOL_F32 * scale
+    assert np.abs(c.astype(np.float64) - want303).max() <= TOL_F32 * scale
+    assert np.abs(e.astype(np.float64) - want303).max() <= TOL_F32 * scale
+    assert np.abs(want303 - x).max() > 1e-3
+
+
 # FP32 Cahn-Hilliard grids that the streaming kernel does not take use the row
 # kernel (any row length, plain loads): 2D rows up to 1024 cells, 3D grids
 # with fewer than 12 rows per plane or rows shorter than 32 cells.
