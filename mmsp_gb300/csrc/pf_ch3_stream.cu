@@ -100,14 +100,16 @@ static __device__ __forceinline__ VT lap_v(VT sx, VT sy, VT sz, VT c, const F32C
 }
 
 // Threads of a block for rows of Z cells, V per thread: whole warps.
-static int ch3_threads(int Z, int V) { return (Z / V + 31) / 32 * 32; }
+static int ch3_threads(int Z, int V) { return ((Z + V - 1) / V + 31) / 32 * 32; }
 
-// Shared memory: kRing slots of (R+4) x Z floats, the warp-end mu buffers
+// Shared memory: kRing slots of (R+4) x ZS floats (ZS = Z, or Z + 1 for odd
+// rows of two cells per thread), the warp-end mu buffers
 // [parity][warp][side][R], then kRing mbarriers.
 static size_t ch3_smem(int R, int Z, int V)
 {
     const int warps = ch3_threads(Z, V) / 32;
-    return sizeof(float) * (size_t)kRing * (R + 4) * Z + sizeof(float) * 2 * warps * 2 * R +
+    const int ZS = V == 2 && Z % 2 ? Z + 1 : Z;
+    return sizeof(float) * (size_t)kRing * (R + 4) * ZS + sizeof(float) * 2 * warps * 2 * R +
            sizeof(uint64_t) * kRing;
 }
 
@@ -117,30 +119,36 @@ static size_t ch3_smem(int R, int Z, int V)
 // its timed-out exit (error word, bounded drain, return).  The host selects
 // it only through MMSP_GPU_TEST_STALL_LAUNCHES.
 // ZT: the row length when it is a compile-time constant (32..512 in powers
-// of two, ZT / V = TM threads), 0 when it is taken from the grid (a multiple
-// of V; blockDim.x = ch3_threads(Z, V) <= TM).  BULK: rows are 16-byte
-// multiples and thread 0 stages each plane with cp.async.bulk (one arrival,
+// of two, ZT / V = TM threads), 0 when it is taken from the grid
+// (blockDim.x = ch3_threads(Z, V) <= TM).  BULK: rows are 16-byte multiples
+// and thread 0 stages each plane with cp.async.bulk (one arrival,
 // transaction-counted); otherwise every thread copies its cells with 4- or
-// 8-byte cp.async and arrives when they land.
-template <int R, int ZT, int TM, int V, int MODEL, bool UNIT, bool STALL, bool BULK>
+// 8-byte cp.async and arrives when they land.  PAD: odd rows of two cells
+// per thread: shared rows hold Z + 1 cells, the extra one a copy of the
+// row's cell 0 (the periodic right neighbour of the last cell), the last
+// thread takes mu of cell 0 from the warp-end exchange for its second cell,
+// and stores are 4-byte (odd rows break 8-byte alignment).
+template <int R, int ZT, int TM, int V, int MODEL, bool UNIT, bool STALL, bool BULK, bool PAD>
 __global__ void __launch_bounds__(TM, TM <= 128 ? PF_CH3_MINB : (V == 1 && TM == 256 ? 2 : 1))
 ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, F32Coef q, int planes,
                int* __restrict__ err)
 {
     constexpr int RR = R + 4;
     static_assert(TM % 32 == 0 && R % 4 == 0 && (!ZT || ZT == TM * V), "row split");
+    static_assert(!PAD || (V == 2 && !ZT && !BULK), "odd rows: runtime rows, per-thread copies");
     const int Z = ZT ? ZT : g.Z;
+    const int ZS = PAD ? Z + 1 : Z;      // shared-memory row stride
     const int W = ZT ? TM / 32 : (int)(blockDim.x >> 5);   // warps per block
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
-    const int tl = Z / V - 1;            // the thread holding the row's last cells
+    const int tl = (Z + V - 1) / V - 1;  // the thread holding the row's last cells
     const bool real = ZT || t <= tl;     // past the row's end: compute on the last cells, store nothing
     const int z0 = (real ? t : tl) * V;  // first cell of this thread
     const int wlast = W - 1;             // (whole warps: the last warp holds the row's last cells)
     const int lane_last = warp == wlast ? (ZT ? 31 : tl & 31) : 31;   // this warp's last real lane
     extern __shared__ __align__(128) unsigned char sm[];
     float* slots = reinterpret_cast<float*>(sm);
-    float* edges = slots + (size_t)kRing * RR * Z;
+    float* edges = slots + (size_t)kRing * RR * ZS;
     uint64_t* bars = reinterpret_cast<uint64_t*>(edges + 2 * W * 2 * R);
     __shared__ int s_err;
 
@@ -149,7 +157,9 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     const int xe = min(xs + planes, g.X);
     if (xs >= xe) return;
     const int zl = z0 == 0 ? Z - 1 : z0 - 1;            // cell left of this thread's first
-    const int zh = z0 + V == Z ? 0 : z0 + V;            // cell right of this thread's last
+    // cell right of this thread's last (PAD: the last thread's second cell is
+    // the copy of cell 0, and its right neighbour, unused, is any cell)
+    const int zh = z0 + V >= Z ? z0 + V - Z : z0 + V;
     const int wl = warp == 0 ? wlast : warp - 1;
     const int wh = warp == wlast ? 0 : warp + 1;
     const int x_first = xs - 2, x_last = xe + 1;        // planes read from global memory
@@ -158,7 +168,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     auto fill = [&](int pl) {
         const int k = pl - x_first, s = k % kRing;
         uint64_t* bar = &bars[s];
-        float* dst = slots + (size_t)s * RR * Z;
+        float* dst = slots + (size_t)s * RR * ZS;
         const float* base = cin + (long long)wrapi(pl, g.X) * g.YZ;
         if constexpr (BULK) {
             const uint32_t row = (uint32_t)Z * sizeof(float);
@@ -181,14 +191,20 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
             if (STALL) return;   // no copies and no arrivals: the waits run out
             if (real)
                 for (int i = 0; i < RR; i++) {
-                    const float* src = base + (long long)wrapi(y0 - 2 + i, g.Y) * Z + z0;
-                    if (V == 2) cp_async8(dst + i * Z + z0, src);
-                    else cp_async4(dst + i * Z + z0, src);
+                    const float* row = base + (long long)wrapi(y0 - 2 + i, g.Y) * Z;
+                    if (PAD) {   // 4-byte copies: odd rows break 8-byte alignment; cell Z is cell 0
+                        cp_async4(dst + i * ZS + z0, row + z0);
+                        cp_async4(dst + i * ZS + z0 + 1, row + (z0 + 1 == Z ? 0 : z0 + 1));
+                    } else if (V == 2) {
+                        cp_async8(dst + i * ZS + z0, row + z0);
+                    } else {
+                        cp_async4(dst + i * ZS + z0, row + z0);
+                    }
                 }
             cp_async_arrive(bar);
         }
     };
-    auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % kRing) * RR * Z; };
+    auto slot_of = [&](int pl) -> const float* { return slots + (size_t)((pl - x_first) % kRing) * RR * ZS; };
     auto wait_plane = [&](int pl) {
         const int k = pl - x_first;
         if (!mbar_wait(&bars[k % kRing], (uint32_t)(k / kRing) & 1u, STALL ? 4u : kSpinLimit)) {
@@ -216,8 +232,8 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         const float* s1 = slot_of(x_first + 1) + z0;
 #pragma unroll
         for (int i = 0; i < RR; i++) {
-            cA[i] = *reinterpret_cast<const VT*>(s0 + i * Z);
-            cB[i] = *reinterpret_cast<const VT*>(s1 + i * Z);
+            cA[i] = *reinterpret_cast<const VT*>(s0 + i * ZS);
+            cB[i] = *reinterpret_cast<const VT*>(s1 + i * ZS);
         }
     }
 #pragma unroll
@@ -232,13 +248,13 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
         wait_plane(x + 2);
         const float* s2 = slot_of(x + 2) + z0;
 #pragma unroll
-        for (int i = 0; i < RR; i++) c[i] = *reinterpret_cast<const VT*>(s2 + i * Z);
+        for (int i = 0; i < RR; i++) c[i] = *reinterpret_cast<const VT*>(s2 + i * ZS);
         const float* s1 = slot_of(x + 1);
 #pragma unroll
         for (int r = -1; r <= R; r++) {
             const int i = r + 2;
-            const float left = s1[i * Z + zl];
-            const float right = s1[i * Z + zh];
+            const float left = s1[i * ZS + zl];
+            const float right = s1[i * ZS + zh];
             const VT cc = b[i];
             const VT lap = lap_v<UNIT>(vadd(a[i], c[i]), vadd(b[i - 1], b[i + 1]), vzsum(cc, left, right), cc, q);
             mc[r + 1] = mu_v<MODEL>(cc, lap, q);
@@ -263,11 +279,19 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
                 for (int r = 0; r < R; r += 4)
                     *reinterpret_cast<float4*>(e1 + r) = make_float4(vfirst(mc[r + 1]), vfirst(mc[r + 2]),
                                                                      vfirst(mc[r + 3]), vfirst(mc[r + 4]));
-            if (lane == lane_last)
+            if (lane == lane_last) {   // (PAD: the row's last real cell is the first of its pair)
+                if (PAD && warp == wlast) {
 #pragma unroll
-                for (int r = 0; r < R; r += 4)
-                    *reinterpret_cast<float4*>(e1 + R + r) = make_float4(vlast(mc[r + 1]), vlast(mc[r + 2]),
-                                                                         vlast(mc[r + 3]), vlast(mc[r + 4]));
+                    for (int r = 0; r < R; r += 4)
+                        *reinterpret_cast<float4*>(e1 + R + r) = make_float4(vfirst(mc[r + 1]), vfirst(mc[r + 2]),
+                                                                             vfirst(mc[r + 3]), vfirst(mc[r + 4]));
+                } else {
+#pragma unroll
+                    for (int r = 0; r < R; r += 4)
+                        *reinterpret_cast<float4*>(e1 + R + r) = make_float4(vlast(mc[r + 1]), vlast(mc[r + 2]),
+                                                                             vlast(mc[r + 3]), vlast(mc[r + 4]));
+                }
+            }
         }
         if (x >= xs) {
             // the neighbouring warps' end cells: every lane reads the same
@@ -290,9 +314,20 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
                 const float left = lane == 0 ? el[r] : up;
                 const float right = lane == lane_last ? eh[r] : down;
                 const VT m = mb[r + 1];
-                const VT lap = lap_v<UNIT>(vadd(ma[r + 1], mc[r + 1]), vadd(mb[r], mb[r + 2]), vzsum(m, left, right), m, q);
+                VT mz = m;   // PAD, last thread: the second cell's mu is that of cell 0
+                if constexpr (PAD) {
+                    if (warp == wlast && lane == lane_last) mz.y = eh[r];
+                }
+                const VT lap = lap_v<UNIT>(vadd(ma[r + 1], mc[r + 1]), vadd(mb[r], mb[r + 2]), vzsum(mz, left, right), m, q);
                 const VT o = vfma(vset<VT>(q.dtm), lap, a[r + 2]);
-                if (r < rows && real) *reinterpret_cast<VT*>(dst + (long long)r * Z) = o;
+                if constexpr (PAD) {
+                    if (r < rows && real) {
+                        dst[(long long)r * Z] = vfirst(o);
+                        if (z0 + 1 < Z) dst[(long long)r * Z + 1] = vlast(o);
+                    }
+                } else {
+                    if (r < rows && real) *reinterpret_cast<VT*>(dst + (long long)r * Z) = o;
+                }
             }
         }
         __syncthreads();
@@ -353,8 +388,8 @@ static int take_stall()
     return cur > 0 ? 1 : 0;
 }
 
-// cells per thread: 2 (packed FP32x2) for even rows, 1 for odd rows and 32-cell rows
-static int cells_per_thread(int Z) { return Z == 32 || Z % 2 ? 1 : 2; }
+// cells per thread: 2 (packed FP32x2), 1 for 32-cell rows
+static int cells_per_thread(int Z) { return Z == 32 ? 1 : 2; }
 
 bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
@@ -362,19 +397,19 @@ bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
            (d.model == MMSP_GPU_CH || d.model == MMSP_GPU_CH_POLY);
 }
 
-template <int ZT, int TM, int V, bool STALL, bool BULK>
+template <int ZT, int TM, int V, bool STALL, bool BULK, bool PAD = false>
 static const void* pick_mu(bool ch, bool unit)
 {
     if (ch)
-        return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, true, STALL, BULK>
-                    : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, false, STALL, BULK>;
-    return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, true, STALL, BULK>
-                : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, false, STALL, BULK>;
+        return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, true, STALL, BULK, PAD>
+                    : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, false, STALL, BULK, PAD>;
+    return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, true, STALL, BULK, PAD>
+                : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, false, STALL, BULK, PAD>;
 }
 
 // The kernel for rows of Z cells: a compile-time instance for rows of
 // 32..512 cells in powers of two (with its STALL form), else the runtime-row
-// instance whose thread bound covers Z / V (no STALL form: nullptr).
+// instance whose thread bound covers Z / 2 (no STALL form: nullptr).
 template <bool STALL>
 static const void* pick_stream(int Z, bool ch, bool unit)
 {
@@ -387,15 +422,12 @@ static const void* pick_stream(int Z, bool ch, bool unit)
     default: break;
     }
     if (STALL) return nullptr;
-    const int V = cells_per_thread(Z), T = ch3_threads(Z, V);
-    if (V == 2) {
-        const bool bulk = Z % 4 == 0;
-        if (T <= 128) return bulk ? pick_mu<0, 128, 2, false, true>(ch, unit) : pick_mu<0, 128, 2, false, false>(ch, unit);
-        return bulk ? pick_mu<0, 256, 2, false, true>(ch, unit) : pick_mu<0, 256, 2, false, false>(ch, unit);
-    }
-    if (T <= 128) return pick_mu<0, 128, 1, false, false>(ch, unit);
-    if (T <= 256) return pick_mu<0, 256, 1, false, false>(ch, unit);
-    return pick_mu<0, 512, 1, false, false>(ch, unit);
+    const int T = ch3_threads(Z, 2);
+    if (Z % 2) return T <= 128 ? pick_mu<0, 128, 2, false, false, true>(ch, unit)
+                               : pick_mu<0, 256, 2, false, false, true>(ch, unit);
+    const bool bulk = Z % 4 == 0;
+    if (T <= 128) return bulk ? pick_mu<0, 128, 2, false, true>(ch, unit) : pick_mu<0, 128, 2, false, false>(ch, unit);
+    return bulk ? pick_mu<0, 256, 2, false, true>(ch, unit) : pick_mu<0, 256, 2, false, false>(ch, unit);
 }
 
 cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)

@@ -362,12 +362,13 @@ def test_full_3d_ac_128_n8(gpu):
 # (partial last strip, periodic Y wrap at both ends, the smallest allowed Y,
 # a single warp per row, few X planes) and its row forms: compile-time rows
 # of 32..512 in powers of two; runtime rows with bulk copies (multiples of 4
-# cells), with per-thread 8-byte copies (even rows), with one cell per thread
-# (odd rows); a last warp that the row fills only in part (the warp-end mu
-# exchange and the periodic wrap from its last real lane).
+# cells), with per-thread 8-byte copies (even rows), odd rows (a padded
+# shared row whose extra cell is the row's cell 0); a last warp that the row
+# fills only in part (the warp-end mu exchange and the periodic wrap from its
+# last real lane), down to lane 0 alone.
 STREAM_SHAPES = [(16, 24, 64), (20, 13, 32), (5, 12, 96), (3, 40, 256), (33, 17, 128), (1, 16, 32),
                  (7, 13, 243), (4, 12, 33), (6, 20, 50), (3, 14, 198), (2, 12, 300), (2, 12, 301), (3, 17, 190),
-                 (4, 12, 36)]
+                 (4, 12, 36), (3, 12, 63), (2, 13, 65)]
 
 
 @pytest.mark.parametrize("shape", STREAM_SHAPES, ids=["x".join(map(str, s)) for s in STREAM_SHAPES])
