@@ -3,8 +3,8 @@
 // cp.async.bulk copies a contiguous global range into shared memory and
 // signals completion on an mbarrier with a transaction count.  Addresses must
 // be 16-byte aligned and sizes multiples of 16 bytes; callers guarantee it.
-// Every wait is bounded: mbar_wait returns false after kSpinLimit polls so a
-// kernel can raise its error flag and leave instead of hanging.
+// Every wait is bounded: mbar_wait returns false after 2 s of the global
+// timer, so a kernel can raise its error flag and leave instead of hanging.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -12,7 +12,7 @@
 
 namespace pf {
 
-constexpr uint32_t kSpinLimit = 1u << 14;     // polls of try_wait before giving up
+constexpr uint32_t kSpinLimit = 1u << 14;     // mbar_wait's default: the time bound below, not a poll count
 constexpr uint32_t kSuspendHintNs = 100000;  // each poll may sleep this long unless the phase completes
 
 static __device__ __forceinline__ uint32_t smem_addr(const void* p)
@@ -66,12 +66,32 @@ static __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t par
     return ok != 0;
 }
 
-// Bounded wait for phase `parity` of `bar` to complete: at most `limit` polls.
+// Nanoseconds of the GPU's global timer.
+static __device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr uint64_t kWaitNs = 2000000000ull;   // a wait gives up after 2 s of the global timer
+
+// Bounded wait for phase `parity` of `bar` to complete: until kWaitNs has
+// passed (the bound is time, not polls: a poll may return at once, so a
+// count of polls can run out while a copy is merely slow), or, with an
+// explicit `limit` (the failure-detection test), at most `limit` polls.
 static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kSpinLimit)
 {
-    for (uint32_t i = 0; i < limit; i++)
+    if (limit != kSpinLimit) {
+        for (uint32_t i = 0; i < limit; i++)
+            if (mbar_try_wait(bar, parity)) return true;
+        return false;
+    }
+    const uint64_t t0 = global_ns();
+    while (true) {
         if (mbar_try_wait(bar, parity)) return true;
-    return false;
+        if (global_ns() - t0 > kWaitNs) return false;
+    }
 }
 
 // Global -> shared bulk copy of `bytes` (multiple of 16, both ends 16-byte
