@@ -100,7 +100,7 @@ static __device__ __forceinline__ T order_sum(const T* __restrict__ s, long long
 
 // Both passes run on (y, z) columns: a block of kOstZ x kOstY threads over a
 // run of kOstPlanes X planes (coalesced rows, no per-cell division).
-constexpr int kOstZ = 32, kOstY = 4, kOstPlanes = 16;
+constexpr int kOstZ = 32, kOstY = 4, kOstPlanes = 8;
 
 // Pass 1, ostwald.cpp:95-99:
 //   w = -A*(C-Cm) + B*pow(C-Cm,3) + Da*pow(C-Ca,3) + Db*pow(C-Cb,3) - g*(C-Ca)*sum - kappa*lap C
