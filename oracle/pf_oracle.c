@@ -144,8 +144,6 @@ int pfo_laplacian(const pfo_grid* g, const double* in, double* out)
     return 0;
 }
 
-/* Two-pass explicit Cahn-Hilliard in the structure of cahn-hilliard.cpp:65-80.
- * form 0: BASELINE free energy, form 1: the shipped polynomial. */
 /* Value j of the SplitMix64 stream `seed` (Steele, Lea and Flood, OOPSLA
  * 2014), as mmsp_gb300/inputs.py and the device compute it. */
 static uint64_t splitmix64_at(uint64_t seed, uint64_t j)
@@ -173,6 +171,9 @@ static inline double noise_at(double nstd, uint64_t seed, long long step, long c
     return 0.0 + pfo_gaussian(seed, (uint64_t)step * (uint64_t)cells + (uint64_t)i) * nstd;
 }
 
+/* Two-pass explicit Cahn-Hilliard in the structure of cahn-hilliard.cpp:65-80.
+ * form 0: the configured free energy f = c^2 (1-c)^2, form 1: the shipped
+ * polynomial. */
 static int ch_run(const pfo_grid* g, double* c, int steps, int form,
                   double r, double u, double K, double M, double dt, int threads,
                   double nstd, uint64_t seed, long long step0)
@@ -242,7 +243,7 @@ int pfo_ch_shipped_noise(const pfo_grid* g, double* c, int steps, double r, doub
 }
 
 /* Single-pass multi-field Allen-Cahn in the structure of graingrowth.cpp:86-110.
- * form 0: BASELINE free energy with gamma; form 1: graingrowth.cpp:105 as
+ * form 0: the configured free energy with gamma; form 1: graingrowth.cpp:105 as
  * shipped; form 2: allen-cahn.cpp:70 as shipped (N must be 1); form 3:
  * isotropic phase-field Zener pinning as shipped
  * (examples/coarsening/zener_pinning/isotropic/phase_field/zener.cpp:121-138):
