@@ -671,10 +671,9 @@ def batched(native, inputs, stream, reps, flush):
     for _ in range(max(2, reps // 2)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for i, h in enumerate(pin_in):
-            b.upload(i, h)
+        b.upload_all(pin_in)
         b.step(BATCH_STEPS)
-        res = [b.download(i, pin_out[i]) for i in range(len(work))]
+        res = b.download_all(pin_out)
         e2e.append(time.perf_counter() - t0)
     e2e_s = float(np.mean(e2e))
     b.close()

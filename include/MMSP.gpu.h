@@ -354,6 +354,11 @@ int mmsp_gpu_batch_set_stream(mmsp_gpu_batch* b, void* cuda_stream);
 /* Copy grid `index` in/out (synchronous), as mmsp_gpu_upload/download. */
 int mmsp_gpu_batch_upload(mmsp_gpu_batch* b, int index, const void* host, size_t bytes, int layout);
 int mmsp_gpu_batch_download(mmsp_gpu_batch* b, int index, void* host, size_t bytes, int layout);
+/* Every grid in one call: host[i] is grid i's buffer of its state size (as
+ * mmsp_gpu_batch_upload/download); the copies are queued back to back and
+ * the call synchronises once.  Synchronous. */
+int mmsp_gpu_batch_upload_all(mmsp_gpu_batch* b, const void* const* host, int layout);
+int mmsp_gpu_batch_download_all(mmsp_gpu_batch* b, void* const* host, int layout);
 /* Advance every grid by `steps` steps (asynchronous). */
 int mmsp_gpu_batch_step(mmsp_gpu_batch* b, int steps);
 int mmsp_gpu_batch_synchronize(mmsp_gpu_batch* b);

@@ -234,28 +234,22 @@ static int bcheck_io(mmsp_gpu_batch* b, int index, const void* p, size_t bytes, 
     return MMSP_GPU_OK;
 }
 
-extern "C" int mmsp_gpu_batch_upload(mmsp_gpu_batch* b, int index, const void* host, size_t bytes, int layout)
+// Queue grid `index`'s upload / download on the batch stream (no synchronisation).
+static cudaError_t queue_upload(mmsp_gpu_batch* b, int index, const void* host, size_t bytes, int layout)
 {
-    int rc = bcheck_io(b, index, host, bytes, layout);
-    if (rc) return rc;
     const Member& mm = b->m[index];
     char* dst = (char*)b->pool[b->cur] + mm.off * b->esize;
-    cudaError_t e;
     if (layout == MMSP_GPU_CELL_MAJOR && mm.d.fields > 1) {
         char* tmp = (char*)b->pool[b->cur ^ 1] + mm.off * b->esize;   // idle pool as staging
-        e = cudaMemcpyAsync(tmp, host, bytes, cudaMemcpyHostToDevice, b->stream);
+        cudaError_t e = cudaMemcpyAsync(tmp, host, bytes, cudaMemcpyHostToDevice, b->stream);
         if (e == cudaSuccess) e = launch_transpose(b->dtype, tmp, dst, mm.g.cells, mm.d.fields, true, b->stream);
-    } else {
-        e = cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, b->stream);
+        return e;
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-    return e == cudaSuccess ? MMSP_GPU_OK : bcuda(b, e, "batch upload");
+    return cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, b->stream);
 }
 
-extern "C" int mmsp_gpu_batch_download(mmsp_gpu_batch* b, int index, void* host, size_t bytes, int layout)
+static cudaError_t queue_download(mmsp_gpu_batch* b, int index, void* host, size_t bytes, int layout)
 {
-    int rc = bcheck_io(b, index, host, bytes, layout);
-    if (rc) return rc;
     const Member& mm = b->m[index];
     const char* src = (const char*)b->pool[b->cur] + mm.off * b->esize;
     cudaError_t e = cudaSuccess;
@@ -265,12 +259,62 @@ extern "C" int mmsp_gpu_batch_download(mmsp_gpu_batch* b, int index, void* host,
         src = tmp;
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, b->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-    if (e != cudaSuccess) return bcuda(b, e, "batch download");
+    return e;
+}
+
+// After a download: a step kernel's timed-out wait leaves its word set.
+static int check_wait_word(mmsp_gpu_batch* b)
+{
     int f = 0;
     if (cudaMemcpy(&f, b->counters + 2, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && f)
         return bfail(b, MMSP_GPU_ETIMEDOUT, "a step kernel's bounded wait ran out");
     return MMSP_GPU_OK;
+}
+
+extern "C" int mmsp_gpu_batch_upload(mmsp_gpu_batch* b, int index, const void* host, size_t bytes, int layout)
+{
+    int rc = bcheck_io(b, index, host, bytes, layout);
+    if (rc) return rc;
+    cudaError_t e = queue_upload(b, index, host, bytes, layout);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    return e == cudaSuccess ? MMSP_GPU_OK : bcuda(b, e, "batch upload");
+}
+
+extern "C" int mmsp_gpu_batch_download(mmsp_gpu_batch* b, int index, void* host, size_t bytes, int layout)
+{
+    int rc = bcheck_io(b, index, host, bytes, layout);
+    if (rc) return rc;
+    cudaError_t e = queue_download(b, index, host, bytes, layout);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "batch download");
+    return check_wait_word(b);
+}
+
+extern "C" int mmsp_gpu_batch_upload_all(mmsp_gpu_batch* b, const void* const* host, int layout)
+{
+    if (!b || !host) return MMSP_GPU_EINVAL;
+    for (int i = 0; i < (int)b->m.size(); i++) {
+        int rc = bcheck_io(b, i, host[i], b->m[i].bytes, layout);
+        if (rc) return rc;
+    }
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < (int)b->m.size() && e == cudaSuccess; i++) e = queue_upload(b, i, host[i], b->m[i].bytes, layout);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    return e == cudaSuccess ? MMSP_GPU_OK : bcuda(b, e, "batch upload");
+}
+
+extern "C" int mmsp_gpu_batch_download_all(mmsp_gpu_batch* b, void* const* host, int layout)
+{
+    if (!b || !host) return MMSP_GPU_EINVAL;
+    for (int i = 0; i < (int)b->m.size(); i++) {
+        int rc = bcheck_io(b, i, host[i], b->m[i].bytes, layout);
+        if (rc) return rc;
+    }
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < (int)b->m.size() && e == cudaSuccess; i++) e = queue_download(b, i, host[i], b->m[i].bytes, layout);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "batch download");
+    return check_wait_word(b);
 }
 
 // ---------------------------------------------------------------------------

@@ -39,7 +39,7 @@ EXPORTS = [
     "mmsp_gpu_sparse_upload", "mmsp_gpu_sparse_download",
     "mmsp_gpu_output_opts_init", "mmsp_gpu_write_grid", "mmsp_gpu_output", "mmsp_gpu_output_wait",
     "mmsp_gpu_batch_create", "mmsp_gpu_batch_destroy", "mmsp_gpu_batch_set_stream", "mmsp_gpu_batch_upload",
-    "mmsp_gpu_batch_download", "mmsp_gpu_batch_step", "mmsp_gpu_batch_synchronize", "mmsp_gpu_batch_reduce",
+    "mmsp_gpu_batch_download", "mmsp_gpu_batch_upload_all", "mmsp_gpu_batch_download_all", "mmsp_gpu_batch_step", "mmsp_gpu_batch_synchronize", "mmsp_gpu_batch_reduce",
     "mmsp_gpu_batch_tune", "mmsp_gpu_batch_get_info", "mmsp_gpu_batch_last_error",
     "mmsp_gpu_server_start", "mmsp_gpu_server_submit", "mmsp_gpu_server_poll", "mmsp_gpu_server_wait",
     "mmsp_gpu_server_fetch", "mmsp_gpu_server_cancel", "mmsp_gpu_server_get_stats", "mmsp_gpu_server_stop",
@@ -149,6 +149,8 @@ def load(build_if_missing: bool = False):
         "mmsp_gpu_batch_set_stream": (i, [vp, vp]),
         "mmsp_gpu_batch_upload": (i, [vp, i, vp, sz, i]),
         "mmsp_gpu_batch_download": (i, [vp, i, vp, sz, i]),
+        "mmsp_gpu_batch_upload_all": (i, [vp, ctypes.POINTER(vp), i]),
+        "mmsp_gpu_batch_download_all": (i, [vp, ctypes.POINTER(vp), i]),
         "mmsp_gpu_batch_step": (i, [vp, i]),
         "mmsp_gpu_batch_synchronize": (i, [vp]),
         "mmsp_gpu_batch_reduce": (i, [vp, i, ctypes.POINTER(Stats)]),
@@ -422,6 +424,33 @@ class Batch:
         _bcheck(self.L.mmsp_gpu_batch_download(self.b, i, out.ctypes.data, out.nbytes, CELL_MAJOR), self.b,
                 "download")
         return out
+
+    def upload_all(self, arrs):
+        """Every grid's state in one call (one synchronisation)."""
+        keep = []
+        for i, arr in enumerate(arrs):
+            a = np.ascontiguousarray(arr, dtype=self.dtype)
+            if a.shape != self._shape(i):
+                raise ValueError("grid %d: shape %s, expected %s" % (i, a.shape, self._shape(i)))
+            keep.append(a)
+        if len(keep) != len(self.descs):
+            raise ValueError("expected %d arrays" % len(self.descs))
+        ptrs = (ctypes.c_void_p * len(keep))(*[a.ctypes.data for a in keep])
+        _bcheck(self.L.mmsp_gpu_batch_upload_all(self.b, ptrs, CELL_MAJOR), self.b, "upload_all")
+
+    def download_all(self, outs=None):
+        """Every grid's state in one call; into `outs` (C-contiguous arrays of
+        each grid's shape and dtype) when given."""
+        if outs is None:
+            outs = [np.empty(self._shape(i), dtype=self.dtype) for i in range(len(self.descs))]
+        if len(outs) != len(self.descs):
+            raise ValueError("expected %d arrays" % len(self.descs))
+        for i, o in enumerate(outs):
+            if o.shape != self._shape(i) or o.dtype != self.dtype or not o.flags.c_contiguous:
+                raise ValueError("grid %d: expected a C-contiguous %s array of shape %s" % (i, self.dtype, self._shape(i)))
+        ptrs = (ctypes.c_void_p * len(outs))(*[o.ctypes.data for o in outs])
+        _bcheck(self.L.mmsp_gpu_batch_download_all(self.b, ptrs, CELL_MAJOR), self.b, "download_all")
+        return outs
 
     def step(self, steps: int):
         _bcheck(self.L.mmsp_gpu_batch_step(self.b, int(steps)), self.b, "step")

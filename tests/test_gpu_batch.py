@@ -52,6 +52,30 @@ def make_batch(gpu, members, dtype):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_batch_whole_transfers(gpu, dtype):
+    """upload_all / download_all (every grid in one call, one synchronisation)
+    move the same bytes as the per-grid calls, cell-major vector grids
+    included, before and after steps."""
+    members = mixed_members(dtype)
+    b = make_batch(gpu, members, dtype)
+    try:
+        xs = [x.astype(dtype) for _, x, _ in members]
+        assert all(np.array_equal(o, x) for o, x in zip(b.download_all(), xs))
+        b.step(37)
+        one = [b.download(i) for i in range(len(members))]
+        allv = b.download_all()
+        assert all(np.array_equal(o, a) for o, a in zip(one, allv))
+        b.upload_all(xs)
+        b.step(37)
+        again = b.download_all()
+        assert all(np.array_equal(o, a) for o, a in zip(one, again))
+        with pytest.raises(ValueError):
+            b.upload_all(xs[:-1])
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_batch_matches_single_grid_updates(gpu, oracle, dtype):
     members = mixed_members(dtype)
     b = make_batch(gpu, members, dtype)
