@@ -374,12 +374,15 @@ static int setup_tb(mmsp_gpu_handle* h)
     h->tb_fn = aligned ? pf::tb_kernel(0, pf::kTbAnyDepth, h->d.model, h->c.unit_w)
                        : pf::tb_kernel_any(h->d.model, h->c.unit_w);
     h->tb_smem = pf::tb_smem(0);
+    // Queued on the handle's stream, ahead of its first launch, with no
+    // synchronisation: a server request's stream may carry another request's
+    // queued steps.  A copy from pageable memory has staged its source when
+    // the call returns, so the host arrays may go out of scope.
     cudaError_t e = cudaMemcpyAsync(h->tb_inst, &bi, sizeof(bi), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h->tb_list, items.data(), sizeof(pf::TbItem) * items.size(), cudaMemcpyHostToDevice,
                             h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->tb_counters, 0, 256, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);   // the host arrays go out of scope
     if (e == cudaSuccess) e = pf::ensure_smem(h->tb_fn, h->tb_smem);
     int per_sm = 0;
     if (e == cudaSuccess)

@@ -42,7 +42,7 @@
 
 namespace {
 
-constexpr int kStreams = 128;      // streams shared round-robin by running requests (half high priority)
+constexpr int kStreams = 128;      // streams for running requests, each given the least-used one of its priority class (half high priority)
 constexpr long long kSmallValues = 1ll << 21;   // requests of at most this many values take high-priority streams
 constexpr int kInFlight = 2;       // chunks queued ahead per request
 constexpr size_t kGranule = 256;
@@ -58,6 +58,7 @@ struct Request {
     size_t block_off = 0, block_bytes = 0;
     mmsp_gpu_handle* h = nullptr;
     cudaStream_t stream = nullptr;
+    int stream_index = -1;             // into the server's streams (scheduler thread)
     int state = MMSP_GPU_REQ_QUEUED;
     std::atomic<bool> cancel{false};
     int64_t queued = 0;                // steps queued on the device so far
@@ -135,7 +136,7 @@ struct mmsp_gpu_server {
     mmsp_gpu_server_stats st;
     Pool pool;                    // the scheduler thread alone touches it
     cudaStream_t streams[kStreams] = {};   // [0, kStreams/2): high priority; the rest: low
-    int next_stream[2] = {0, 0};
+    int stream_users[kStreams] = {};        // running requests on each stream
 };
 
 static double since(const mmsp_gpu_server* s) { return std::chrono::duration<double>(Clock::now() - s->t0).count(); }
@@ -156,6 +157,8 @@ static void finish(mmsp_gpu_server* s, Request* r, int state)
 static void release_request(mmsp_gpu_server* s, Request* r)
 {
     if (r->stream) cudaStreamSynchronize(r->stream);
+    if (r->stream_index >= 0) s->stream_users[r->stream_index]--;
+    r->stream_index = -1;
     if (r->h) {
         mmsp_gpu_destroy(r->h);
         r->h = nullptr;
@@ -200,9 +203,14 @@ static int start_request(mmsp_gpu_server* s, Request* r)
     const long long values = (long long)r->d.n[0] * (r->d.dim > 1 ? r->d.n[1] : 1) * (r->d.dim > 2 ? r->d.n[2] : 1) *
                              r->d.fields;
     const int pri = values <= kSmallValues ? 0 : 1;
-    int& next = s->next_stream[pri];
-    r->stream = s->streams[pri * (kStreams / 2) + next];
-    next = (next + 1) % (kStreams / 2);
+    // the least-used stream of the class: a stream shared with another running
+    // request would make this request's synchronisations wait for its steps
+    int best = pri * (kStreams / 2);
+    for (int i = best + 1; i < (pri + 1) * (kStreams / 2); i++)
+        if (s->stream_users[i] < s->stream_users[best]) best = i;
+    s->stream_users[best]++;
+    r->stream_index = best;
+    r->stream = s->streams[best];
     for (auto& e : r->ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
