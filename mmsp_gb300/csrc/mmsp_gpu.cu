@@ -573,7 +573,7 @@ static cudaError_t one_step(mmsp_gpu_handle* h, cudaStream_t s)
     const void* in = h->buf[h->cur];
     void* out = h->buf[h->cur ^ 1];
     const pf::Coeffs& c = h->c;
-    cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, c, in, out, h->work, s)
+    cudaError_t e = h->d.model == MMSP_GPU_OSTWALD ? pf::launch_ostwald(h->plan, h->d, h->g, c, in, out, h->work, h->flags, s)
                     : h->plan.kind == 6 ? pf::launch_ch64(h->plan, h->d, h->g, c, in, out, h->work, h->flags, s)
                     : h->plan.kind == 7 ? pf::launch_sparse_gg(h->d, h->g, c, in, out, h->flags, s)
                     : ch ? pf::launch_ch(h->plan, h->d, h->g, c, in, out, h->flags, s)

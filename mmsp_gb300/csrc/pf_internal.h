@@ -84,7 +84,8 @@ struct StepPlan {
     int fields;
     int kind;          // 0: generic tile kernel, 1: FP32 3D CH streaming, 2: FP32 3D AC streaming,
                        // 3: FP32 CH rows of any length, 4: Ostwald ripening (two kernels),
-                       // 5: convex splitting, 6: FP64 CH in two passes through a work grid
+                       // 5: convex splitting, 6: FP64 CH in two passes through a work grid,
+                       // 8: FP32 3D Ostwald ripening streaming (one kernel)
     int ring;          // planes in the shared-memory ring (streaming kernels)
     bool ok;
 };
@@ -135,10 +136,16 @@ cudaError_t launch_ac(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, 
                       const void* in, void* out, int* err, cudaStream_t s);
 
 // Ostwald ripening (pf_ostwald.cu): the chemical potential of the
-// composition into `work` (cells values), then the update of every field.
+// composition into `work` (cells values), then the update of every field;
+// FP32 3D grids with rows of 32, 64 or 128 cells and 2..4 fields take the
+// one-kernel streaming step of pf_ost3_stream.cu instead (plan kind 8).
 cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p);
 cudaError_t launch_ostwald(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
-                           const void* in, void* out, void* work, cudaStream_t s);
+                           const void* in, void* out, void* work, int* err, cudaStream_t s);
+bool ost3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g);
+cudaError_t plan_ost3_stream(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, StepPlan* p);
+cudaError_t launch_ost3_stream(const StepPlan& p, const Geom& g, const OstConst& o, const Coeffs& c,
+                               const void* in, void* out, int* err, cudaStream_t s);
 
 // Convex-splitting Cahn-Hilliard (pf_convex.cu).  One red-black sweep
 // (color 1, then color 0 as the example orders them) of the guess `nw`

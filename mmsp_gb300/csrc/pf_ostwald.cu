@@ -14,6 +14,8 @@
 // FP64 follows the reference's operation order with separately rounded
 // operations (pow(x,3) as the compensated cube of pf_device.cuh, pow(x,2)
 // as x*x); FP32 uses the same expressions in float.
+#include <stdlib.h>
+
 #include "pf_device.cuh"
 #include "pf_internal.h"
 
@@ -233,6 +235,7 @@ static void ost_pick(int dim, bool unit, int N, const void** mu, const void** up
 cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 {
     const Coeffs c = make_coeffs(d);
+    if (ost3_stream_eligible(d, g) && !getenv("MMSP_GPU_OST_TWO_KERNELS")) return plan_ost3_stream(d, g, c, p);
     const void* up = nullptr;
     if (d.dtype == MMSP_GPU_F64) ost_pick<double>(g.dim, c.unit_w, d.fields, &p->fn, &up);
     else ost_pick<float>(g.dim, c.unit_w, d.fields, &p->fn, &up);
@@ -250,8 +253,9 @@ cudaError_t plan_ostwald(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
 }
 
 cudaError_t launch_ostwald(const StepPlan& p, const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c,
-                           const void* in, void* out, void* work, cudaStream_t s)
+                           const void* in, void* out, void* work, int* err, cudaStream_t s)
 {
+    if (p.kind == 8) return launch_ost3_stream(p, g, c.ost, c, in, out, err, s);
     const void* mu = nullptr;
     const void* up = nullptr;
     int n = d.fields;

@@ -585,6 +585,38 @@ def test_ostwald_fp32_and_fp64_against_oracle(gpu, oracle, shape, fields):
     assert abs(got64[..., 0].sum() - x[..., 0].sum()) < 1e-9 * x[..., 0].size
 
 
+# FP32 3D grids with rows of 32, 64 or 128 cells and 2..4 fields take the
+# one-kernel streaming step (strips of 16 rows, 8 for 128-cell rows): ragged
+# last strips, short plane runs, non-unit spacing.
+OST_STREAM = [((6, 21, 32), 2, None), ((5, 40, 64), 3, None), ((4, 13, 128), 4, None), ((9, 20, 64), 2, None),
+              ((7, 24, 64), 2, (1.0, 0.8, 1.25))]
+
+
+@pytest.mark.parametrize("shape,fields,dx", OST_STREAM,
+                         ids=["%s-%d-%s" % ("x".join(map(str, s)), f, "unit" if h is None else "dx")
+                              for s, f, h in OST_STREAM])
+def test_ostwald_stream_kernel_against_oracle(gpu, oracle, shape, fields, dx):
+    """The one-kernel FP32 Ostwald step within the precision-form tolerance
+    of the FP64 oracle, and close to the two-kernel FP32 path (selected by
+    MMSP_GPU_OST_TWO_KERNELS at planning)."""
+    from mmsp_gb300 import inputs
+
+    x = inputs.ostwald_start(shape, fields, 70 + fields)
+    steps = 120
+    want = oracle.ostwald(x, steps, dx=dx)
+    d32 = gpu.make_desc(shape, fields, np.float32, "ostwald", dx=dx)
+    got = run_gpu(gpu, d32, x.astype(np.float32), steps).astype(np.float64)
+    assert np.abs(got - want).max() <= TOL_F32
+    assert np.abs(want - x).max() > 1e-3
+    os.environ["MMSP_GPU_OST_TWO_KERNELS"] = "1"
+    try:
+        two = run_gpu(gpu, d32, x.astype(np.float32), steps).astype(np.float64)
+    finally:
+        del os.environ["MMSP_GPU_OST_TWO_KERNELS"]
+    assert np.abs(two - want).max() <= TOL_F32
+    assert np.abs(got - two).max() <= 2e-6
+
+
 def ostwald_energy(x, dx, Ca=0.05, Cb=0.95, A=2.0, delta=1.0, eps=3.0, kappa=2.0):
     """The free energy the library reports for the Ostwald model, in numpy:
     -A/2 (C-Cm)^2 + B/4 (C-Cm)^4 + Da/4 (C-Ca)^4 + Db/4 (C-Cb)^4 - g/2 (C-Ca)^2 sum e^2
