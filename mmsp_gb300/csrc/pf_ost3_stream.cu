@@ -13,16 +13,16 @@
 //   all fields arrive in shared memory on an mbarrier ring by cp.async.bulk
 //   (rows are 16-byte multiples), D planes deep: planes x-1 .. x+2 are in
 //   use while plane x is updated, the rest are copies in flight.
-// * For plane x the block first computes w(x+1) on rows -1..R into a ring of
-//   three w planes in shared memory, then updates plane x from w(x-1),
-//   w(x), w(x+1) and the staged fields.  w never goes to global memory:
-//   each step reads the state once (plus halo re-reads that hit L2) and
-//   writes it once.
+// * A warp owns RT consecutive rows of the strip.  For plane x it computes
+//   w(x+1) on its rows and one row either side (the neighbouring warps
+//   compute those rows again), then updates plane x from w(x-1), w(x),
+//   w(x+1), which stay in its registers, and the staged fields.  w never
+//   goes to shared or global memory, the warps meet only at one barrier per
+//   plane (the release of a ring slot), and each step reads the state once
+//   (plus halo re-reads that hit L2) and writes it once.
 // * A warp spans a row, V = Z/32 adjacent cells per lane; Z neighbours at a
 //   lane's ends come from the adjacent lanes by shuffle (lane 0 and lane 31
-//   are neighbours: the periodic wrap of the row).  Warps take w rows in
-//   turn and RT consecutive rows of the update, whose Y neighbours stay in
-//   registers.
+//   are neighbours: the periodic wrap of the row).
 //
 // FP32 arithmetic is regrouped for throughput (neighbour sums before the
 // weights); the result is checked against the FP64 oracle with a
@@ -88,24 +88,25 @@ __global__ void __launch_bounds__(32 * TY)
 ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g, OstF32 q, int planes,
                 int* __restrict__ err)
 {
-    constexpr int Z = 32 * V, R = TY * RT, RR = R + 4, WR = R + 2;
+    constexpr int Z = 32 * V, R = TY * RT, RR = R + 4;
     constexpr int FS = RR * Z;        // floats of one field's rows in a slot
     constexpr int SS = NF * FS;       // floats of a slot
     static_assert(D >= 5 && NF >= 2, "ring depth, fields");
     extern __shared__ __align__(128) unsigned char sm[];
     float* ring = reinterpret_cast<float*>(sm);
-    float* wring = ring + D * SS;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(wring + 3 * WR * Z);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(ring + D * SS);
 
     const int t = threadIdx.x, lane = t & 31, ty = t >> 5;
     const int z0 = lane * V;
+    const int r0 = ty * RT;           // this warp's first row of the strip
     const int y0 = blockIdx.x * R;
     const int xs = blockIdx.y * planes, xe = min(xs + planes, g.X);
     if (xs >= xe) return;
     const int x_first = xs - 2, x_last = xe + 1;   // planes read from global memory
     const long long cells = g.cells;
 
-    // thread 0: stage plane pl (wrapped) of every field into its slot
+    // thread 0: stage plane pl (wrapped) of every field into its slot; slot
+    // row i holds strip row i-2
     auto fill = [&](int pl) {
         const int k = pl - x_first, s = k % D;
         uint64_t* bar = &bars[s];
@@ -132,88 +133,80 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
         }
     };
     auto slot = [&](int pl) -> const float* { return ring + ((pl - x_first) % D) * SS; };
-    auto wslot = [&](int xp) -> float* { return wring + ((xp - x_first) % 3) * WR * Z; };
     auto arrived = [&](int pl) {
         const int k = pl - x_first;
         return mbar_wait(&bars[k % D], (uint32_t)(k / D) & 1u);
     };
 
-    // w(xp) on rows -1..R (ostwald.cpp:95-99):
+    // w(xp) on this warp's rows r0-1 .. r0+RT (ostwald.cpp:95-99), into w:
     //   w = -A*(C-Cm) + B*(C-Cm)^3 + Da*(C-Ca)^3 + Db*(C-Cb)^3 - g*(C-Ca)*sum - kappa*lap C
-    // with sum the squares of the order parameters; planes xp-1, xp, xp+1 staged.
-    auto compute_w = [&](int xp) {
+    // with sum the squares of the order parameters; planes xp-1, xp, xp+1
+    // staged.  The rows either side of the warp's own are computed again by
+    // the neighbouring warps, so w never leaves registers.
+    auto compute_w = [&](int xp, float (&w)[RT + 2][V]) {
         const float* sl = slot(xp - 1);
         const float* sc = slot(xp);
         const float* sh = slot(xp + 1);
-        float* wd = wslot(xp);
-        for (int r = ty - 1; r <= R; r += TY) {
-            const int o = (r + 2) * Z + z0;
-            float c[V], cu[V], cd[V], xh[V], xl[V], sz[V], sum[V];
-            ldv<V>(sc + o, c);
-            ldv<V>(sc + o - Z, cd);
-            ldv<V>(sc + o + Z, cu);
+        float c[RT + 4][V];   // C(xp) on rows r0-2 .. r0+RT+1 (slot rows r0 .. r0+RT+3)
+#pragma unroll
+        for (int k = 0; k < RT + 4; k++) ldv<V>(sc + (r0 + k) * Z + z0, c[k]);
+#pragma unroll
+        for (int k = 0; k < RT + 2; k++) {   // row r0-1+k
+            const int o = (r0 + 1 + k) * Z + z0;
+            float xh[V], xl[V], sz[V], sum[V], e[V];
             ldv<V>(sl + o, xl);
             ldv<V>(sh + o, xh);
-            {
-                float e[V];
-                ldv<V>(sc + FS + o, e);
+            ldv<V>(sc + FS + o, e);
 #pragma unroll
-                for (int v = 0; v < V; v++) sum[v] = e[v] * e[v];
+            for (int v = 0; v < V; v++) sum[v] = e[v] * e[v];
 #pragma unroll
-                for (int j = 2; j < NF; j++) {
-                    ldv<V>(sc + j * FS + o, e);
+            for (int j = 2; j < NF; j++) {
+                ldv<V>(sc + j * FS + o, e);
 #pragma unroll
-                    for (int v = 0; v < V; v++) sum[v] = fmaf(e[v], e[v], sum[v]);
-                }
+                for (int v = 0; v < V; v++) sum[v] = fmaf(e[v], e[v], sum[v]);
             }
-            zsum<V>(c, lane, sz);
-            float w[V];
+            zsum<V>(c[k + 1], lane, sz);
 #pragma unroll
             for (int v = 0; v < V; v++) {
-                const float lap = lap3<UNIT>(xh[v] + xl[v], cu[v] + cd[v], sz[v], c[v], q);
-                const float dm = c[v] - q.Cm, da = c[v] - q.Ca, db = c[v] - q.Cb;
+                const float cc = c[k + 1][v];
+                const float lap = lap3<UNIT>(xh[v] + xl[v], c[k][v] + c[k + 2][v], sz[v], cc, q);
+                const float dm = cc - q.Cm, da = cc - q.Ca, db = cc - q.Cb;
                 float s = fmaf(q.B * dm, dm * dm, q.negA * dm);
                 s = fmaf(q.Da * da, da * da, s);
                 s = fmaf(q.Db * db, db * db, s);
                 s = fmaf(-q.g * da, sum[v], s);
-                w[v] = fmaf(-q.kappa, lap, s);
+                w[k][v] = fmaf(-q.kappa, lap, s);
             }
-            stv<V>(wd + (r + 1) * Z + z0, w);
         }
     };
 
-    // Plane x, rows ty*RT .. ty*RT+RT-1 (ostwald.cpp:103-120):
+    // Plane x on this warp's rows r0 .. r0+RT-1 (ostwald.cpp:103-120), from
+    // wa = w(x-1), wb = w(x), wc = w(x+1):
     //   C'   = C + dt*D*lap w
     //   e_j' = e_j - dt*L*(-g*(C-Ca)^2 + delta*e_j^3 + eps*e_j*(sum - e_j^2) - kappa*lap e_j)
-    auto update = [&](int x) {
+    auto update = [&](int x, const float (&wa)[RT + 2][V], const float (&wb)[RT + 2][V],
+                      const float (&wc)[RT + 2][V]) {
         const float* sl = slot(x - 1);
         const float* sc = slot(x);
         const float* sh = slot(x + 1);
-        const float* wm = wslot(x - 1);
-        const float* w0 = wslot(x);
-        const float* wp = wslot(x + 1);
-        const int r0 = ty * RT;
-        // columns of rows r0-1 .. r0+RT: w(x) and every order parameter at plane x
-        float wc[RT + 2][V], ec[NF - 1][RT + 2][V];
+        // every order parameter at plane x on rows r0-1 .. r0+RT
+        float ec[NF - 1][RT + 2][V];
 #pragma unroll
-        for (int k = 0; k < RT + 2; k++) {
-            ldv<V>(w0 + (r0 + k) * Z + z0, wc[k]);
+        for (int k = 0; k < RT + 2; k++)
 #pragma unroll
             for (int j = 1; j < NF; j++) ldv<V>(sc + j * FS + (r0 + k + 1) * Z + z0, ec[j - 1][k]);
-        }
         float* dst = sout + (long long)x * g.YZ + (long long)(y0 + r0) * Z + z0;
 #pragma unroll
         for (int k = 0; k < RT; k++) {
             const bool inside = y0 + r0 + k < g.Y;
-            const int o = (r0 + k + 2) * Z + z0;   // ring row of update row r0+k
+            const int o = (r0 + k + 2) * Z + z0;   // slot row of row r0+k
             float a[V], b[V], sz[V], C[V], out[V];
-            ldv<V>(wm + (r0 + k + 1) * Z + z0, a);
-            ldv<V>(wp + (r0 + k + 1) * Z + z0, b);
             ldv<V>(sc + o, C);
-            zsum<V>(wc[k + 1], lane, sz);
+            zsum<V>(wb[k + 1], lane, sz);
 #pragma unroll
             for (int v = 0; v < V; v++) {
-                const float lap = lap3<UNIT>(a[v] + b[v], wc[k][v] + wc[k + 2][v], sz[v], wc[k + 1][v], q);
+                const float lap =
+                    lap3<UNIT>(wa[k + 1][v] + wc[k + 1][v], wb[k][v] + wb[k + 2][v], sz[v], wb[k + 1][v], q);
                 out[v] = fmaf(q.dtD, lap, C[v]);
             }
             if (inside) stv<V>(dst + (long long)k * Z, out);
@@ -257,21 +250,34 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
     // warm-up: w(xs-1) and w(xs) from planes xs-2 .. xs+1.  Whether to stop
     // is decided block-wide at a barrier (__syncthreads_or), so every thread
     // leaves the loop at the same point.
+    float wA[RT + 2][V], wB[RT + 2][V], wC[RT + 2][V];
     bool bad = false;
     for (int pl = x_first; pl <= xs + 1; pl++) bad |= !arrived(pl);
-    compute_w(xs - 1);
-    compute_w(xs);
+    compute_w(xs - 1, wA);
+    compute_w(xs, wB);
     bool stop = __syncthreads_or(bad);
     if (!stop && t == 0 && x_first + D <= x_last) fill(issued = x_first + D);   // the slot of xs-2 is free
-    for (int x = xs; x < xe && !stop; x++) {
-        bad = !arrived(x + 2);
-        compute_w(x + 1);
-        stop = __syncthreads_or(bad);
-        if (stop) break;
-        update(x);
-        __syncthreads();
-        // the slot of plane x-1 and the w plane of x-1 are free now
+
+    // One plane: w(x+1) into wc, then plane x.  (A failed wait computes and
+    // stores garbage for this plane; the error word reports the step.)
+    auto iter = [&](int x, const float (&wa)[RT + 2][V], const float (&wb)[RT + 2][V], float (&wc)[RT + 2][V]) {
+        const bool late = !arrived(x + 2);
+        compute_w(x + 1, wc);
+        update(x, wa, wb, wc);
+        if (__syncthreads_or(late)) return false;
+        // the slot of plane x-1 is free now
         if (t == 0 && x - 1 + D <= x_last) fill(issued = x - 1 + D);
+        return true;
+    };
+    int x = xs;
+    while (!stop) {
+        if (x >= xe) break;
+        if (!iter(x, wA, wB, wC)) { stop = true; break; }
+        if (++x >= xe) break;
+        if (!iter(x, wB, wC, wA)) { stop = true; break; }
+        if (++x >= xe) break;
+        if (!iter(x, wC, wA, wB)) { stop = true; break; }
+        ++x;
     }
     if (stop && t == 0) {
         atomicExch(err, 1);
@@ -280,66 +286,61 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
     }
 }
 
-// Kernel shapes per row length: rows per warp and warps, ring depth.
-template <int V> struct OstShape;
-template <> struct OstShape<1> { static constexpr int TY = 8, RT = 2, D = 6; };
-template <> struct OstShape<2> { static constexpr int TY = 8, RT = 2, D = 6; };
-template <> struct OstShape<4> { static constexpr int TY = 8, RT = 1, D = 5; };
+// The instance for rows of 32*V cells and N fields: warps, rows per warp and
+// ring depth of its shape.
+struct OstKernel {
+    const void* fn;
+    int ty, rt, d;
+};
 
-template <int V, int NF>
-static const void* ost3_fn(bool unit)
+template <int V, int TY, int RT, int D>
+static OstKernel ost3_k(int N, bool unit)
 {
-    using S = OstShape<V>;
-    return unit ? (const void*)&ost3_stream_f32<V, S::TY, S::RT, NF, S::D, true>
-                : (const void*)&ost3_stream_f32<V, S::TY, S::RT, NF, S::D, false>;
+    OstKernel k{nullptr, TY, RT, D};
+    if (N == 2) k.fn = unit ? (const void*)&ost3_stream_f32<V, TY, RT, 2, D, true>
+                            : (const void*)&ost3_stream_f32<V, TY, RT, 2, D, false>;
+    if (N == 3) k.fn = unit ? (const void*)&ost3_stream_f32<V, TY, RT, 3, D, true>
+                            : (const void*)&ost3_stream_f32<V, TY, RT, 3, D, false>;
+    if (N == 4) k.fn = unit ? (const void*)&ost3_stream_f32<V, TY, RT, 4, D, true>
+                            : (const void*)&ost3_stream_f32<V, TY, RT, 4, D, false>;
+    return k;
 }
 
-template <int V>
-static const void* ost3_pick_n(int N, bool unit)
+// Measured on 256x128x64 x 2 fields (us per step; warps, rows per warp,
+// ring depth): 10.7 (4, 4, 6), 10.9 (4, 4, 5), 11.0 (8, 4, 5) and (4, 8, 5),
+// 12.1 (8, 2, 6), 12.6 (2, 8, 6), 15.6 (8, 1, 6); the same step with w in a
+// shared-memory ring and a barrier between the two halves: 12.5.
+static OstKernel ost3_pick(int V, int N, bool unit)
 {
-    if (N == 2) return ost3_fn<V, 2>(unit);
-    if (N == 3) return ost3_fn<V, 3>(unit);
-    if (N == 4) return ost3_fn<V, 4>(unit);
-    return nullptr;
-}
-
-template <int V>
-static size_t ost3_smem(int N)
-{
-    using S = OstShape<V>;
-    constexpr int Z = 32 * V, R = S::TY * S::RT;
-    return sizeof(float) * ((size_t)S::D * N * (R + 4) * Z + 3 * (R + 2) * Z) + sizeof(uint64_t) * S::D;
-}
-
-static int ost3_rows(int V)
-{
-    if (V == 1) return OstShape<1>::TY * OstShape<1>::RT;
-    if (V == 2) return OstShape<2>::TY * OstShape<2>::RT;
-    return OstShape<4>::TY * OstShape<4>::RT;
+    if (V == 1) return ost3_k<1, 8, 2, 6>(N, unit);
+    if (V == 4) return ost3_k<4, 4, 2, 5>(N, unit);
+    return ost3_k<2, 4, 4, 6>(N, unit);
 }
 
 bool ost3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
 {
     if (d.dtype != MMSP_GPU_F32 || g.dim != 3 || d.fields < 2 || d.fields > 4) return false;
     if (g.Z != 32 && g.Z != 64 && g.Z != 128) return false;
-    return g.Y >= ost3_rows(g.Z / 32) + 4 && g.X >= 4;
+    const OstKernel k = ost3_pick(g.Z / 32, d.fields, true);
+    return g.Y >= k.ty * k.rt + 4 && g.X >= 4;
 }
 
 cudaError_t plan_ost3_stream(const mmsp_gpu_desc& d, const Geom& g, const Coeffs& c, StepPlan* p)
 {
     const int V = g.Z / 32;
     const int N = d.fields;
-    p->fn = V == 1 ? ost3_pick_n<1>(N, c.unit_w) : V == 2 ? ost3_pick_n<2>(N, c.unit_w) : ost3_pick_n<4>(N, c.unit_w);
-    p->smem = V == 1 ? ost3_smem<1>(N) : V == 2 ? ost3_smem<2>(N) : ost3_smem<4>(N);
-    p->block = dim3(32 * (V == 1 ? OstShape<1>::TY : V == 2 ? OstShape<2>::TY : OstShape<4>::TY), 1, 1);
-    if (!p->fn) return cudaErrorInvalidConfiguration;
+    const OstKernel k = ost3_pick(V, N, c.unit_w);
+    if (!k.fn) return cudaErrorInvalidConfiguration;
+    const int R = k.ty * k.rt;
+    p->fn = k.fn;
+    p->smem = sizeof(float) * (size_t)k.d * N * (R + 4) * g.Z + sizeof(uint64_t) * k.d;
+    p->block = dim3(32 * k.ty, 1, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fn, (int)p->block.x, p->smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    const int R = ost3_rows(V);
     const int strips = (g.Y + R - 1) / R;
     // one wave: strips * segments <= resident blocks, segments >= 1
     const long long slots = (long long)sm_count() * per_sm;
