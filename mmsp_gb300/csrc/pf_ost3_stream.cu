@@ -40,45 +40,73 @@ struct OstF32 {
     float Cm, Ca, Cb, negA, B, Da, Db, g, neg_g, delta, eps, kappa, dtD, dtL;
 };
 
+// A lane's V cells as NP packs: float2 pairs (V = 2, 4), whose arithmetic
+// runs in packed FP32x2 instructions (one instruction for both cells), or
+// one float (V = 1).
+template <int V> struct Pack { using T = float2; static constexpr int NP = V / 2; };
+template <> struct Pack<1> { using T = float; static constexpr int NP = 1; };
+
+static __device__ __forceinline__ float padd(float a, float b) { return a + b; }
+static __device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+static __device__ __forceinline__ float pmul(float a, float b) { return a * b; }
+static __device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+static __device__ __forceinline__ float pfma(float a, float b, float c) { return fmaf(a, b, c); }
+static __device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+template <typename T> static __device__ __forceinline__ T splat(float k);
+template <> __device__ __forceinline__ float splat<float>(float k) { return k; }
+template <> __device__ __forceinline__ float2 splat<float2>(float k) { return make_float2(k, k); }
+
 template <int V>
-static __device__ __forceinline__ void ldv(const float* p, float (&v)[V])
+static __device__ __forceinline__ void ldp(const float* p, typename Pack<V>::T (&v)[Pack<V>::NP])
 {
     if constexpr (V == 4) {
         const float4 t = *reinterpret_cast<const float4*>(p);
-        v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+        v[0] = make_float2(t.x, t.y);
+        v[1] = make_float2(t.z, t.w);
     } else if constexpr (V == 2) {
-        const float2 t = *reinterpret_cast<const float2*>(p);
-        v[0] = t.x, v[1] = t.y;
+        v[0] = *reinterpret_cast<const float2*>(p);
     } else {
         v[0] = *p;
     }
 }
 
 template <int V>
-static __device__ __forceinline__ void stv(float* p, const float (&v)[V])
+static __device__ __forceinline__ void stp(float* p, const typename Pack<V>::T (&v)[Pack<V>::NP])
 {
-    if constexpr (V == 4) *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
-    else if constexpr (V == 2) *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    if constexpr (V == 4) *reinterpret_cast<float4*>(p) = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+    else if constexpr (V == 2) *reinterpret_cast<float2*>(p) = v[0];
     else *p = v[0];
 }
 
-// sums of the two Z neighbours of each of a lane's V cells (the row wraps
-// across lanes 31 and 0)
+// Sums of the two Z neighbours of each of a lane's V cells (the row wraps
+// across lanes 31 and 0).  Scalar adds, so no pairs are built before them.
 template <int V>
-static __device__ __forceinline__ void zsum(const float (&c)[V], int lane, float (&s)[V])
+static __device__ __forceinline__ void zsum(const typename Pack<V>::T (&c)[Pack<V>::NP], int lane,
+                                            typename Pack<V>::T (&s)[Pack<V>::NP])
 {
-    const float left = __shfl_sync(0xffffffffu, c[V - 1], (lane + 31) & 31);
-    const float right = __shfl_sync(0xffffffffu, c[0], (lane + 1) & 31);
+    constexpr int NP = Pack<V>::NP;
+    if constexpr (V == 1) {
+        const float left = __shfl_sync(0xffffffffu, c[0], (lane + 31) & 31);
+        const float right = __shfl_sync(0xffffffffu, c[0], (lane + 1) & 31);
+        s[0] = left + right;
+    } else {
+        const float left = __shfl_sync(0xffffffffu, c[NP - 1].y, (lane + 31) & 31);
+        const float right = __shfl_sync(0xffffffffu, c[0].x, (lane + 1) & 31);
 #pragma unroll
-    for (int v = 0; v < V; v++) s[v] = (v == 0 ? left : c[v - 1]) + (v == V - 1 ? right : c[v + 1]);
+        for (int i = 0; i < NP; i++) {
+            const float lo = i == 0 ? left : c[i - 1].y;
+            const float hi = i == NP - 1 ? right : c[i + 1].x;
+            s[i] = make_float2(lo + c[i].y, c[i].x + hi);
+        }
+    }
 }
 
 // wx*sx + wy*sy + wz*sz - 2(wx+wy+wz)*c from the neighbour sums along each axis
-template <bool UNIT>
-static __device__ __forceinline__ float lap3(float sx, float sy, float sz, float c, const OstF32& q)
+template <bool UNIT, typename T>
+static __device__ __forceinline__ T lap3(T sx, T sy, T sz, T c, const OstF32& q)
 {
-    if (UNIT) return fmaf(-6.0f, c, (sx + sy) + sz);
-    return fmaf(q.wx, sx, fmaf(q.wy, sy, fmaf(q.wz, sz, -q.w2 * c)));
+    if (UNIT) return pfma(splat<T>(-6.0f), c, padd(padd(sx, sy), sz));
+    return pfma(splat<T>(q.wx), sx, pfma(splat<T>(q.wy), sy, pfma(splat<T>(q.wz), sz, pmul(splat<T>(-q.w2), c))));
 }
 
 // V = Z/32 cells per lane, TY warps, RT update rows per warp (R = TY*RT rows
@@ -91,6 +119,8 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
     constexpr int Z = 32 * V, R = TY * RT, RR = R + 4;
     constexpr int FS = RR * Z;        // floats of one field's rows in a slot
     constexpr int SS = NF * FS;       // floats of a slot
+    constexpr int NP = Pack<V>::NP;
+    using T = typename Pack<V>::T;
     static_assert(D >= 5 && NF >= 2, "ring depth, fields");
     extern __shared__ __align__(128) unsigned char sm[];
     float* ring = reinterpret_cast<float*>(sm);
@@ -143,39 +173,39 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
     // with sum the squares of the order parameters; planes xp-1, xp, xp+1
     // staged.  The rows either side of the warp's own are computed again by
     // the neighbouring warps, so w never leaves registers.
-    auto compute_w = [&](int xp, float (&w)[RT + 2][V]) {
+    auto compute_w = [&](int xp, T (&w)[RT + 2][NP]) {
         const float* sl = slot(xp - 1);
         const float* sc = slot(xp);
         const float* sh = slot(xp + 1);
-        float c[RT + 4][V];   // C(xp) on rows r0-2 .. r0+RT+1 (slot rows r0 .. r0+RT+3)
+        T c[RT + 4][NP];   // C(xp) on rows r0-2 .. r0+RT+1 (slot rows r0 .. r0+RT+3)
 #pragma unroll
-        for (int k = 0; k < RT + 4; k++) ldv<V>(sc + (r0 + k) * Z + z0, c[k]);
+        for (int k = 0; k < RT + 4; k++) ldp<V>(sc + (r0 + k) * Z + z0, c[k]);
 #pragma unroll
         for (int k = 0; k < RT + 2; k++) {   // row r0-1+k
             const int o = (r0 + 1 + k) * Z + z0;
-            float xh[V], xl[V], sz[V], sum[V], e[V];
-            ldv<V>(sl + o, xl);
-            ldv<V>(sh + o, xh);
-            ldv<V>(sc + FS + o, e);
+            T xh[NP], xl[NP], sz[NP], sum[NP], e[NP];
+            ldp<V>(sl + o, xl);
+            ldp<V>(sh + o, xh);
+            ldp<V>(sc + FS + o, e);
 #pragma unroll
-            for (int v = 0; v < V; v++) sum[v] = e[v] * e[v];
+            for (int i = 0; i < NP; i++) sum[i] = pmul(e[i], e[i]);
 #pragma unroll
             for (int j = 2; j < NF; j++) {
-                ldv<V>(sc + j * FS + o, e);
+                ldp<V>(sc + j * FS + o, e);
 #pragma unroll
-                for (int v = 0; v < V; v++) sum[v] = fmaf(e[v], e[v], sum[v]);
+                for (int i = 0; i < NP; i++) sum[i] = pfma(e[i], e[i], sum[i]);
             }
             zsum<V>(c[k + 1], lane, sz);
 #pragma unroll
-            for (int v = 0; v < V; v++) {
-                const float cc = c[k + 1][v];
-                const float lap = lap3<UNIT>(xh[v] + xl[v], c[k][v] + c[k + 2][v], sz[v], cc, q);
-                const float dm = cc - q.Cm, da = cc - q.Ca, db = cc - q.Cb;
-                float s = fmaf(q.B * dm, dm * dm, q.negA * dm);
-                s = fmaf(q.Da * da, da * da, s);
-                s = fmaf(q.Db * db, db * db, s);
-                s = fmaf(-q.g * da, sum[v], s);
-                w[k][v] = fmaf(-q.kappa, lap, s);
+            for (int i = 0; i < NP; i++) {
+                const T cc = c[k + 1][i];
+                const T lap = lap3<UNIT>(padd(xh[i], xl[i]), padd(c[k][i], c[k + 2][i]), sz[i], cc, q);
+                const T dm = padd(cc, splat<T>(-q.Cm)), da = padd(cc, splat<T>(-q.Ca)), db = padd(cc, splat<T>(-q.Cb));
+                T r = pfma(pmul(splat<T>(q.B), dm), pmul(dm, dm), pmul(splat<T>(q.negA), dm));
+                r = pfma(pmul(splat<T>(q.Da), da), pmul(da, da), r);
+                r = pfma(pmul(splat<T>(q.Db), db), pmul(db, db), r);
+                r = pfma(pmul(splat<T>(-q.g), da), sum[i], r);
+                w[k][i] = pfma(splat<T>(-q.kappa), lap, r);
             }
         }
     };
@@ -184,57 +214,55 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
     // wa = w(x-1), wb = w(x), wc = w(x+1):
     //   C'   = C + dt*D*lap w
     //   e_j' = e_j - dt*L*(-g*(C-Ca)^2 + delta*e_j^3 + eps*e_j*(sum - e_j^2) - kappa*lap e_j)
-    auto update = [&](int x, const float (&wa)[RT + 2][V], const float (&wb)[RT + 2][V],
-                      const float (&wc)[RT + 2][V]) {
+    auto update = [&](int x, const T (&wa)[RT + 2][NP], const T (&wb)[RT + 2][NP], const T (&wc)[RT + 2][NP]) {
         const float* sl = slot(x - 1);
         const float* sc = slot(x);
         const float* sh = slot(x + 1);
         // every order parameter at plane x on rows r0-1 .. r0+RT
-        float ec[NF - 1][RT + 2][V];
+        T ec[NF - 1][RT + 2][NP];
 #pragma unroll
         for (int k = 0; k < RT + 2; k++)
 #pragma unroll
-            for (int j = 1; j < NF; j++) ldv<V>(sc + j * FS + (r0 + k + 1) * Z + z0, ec[j - 1][k]);
+            for (int j = 1; j < NF; j++) ldp<V>(sc + j * FS + (r0 + k + 1) * Z + z0, ec[j - 1][k]);
         float* dst = sout + (long long)x * g.YZ + (long long)(y0 + r0) * Z + z0;
 #pragma unroll
         for (int k = 0; k < RT; k++) {
             const bool inside = y0 + r0 + k < g.Y;
             const int o = (r0 + k + 2) * Z + z0;   // slot row of row r0+k
-            float a[V], b[V], sz[V], C[V], out[V];
-            ldv<V>(sc + o, C);
+            T a[NP], b[NP], sz[NP], C[NP], out[NP], sum[NP], t1[NP];
+            ldp<V>(sc + o, C);
             zsum<V>(wb[k + 1], lane, sz);
 #pragma unroll
-            for (int v = 0; v < V; v++) {
-                const float lap =
-                    lap3<UNIT>(wa[k + 1][v] + wc[k + 1][v], wb[k][v] + wb[k + 2][v], sz[v], wb[k + 1][v], q);
-                out[v] = fmaf(q.dtD, lap, C[v]);
+            for (int i = 0; i < NP; i++) {
+                const T lap = lap3<UNIT>(padd(wa[k + 1][i], wc[k + 1][i]), padd(wb[k][i], wb[k + 2][i]), sz[i],
+                                         wb[k + 1][i], q);
+                out[i] = pfma(splat<T>(q.dtD), lap, C[i]);
             }
-            if (inside) stv<V>(dst + (long long)k * Z, out);
-            float sum[V], t1[V];
+            if (inside) stp<V>(dst + (long long)k * Z, out);
 #pragma unroll
-            for (int v = 0; v < V; v++) {
-                sum[v] = ec[0][k + 1][v] * ec[0][k + 1][v];
+            for (int i = 0; i < NP; i++) {
+                sum[i] = pmul(ec[0][k + 1][i], ec[0][k + 1][i]);
 #pragma unroll
-                for (int j = 1; j < NF - 1; j++) sum[v] = fmaf(ec[j][k + 1][v], ec[j][k + 1][v], sum[v]);
-                const float da = C[v] - q.Ca;
-                t1[v] = q.neg_g * (da * da);
+                for (int j = 1; j < NF - 1; j++) sum[i] = pfma(ec[j][k + 1][i], ec[j][k + 1][i], sum[i]);
+                const T da = padd(C[i], splat<T>(-q.Ca));
+                t1[i] = pmul(splat<T>(q.neg_g), pmul(da, da));
             }
 #pragma unroll
             for (int j = 1; j < NF; j++) {
-                const float(&e)[V] = ec[j - 1][k + 1];
-                ldv<V>(sl + j * FS + o, a);
-                ldv<V>(sh + j * FS + o, b);
+                const T(&e)[NP] = ec[j - 1][k + 1];
+                ldp<V>(sl + j * FS + o, a);
+                ldp<V>(sh + j * FS + o, b);
                 zsum<V>(e, lane, sz);
 #pragma unroll
-                for (int v = 0; v < V; v++) {
-                    const float lap =
-                        lap3<UNIT>(a[v] + b[v], ec[j - 1][k][v] + ec[j - 1][k + 2][v], sz[v], e[v], q);
-                    float s = fmaf(q.delta * e[v], e[v] * e[v], t1[v]);
-                    s = fmaf(q.eps * e[v], fmaf(-e[v], e[v], sum[v]), s);
-                    s = fmaf(-q.kappa, lap, s);
-                    out[v] = fmaf(-q.dtL, s, e[v]);
+                for (int i = 0; i < NP; i++) {
+                    const T lap = lap3<UNIT>(padd(a[i], b[i]), padd(ec[j - 1][k][i], ec[j - 1][k + 2][i]), sz[i], e[i], q);
+                    const T e2 = pmul(e[i], e[i]);
+                    T r = pfma(pmul(splat<T>(q.delta), e[i]), e2, t1[i]);
+                    r = pfma(pmul(splat<T>(q.eps), e[i]), pfma(splat<T>(-1.0f), e2, sum[i]), r);
+                    r = pfma(splat<T>(-q.kappa), lap, r);
+                    out[i] = pfma(splat<T>(-q.dtL), r, e[i]);
                 }
-                if (inside) stv<V>(dst + (long long)j * cells + (long long)k * Z, out);
+                if (inside) stp<V>(dst + (long long)j * cells + (long long)k * Z, out);
             }
         }
     };
@@ -250,7 +278,7 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
     // warm-up: w(xs-1) and w(xs) from planes xs-2 .. xs+1.  Whether to stop
     // is decided block-wide at a barrier (__syncthreads_or), so every thread
     // leaves the loop at the same point.
-    float wA[RT + 2][V], wB[RT + 2][V], wC[RT + 2][V];
+    T wA[RT + 2][NP], wB[RT + 2][NP], wC[RT + 2][NP];
     bool bad = false;
     for (int pl = x_first; pl <= xs + 1; pl++) bad |= !arrived(pl);
     compute_w(xs - 1, wA);
@@ -260,7 +288,7 @@ ost3_stream_f32(const float* __restrict__ sin, float* __restrict__ sout, Geom g,
 
     // One plane: w(x+1) into wc, then plane x.  (A failed wait computes and
     // stores garbage for this plane; the error word reports the step.)
-    auto iter = [&](int x, const float (&wa)[RT + 2][V], const float (&wb)[RT + 2][V], float (&wc)[RT + 2][V]) {
+    auto iter = [&](int x, const T (&wa)[RT + 2][NP], const T (&wb)[RT + 2][NP], T (&wc)[RT + 2][NP]) {
         const bool late = !arrived(x + 2);
         compute_w(x + 1, wc);
         update(x, wa, wb, wc);
