@@ -126,7 +126,8 @@ ac3_stream_f32(const float* __restrict__ ein, float* __restrict__ eout, Geom g, 
                 for (int f = 0; f < N; f++) {
                     const float* base = ein + (long long)f * cells + plane + z;
                     float* dst = dst0 + f * chunk + z;
-                    for (int r = ty; r < RR; r += TY) cp_async4(dst + r * Z, base + (long long)wrapi(y0 - 1 + r, g.Y) * Z);
+                    for (int r = ty; r < RR; r += TY)   // (g.Y >= R + 2)
+                        cp_async4(dst + r * Z, base + (long long)wrap_near(y0 - 1 + r, g.Y) * Z);
                 }
             cp_async_arrive(bar);
         }

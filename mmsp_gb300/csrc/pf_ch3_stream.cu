@@ -191,7 +191,7 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
             if (STALL) return;   // no copies and no arrivals: the waits run out
             if (real)
                 for (int i = 0; i < RR; i++) {
-                    const float* row = base + (long long)wrapi(y0 - 2 + i, g.Y) * Z;
+                    const float* row = base + (long long)wrap_near(y0 - 2 + i, g.Y) * Z;   // g.Y >= R + 4
                     if (PAD) {   // 4-byte copies: odd rows break 8-byte alignment; cell Z is cell 0
                         cp_async4(dst + i * ZS + z0, row + z0);
                         cp_async4(dst + i * ZS + z0 + 1, row + (z0 + 1 == Z ? 0 : z0 + 1));
@@ -411,7 +411,7 @@ static const void* pick_mu(bool ch, bool unit)
 // 32..512 cells in powers of two (with its STALL form), else the runtime-row
 // instance whose thread bound covers Z / 2 (no STALL form: nullptr).
 template <bool STALL>
-static const void* pick_stream(int Z, bool ch, bool unit)
+static const void* pick_stream(int Z, int Y, bool ch, bool unit)
 {
     switch (Z) {
     case 32: return pick_mu<32, 32, 1, STALL, true>(ch, unit);
@@ -425,7 +425,11 @@ static const void* pick_stream(int Z, bool ch, bool unit)
     const int T = ch3_threads(Z, 2);
     if (Z % 2) return T <= 128 ? pick_mu<0, 128, 2, false, false, true>(ch, unit)
                                : pick_mu<0, 256, 2, false, false, true>(ch, unit);
-    const bool bulk = Z % 4 == 0;
+    // Bulk copies need 16-byte aligned rows, or, for rows of 2 mod 4 cells,
+    // pieces that start on even rows and span an even number of rows: the
+    // strip starts on an even row (R is even) and the wrapped pieces do
+    // where Y is even.
+    const bool bulk = Z % 4 == 0 || (Y % 2 == 0 && kStreamR % 2 == 0);
     if (T <= 128) return bulk ? pick_mu<0, 128, 2, false, true>(ch, unit) : pick_mu<0, 128, 2, false, false>(ch, unit);
     return bulk ? pick_mu<0, 256, 2, false, true>(ch, unit) : pick_mu<0, 256, 2, false, false>(ch, unit);
 }
@@ -435,8 +439,8 @@ cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     const Coeffs c = make_coeffs(d);
     const int V = cells_per_thread(g.Z);
     const int threads = ch3_threads(g.Z, V);
-    p->fn = pick_stream<false>(g.Z, d.model == MMSP_GPU_CH, c.unit_w);
-    p->fn2 = pick_stream<true>(g.Z, d.model == MMSP_GPU_CH, c.unit_w);   // the failure-detection test's form
+    p->fn = pick_stream<false>(g.Z, g.Y, d.model == MMSP_GPU_CH, c.unit_w);
+    p->fn2 = pick_stream<true>(g.Z, g.Y, d.model == MMSP_GPU_CH, c.unit_w);   // the failure-detection test's form
     p->smem = ch3_smem(kStreamR, g.Z, V);
     p->block = dim3(threads, 1, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);

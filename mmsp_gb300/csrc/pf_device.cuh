@@ -211,6 +211,12 @@ static __device__ __forceinline__ int wrapi(int v, int n)
     return r < 0 ? r + n : r;
 }
 
+// v mod n for v in [-n, 2n): one compare and add instead of a division.
+static __device__ __forceinline__ int wrap_near(int v, int n)
+{
+    return v < 0 ? v + n : (v >= n ? v - n : v);
+}
+
 // Model constants narrowed to the state type; padded axes X, Y, Z take the
 // last `dim` real-axis weights.
 template <typename T>

@@ -368,7 +368,7 @@ def test_full_3d_ac_128_n8(gpu):
 # last real lane), down to lane 0 alone.
 STREAM_SHAPES = [(16, 24, 64), (20, 13, 32), (5, 12, 96), (3, 40, 256), (33, 17, 128), (1, 16, 32),
                  (7, 13, 243), (4, 12, 33), (6, 20, 50), (3, 14, 198), (2, 12, 300), (2, 12, 301), (3, 17, 190),
-                 (4, 12, 36), (3, 12, 63), (2, 13, 65)]
+                 (4, 12, 36), (3, 12, 63), (2, 13, 65), (3, 22, 242)]
 
 
 @pytest.mark.parametrize("shape", STREAM_SHAPES, ids=["x".join(map(str, s)) for s in STREAM_SHAPES])
