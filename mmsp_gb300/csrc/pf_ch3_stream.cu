@@ -10,7 +10,9 @@
 // For every plane the block's R+4 rows (2 halo rows on each side, wrapped
 // periodically) arrive in shared memory on an mbarrier ring, several planes
 // ahead of the one being computed: by cp.async.bulk where rows are 16-byte
-// multiples, by per-thread 8-byte cp.async otherwise.  Each thread keeps its
+// multiples, or rows of 2 mod 4 cells on an even number of rows (every
+// copied piece then starts on an even row and spans an even number of
+// rows), by per-thread 8-byte cp.async otherwise.  Each thread keeps its
 // cells of c for planes x, x+1, x+2 and of mu for x-1, x, x+1 in registers:
 // Y neighbours are neighbouring registers, X neighbours the neighbouring
 // planes' registers, Z neighbours inside a thread are registers, Z
@@ -120,10 +122,11 @@ static size_t ch3_smem(int R, int Z, int V)
 // it only through MMSP_GPU_TEST_STALL_LAUNCHES.
 // ZT: the row length when it is a compile-time constant (32..512 in powers
 // of two, ZT / V = TM threads), 0 when it is taken from the grid
-// (blockDim.x = ch3_threads(Z, V) <= TM).  BULK: rows are 16-byte multiples
-// and thread 0 stages each plane with cp.async.bulk (one arrival,
-// transaction-counted); otherwise every thread copies its cells with 4- or
-// 8-byte cp.async and arrives when they land.  PAD: odd rows of two cells
+// (blockDim.x = ch3_threads(Z, V) <= TM).  BULK: the pieces of a plane's
+// strip are 16-byte aligned (rows of a multiple of 4 cells, or of 2 mod 4
+// cells with Y even) and thread 0 stages each plane with cp.async.bulk (one
+// arrival, transaction-counted); otherwise every thread copies its cells
+// with 4- or 8-byte cp.async and arrives when they land.  PAD: odd rows of two cells
 // per thread: shared rows hold Z + 1 cells, the extra one a copy of the
 // row's cell 0 (the periodic right neighbour of the last cell), the last
 // thread takes mu of cell 0 from the warp-end exchange for its second cell,
