@@ -885,6 +885,8 @@ CASES = {
     "ch3d_f64": (SHAPE, 1, np.float64, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
     "ch3d_f64c": (SHAPE, 1, np.float64, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB, contract=True)),
     "ch3d208_f32": ((208, 208, 208), 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
+    "ch3d243_f32": ((243, 243, 243), 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
+    "ac3d74_n14_f32": ((74, 74, 74), 14, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ch2d_f64": ((256, 256), 1, np.float64, "ch", dict(dt=0.005, kappa=1.0, mobility=1.0)),
     "ac3d_f32": ((128, 128, 128), 8, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
