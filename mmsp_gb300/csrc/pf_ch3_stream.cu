@@ -104,13 +104,13 @@ static __device__ __forceinline__ VT lap_v(VT sx, VT sy, VT sz, VT c, const F32C
 // Threads of a block for rows of Z cells, V per thread: whole warps.
 static int ch3_threads(int Z, int V) { return ((Z + V - 1) / V + 31) / 32 * 32; }
 
-// Shared memory: kRing slots of (R+4) x ZS floats (ZS = Z, or Z + 1 for odd
-// rows of two cells per thread), the warp-end mu buffers
-// [parity][warp][side][R], then kRing mbarriers.
-static size_t ch3_smem(int R, int Z, int V)
+// Shared memory: kRing slots of (R+4) x ZS floats (ZS the shared row
+// stride: Z, Z + 1 for odd rows of two cells per thread, or the instance's
+// full TM*V row), the warp-end mu buffers [parity][warp][side][R], then
+// kRing mbarriers.
+static size_t ch3_smem(int R, int Z, int V, int ZS)
 {
     const int warps = ch3_threads(Z, V) / 32;
-    const int ZS = V == 2 && Z % 2 ? Z + 1 : Z;
     return sizeof(float) * (size_t)kRing * (R + 4) * ZS + sizeof(float) * 2 * warps * 2 * R +
            sizeof(uint64_t) * kRing;
 }
@@ -126,12 +126,14 @@ static size_t ch3_smem(int R, int Z, int V)
 // strip are 16-byte aligned (rows of a multiple of 4 cells, or of 2 mod 4
 // cells with Y even) and thread 0 stages each plane with cp.async.bulk (one
 // arrival, transaction-counted); otherwise every thread copies its cells
-// with 4- or 8-byte cp.async and arrives when they land.  PAD: odd rows of two cells
-// per thread: shared rows hold Z + 1 cells, the extra one a copy of the
-// row's cell 0 (the periodic right neighbour of the last cell), the last
-// thread takes mu of cell 0 from the warp-end exchange for its second cell,
-// and stores are 4-byte (odd rows break 8-byte alignment).
-template <int R, int ZT, int TM, int V, int MODEL, bool UNIT, bool STALL, bool BULK, bool PAD>
+// with 4- or 8-byte cp.async and arrives when they land.  PAD: odd rows of
+// two cells per thread: shared rows hold Z + 1 cells, the extra one a copy
+// of the row's cell 0 (the periodic right neighbour of the last cell), the
+// last thread takes mu of cell 0 from the warp-end exchange for its second
+// cell, and stores are 4-byte (odd rows break 8-byte alignment).  WIDE
+// (with per-thread copies): shared rows are TM*V floats apart whatever Z
+// is, so shared offsets are compile-time.
+template <int R, int ZT, int TM, int V, int MODEL, bool UNIT, bool STALL, bool BULK, bool PAD, bool WIDE>
 __global__ void __launch_bounds__(TM, TM <= 128 ? PF_CH3_MINB : (V == 1 && TM == 256 ? 2 : 1))
 ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, F32Coef q, int planes,
                int* __restrict__ err)
@@ -139,8 +141,11 @@ ch3_stream_f32(const float* __restrict__ cin, float* __restrict__ cout, Geom g, 
     constexpr int RR = R + 4;
     static_assert(TM % 32 == 0 && R % 4 == 0 && (!ZT || ZT == TM * V), "row split");
     static_assert(!PAD || (V == 2 && !ZT && !BULK), "odd rows: runtime rows, per-thread copies");
+    static_assert(!WIDE || (!ZT && !BULK), "full-width shared rows: runtime rows, per-thread copies");
     const int Z = ZT ? ZT : g.Z;
-    const int ZS = PAD ? Z + 1 : Z;      // shared-memory row stride
+    // shared-memory row stride: a compile-time TM*V for WIDE instances, so
+    // every shared address in the plane loop is an immediate offset
+    const int ZS = WIDE ? TM * V : PAD ? Z + 1 : Z;
     const int W = ZT ? TM / 32 : (int)(blockDim.x >> 5);   // warps per block
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
@@ -400,14 +405,14 @@ bool ch3_stream_eligible(const mmsp_gpu_desc& d, const Geom& g)
            (d.model == MMSP_GPU_CH || d.model == MMSP_GPU_CH_POLY);
 }
 
-template <int ZT, int TM, int V, bool STALL, bool BULK, bool PAD = false>
+template <int ZT, int TM, int V, bool STALL, bool BULK, bool PAD = false, bool WIDE = false>
 static const void* pick_mu(bool ch, bool unit)
 {
     if (ch)
-        return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, true, STALL, BULK, PAD>
-                    : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, false, STALL, BULK, PAD>;
-    return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, true, STALL, BULK, PAD>
-                : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, false, STALL, BULK, PAD>;
+        return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, true, STALL, BULK, PAD, WIDE>
+                    : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH, false, STALL, BULK, PAD, WIDE>;
+    return unit ? (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, true, STALL, BULK, PAD, WIDE>
+                : (const void*)&ch3_stream_f32<kStreamR, ZT, TM, V, MMSP_GPU_CH_POLY, false, STALL, BULK, PAD, WIDE>;
 }
 
 // The kernel for rows of Z cells: a compile-time instance for rows of
@@ -425,16 +430,26 @@ static const void* pick_stream(int Z, int Y, bool ch, bool unit)
     default: break;
     }
     if (STALL) return nullptr;
+    // Odd rows keep full-width shared rows (WIDE: every shared offset in the
+    // plane loop an immediate; 243^3 46.5 -> 42.9 us per step, 163^3 20.9 ->
+    // 18.2).  Rows of a multiple of 4 cells, and of 2 mod 4 cells on even Y,
+    // are bulk-copied as whole strips, which needs them contiguous in shared
+    // memory (one bulk copy per full-width row measured slower: 208^3 25.7 ->
+    // 29.9 us); for 2 mod 4 cells every piece then starts on an even row (R
+    // is even, and so is Y) and spans an even number of rows.
     const int T = ch3_threads(Z, 2);
-    if (Z % 2) return T <= 128 ? pick_mu<0, 128, 2, false, false, true>(ch, unit)
-                               : pick_mu<0, 256, 2, false, false, true>(ch, unit);
-    // Bulk copies need 16-byte aligned rows, or, for rows of 2 mod 4 cells,
-    // pieces that start on even rows and span an even number of rows: the
-    // strip starts on an even row (R is even) and the wrapped pieces do
-    // where Y is even.
+    if (Z % 2) return T <= 128 ? pick_mu<0, 128, 2, false, false, true, true>(ch, unit)
+                               : pick_mu<0, 256, 2, false, false, true, true>(ch, unit);
     const bool bulk = Z % 4 == 0 || (Y % 2 == 0 && kStreamR % 2 == 0);
     if (T <= 128) return bulk ? pick_mu<0, 128, 2, false, true>(ch, unit) : pick_mu<0, 128, 2, false, false>(ch, unit);
     return bulk ? pick_mu<0, 256, 2, false, true>(ch, unit) : pick_mu<0, 256, 2, false, false>(ch, unit);
+}
+
+// The shared row stride of the instance pick_stream chooses.
+static int stream_zs(int Z)
+{
+    if (Z % 2 == 0) return Z;
+    return ch3_threads(Z, 2) <= 128 ? 256 : 512;
 }
 
 cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
@@ -444,7 +459,7 @@ cudaError_t plan_ch3_stream(const mmsp_gpu_desc& d, const Geom& g, StepPlan* p)
     const int threads = ch3_threads(g.Z, V);
     p->fn = pick_stream<false>(g.Z, g.Y, d.model == MMSP_GPU_CH, c.unit_w);
     p->fn2 = pick_stream<true>(g.Z, g.Y, d.model == MMSP_GPU_CH, c.unit_w);   // the failure-detection test's form
-    p->smem = ch3_smem(kStreamR, g.Z, V);
+    p->smem = ch3_smem(kStreamR, g.Z, V, stream_zs(g.Z));
     p->block = dim3(threads, 1, 1);
     cudaError_t e = ensure_smem(p->fn, p->smem);
     if (e == cudaSuccess && p->fn2) e = ensure_smem(p->fn2, p->smem);
