@@ -465,7 +465,8 @@ int mmsp_gpu_server_stop(mmsp_gpu_server* s);
  * a device, do not call this entry point on that device again.
  * Calls that overlap on the GPU (from several threads or streams) share the
  * scratch array and race: serialise them.  MMSP_GPU_OSTWALD (its step needs a
- * work grid beside the state), MMSP_GPU_CH_CONVEX (an iterative solve per
+ * work grid beside the state, except on the FP32 3D grids of its one-kernel
+ * step), MMSP_GPU_CH_CONVEX (an iterative solve per
  * step) and the noisy polynomial forms return MMSP_GPU_EUNSUPPORTED. */
 int mmsp_gpu_step_noalloc(const mmsp_gpu_desc* desc, const void* in, void* out, int steps,
                           void* cuda_stream);
