@@ -264,8 +264,8 @@ def other_configs(native, inputs, stream):
 def other_models(native, inputs, timed):
     """The further explicit models on the same device path: Zener pinning
     (grain growth with the particle field fixed) on 128^3 x 3 fields,
-    Ostwald ripening (composition + order parameter, two kernels per step)
-    on 256 x 128 x 64 x 2 fields (the example's 128 x 64 x 16, doubled per
+    Ostwald ripening (composition + order parameter; one kernel per step in
+    FP32, two in FP64) on 256 x 128 x 64 x 2 fields (the example's 128 x 64 x 16, doubled per
     axis) and model B (Cahn-Hilliard with thermal noise) on 1024^2, 500
     steps each in FP32 and FP64, beside the oracle (the reference's loops
     restated in C, FP64, one thread) on 2 steps."""
@@ -887,6 +887,7 @@ CASES = {
     "ch3d208_f32": ((208, 208, 208), 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
     "ch3d243_f32": ((243, 243, 243), 1, np.float32, "ch", dict(dt=DT, kappa=KAPPA, mobility=MOB)),
     "ac3d74_n14_f32": ((74, 74, 74), 14, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
+    "modelB2d_f32": ((1024, 1024), 1, np.float32, "ch_poly", dict(dt=0.01, noise=float(np.sqrt(2.0)), seed=3)),
     "ch2d_f64": ((256, 256), 1, np.float64, "ch", dict(dt=0.005, kappa=1.0, mobility=1.0)),
     "ac3d_f32": ((128, 128, 128), 8, np.float32, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
     "ac3d_f64": ((128, 128, 128), 8, np.float64, "ac", dict(dt=0.05, kappa=2.0, mobility=1.0, gamma=1.5)),
