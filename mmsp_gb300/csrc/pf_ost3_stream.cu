@@ -25,8 +25,8 @@
 //   are neighbours: the periodic wrap of the row).
 //
 // FP32 arithmetic is regrouped for throughput (neighbour sums before the
-// weights); the result is checked against the FP64 oracle with a
-// tolerance, not bitwise.  Every wait is bounded: a wait that runs out sets
+// weights) and runs on pairs of cells in packed FP32x2 instructions; the
+// result is checked against the FP64 oracle with a tolerance, not bitwise.  Every wait is bounded: a wait that runs out sets
 // the error word, and the block waits (bounded) for its copies in flight
 // and leaves.
 #include "pf_async.cuh"
